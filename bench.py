@@ -1,0 +1,341 @@
+"""Benchmark: shot-gradients per second of one FWI gradient pass.
+
+Workload (default): one stage-1 FWI iteration at 376x201, dx=dz=10 m, PML 20,
+nt=3000, dt=1 ms, 15 Hz Ricker; 38 shots 10 nodes apart, 376 surface
+receivers each (full-aperture windows); each shot runs the background +
+Born-scattered forward, the 1D optimal-transport adjoint source and the
+adjoint gradient.  Models are seeded synthetics (layered Vp 1500-4500 m/s with
+three +-10% Gaussian anomalies, Vs = Vp/1.73, Gardner rho); observed data are
+modelled on the true model, the gradient is taken on a z-smoothed start model
+with the Born perturbation = true - start.
+
+A step = one gradient pass over all 38 shots (one sfwi_run call).  `value`
+counts device time only (CUDA events on the engine's stream, inputs resident);
+`e2e` times the public API call from host buffers: per step the observed
+records are copied host->device from page-locked memory and the gradients and
+misfit are read back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# one process per GPU under torchrun: pin this process's device before any CUDA use
+if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(name="fwi-iteration-376x201-38shots-born-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
+                dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0)
+METRIC = "shot-gradients/s"
+
+# algorithmic bytes per padded cell per time step of each kernel (FP32; each
+# array read once and written once per sweep, stencil neighbours reused on
+# chip)
+KERNEL_BYTES = {
+    "k_fwd_v<born>": 60,   # read sigma(3) + sigma_s(3) + 1/rho; RMW v(2) + v_s(2)
+    "k_fwd_s<born>": 80,   # read v(2) + v_s(2) + lam, mu, bp, bs; RMW sigma(3) + sigma_s(3)
+    "k_bwd_s": 88,         # read v(2) + v_adj(2) + lam, mu; RMW sigma(3) + sigma_adj(3) + G_lam, G_mu
+    "k_bwd_v": 76,         # read sigma(3) + sigma_adj(3) + lam, mu, 1/rho; RMW v(2) + v_adj(2) + illum
+}
+SURVEY_BYTES_PER_CELL_STEP = 328  # forward 72 + reconstruction 72 + adjoint 72 + imaging 32 + Born 80
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def build_workload(w):
+    from sfwi_gb300 import synth
+    from oracle import pyoracle  # noqa: F401  (wavelet only through the package below)
+    vp, vs, rho = synth.layered_model(w["allnx"], w["allnz"], w["dx"])
+    vp0 = synth.smooth_z(vp, 10)
+    vs0 = (vp0 / 1.73).astype(np.float32)
+    rho0 = (310.0 * vp0.astype(np.float64) ** 0.25).astype(np.float32)
+    shots = synth.config_shots(w["allnx"], w["dx"], w["pml"], w["nshots"], w["spacing"])
+    sou = ricker(w["nt"], w["dt"], w["f0"])
+    return dict(vp=vp, vs=vs, rho=rho, vp0=vp0, vs0=vs0, rho0=rho0, dvp=(vp - vp0).astype(np.float32),
+                dvs=(vs - vs0).astype(np.float32), shots=shots, sou=sou)
+
+
+def ricker(nt, dt, fm):
+    """Ricker wavelet as the reference computes it (sfwi-stage1/main.cpp:251-260)."""
+    PI = np.float32(3.14159265358979)
+    fm, dt = np.float32(fm), np.float32(dt)
+    Nk = np.float32(PI * PI * fm * fm * dt * dt)
+    t0 = int(np.ceil(1.0 / float(np.float32(fm * dt))))
+    t = np.arange(nt, dtype=np.float64) - t0
+    return ((1.0 - 2.0 * float(Nk) * t * t) * np.exp(-float(Nk) * t * t)).astype(np.float32)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.samples, self.proc = [], None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = max(mx, float(s[2]))
+                for n, v in zip(names, s[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline_sample(w, data, nthreads, nt_sample, kind="port"):
+    """Time one shot-gradient of the workload with nt_sample time steps on the
+    host (the oracle: 'port' = FP32 transliteration, 'reference' = the
+    reference's kernels built for the CPU), scaled to the full nt."""
+    from oracle import pyoracle as po
+    po.build()
+    d = data["shots"][len(data["shots"]) // 2]
+    nt = nt_sample
+    shot = dict(stage=2, allnx=w["allnx"], allnz=w["allnz"], nx=d["nx"], pml=w["pml"], nop=4, nt=nt, ntr=d["ntr"],
+                dx=w["dx"], dz=w["dx"], dt=w["dt"], isx=d["isx"], isz=w["pml"] + w["sy"], igz=w["pml"] + w["gy"],
+                ngx_left=d["ngx_left"], delta_left=d["delta_left"], record_left_in_v=0, forward_only=0,
+                misfit_kind=0 if kind == "reference" else 1, nthreads=nthreads)
+    rng = np.random.default_rng(0)
+    model = dict(vp=data["vp0"], vs=data["vs0"], rho=data["rho0"], dvp=data["dvp"], dvs=data["dvs"],
+                 sou=data["sou"][:nt], gc=d["gc"],
+                 obs_z=(1e-9 * rng.standard_normal((d["ntr"], nt))).astype(np.float32),
+                 obs_x=(1e-9 * rng.standard_normal((d["ntr"], nt))).astype(np.float32))
+    lib = {"port": "f32", "reference": "ref2"}[kind]
+    t = time.perf_counter()
+    po.run_shot(lib, shot, model)
+    el = time.perf_counter() - t
+    per_shot = el * w["nt"] / nt
+    return 1.0 / per_shot, el
+
+
+def run_reference_arm(args, w):
+    ws, rank = dist_info()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as po
+    kind = "reference" if po.available("ref2") else "port"
+    try:
+        if kind == "reference":
+            po.load("ref2")
+    except OSError:
+        kind = "port"
+    data = build_workload(w)
+    threads = os.cpu_count() or 1
+    nt_sample = 200
+    for _ in range(args.warmup):
+        cpu_baseline_sample(w, data, threads, 20, kind)
+    vals, els = [], []
+    for _ in range(args.steps):
+        v, el = cpu_baseline_sample(w, data, threads, nt_sample, kind)
+        vals.append(v)
+        els.append(el)
+    value = float(np.mean(vals))
+    sample = "one %dx%d shot (stage-2 Born forward + %s adjoint), %d of %d time steps, scaled by nt" % (
+        w["allnx"], w["allnz"], "L2" if kind == "reference" else "OT", nt_sample, w["nt"])
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "shot-gradients/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(els)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["name"], "cpu": True, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "shot-gradients/s", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "shot-gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nt", type=int, default=None, help="override the number of time steps (testing)")
+    ap.add_argument("--shots", type=int, default=None, help="override the number of shots (testing)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
+    args = ap.parse_args()
+    w = dict(WORKLOAD)
+    if args.nt:
+        w["nt"] = args.nt
+    if args.shots:
+        w["nshots"] = args.shots
+        w["spacing"] = max(1, min(w["spacing"], (w["allnx"] - 1) // max(1, args.shots)))
+    if args.impl == "reference":
+        return run_reference_arm(args, w)
+
+    ws, rank = dist_info()
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="gloo", init_method="env://")
+        pg = dist
+
+    import sfwi_gb300 as sg
+    data = build_workload(w)
+    nt, pml = w["nt"], w["pml"]
+    nxpml, nzpml = w["allnx"] + 2 * pml, w["allnz"] + 2 * pml
+    shots = data["shots"]
+    isz, igz = pml + w["sy"], pml + w["gy"]
+
+    # observed data: background forward on the true model (untimed)
+    fwd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml,
+                             nt, 4, shots[0]["ntr"], stage=1)
+    fwd.GPUbufferVPVS(data["vp"], data["vs"], data["rho"])
+    for d in shots:
+        fwd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"])
+    fwd.run_forward()
+    obs = []
+    for i, d in enumerate(shots):
+        r = fwd.read_records(i, d["ntr"])
+        pz, px = sg.PinnedArray((d["ntr"], nt)), sg.PinnedArray((d["ntr"], nt))
+        pz.array[...] = r["syn_z"]
+        px.array[...] = r["syn_x"]
+        obs.append((pz, px))
+    fwd.close()
+
+    fd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml, nt,
+                            4, shots[0]["ntr"], stage=2)
+    fd.GPUbufferVPVS(data["vp0"], data["vs0"])
+    fd.GPUbufferM(data["dvp"], data["dvs"])
+    fd.set_misfit(sg.MISFIT_OT)
+
+    def step():
+        for d, (pz, px) in zip(shots, obs):
+            fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], pz.array,
+                            px.array)
+        m, _ = fd.run()
+        g = fd.imagebuffer_resettozero()
+        return m, g
+
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        m, g = step()
+    log("warm-up: %d steps in %.2f s, misfit %.6e" % (args.warmup, time.perf_counter() - t0, m))
+    if args.profile_kernels:
+        return 0
+
+    # device-timed steps (CUDA events inside the engine: set-up kernel .. final reduction)
+    if pg:
+        pg.barrier()
+    clocks = Clocks()
+    clocks.start()
+    launches0 = fd.kernel_launches()
+    dev_ms, fwd_ms, bwd_ms = [], [], []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        m, g = step()
+        t = fd.last_timing()
+        dev_ms.append(t["total_ms"])
+        fwd_ms.append(t["forward_ms"])
+        bwd_ms.append(t["backward_ms"])
+    wall = time.perf_counter() - wall0
+    launches = fd.kernel_launches() - launches0
+    clk = clocks.stop()
+    total_dev_s = sum(dev_ms) / 1000.0
+    if pg:
+        import torch
+        tt = torch.tensor([total_dev_s, wall], dtype=torch.float64)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        total_dev_s, wall = float(tt[0]), float(tt[1])
+    nsh = len(shots) * ws
+    value = nsh * args.steps / total_dev_s
+    e2e = nsh * args.steps / wall
+    h2d = sum(2 * d["ntr"] * nt * 4 for d in shots)
+    d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots)
+
+    # per-kernel average launch durations (CUDA events on the engine stream)
+    kt = fd.time_kernels(reps=20) if hasattr(fd, "time_kernels") else {}
+    peak, peak_kind = measured_peak_hbm()
+    cells = sum((d["nx"] + 2 * pml) * nzpml for d in shots)
+    roof = None
+    if kt:
+        shares = {k: v for k, v in kt.items()}
+        dom = max(shares, key=shares.get)
+        achieved = KERNEL_BYTES[dom] * cells / (kt[dom] / 1000.0) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()}}
+    alg_bytes_step = SURVEY_BYTES_PER_CELL_STEP * cells * nt
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, el = cpu_baseline_sample(w, data, 1, 150, "port")
+        cpu = {"value": v, "unit": "shot-gradients/s", "cores": 1, "kind": "port",
+               "sample": "one shot, 150 of %d time steps (%.1f s), FP32 single-thread transliteration, scaled by nt"
+                         % (nt, el)}
+    fd.close()
+    for pz, px in obs:
+        pz.free()
+        px.free()
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "shot-gradients/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
+                       "nt": nt, "misfit": "OT", "born": True, "parallelism": "shots-per-gpu",
+                       "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),
+                       "alg_bytes_per_step_GB": round(alg_bytes_step / 1e9, 2),
+                       "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
+            "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,159 @@
+/* sfwi_gb300.h — C ABI of the GB300 shot-gradient engine.
+ *
+ * The entry points replace the per-shot engine of the SFWI elastic FWI code:
+ * the class FD2DGPU_ELASTIC and the free functions of sfwi-stage{1,2}/FD2DGPU.cuh
+ * that sfwi-stage{1,2}/main.cpp calls.  A handle stands for one
+ * FD2DGPU_ELASTIC object; the public fields the driver writes before
+ * IMAGE_SINGLESHOT (isx, isz, igz, ngx_left, delta_left, record_left_in_v, ntr)
+ * are set through sfwi_set_shot_geometry.  All buffers are caller-owned host
+ * arrays with the reference's layouts:
+ *   models, gradients, illumination  float [allnx][allnz]  (z fastest)
+ *   records                          float [ntr][nt]       (time fastest)
+ *   receiver coordinates             int   [ntr]
+ * Every function returns 0 on success and a negative SFWI_E* code on failure;
+ * sfwi_last_error() gives a message for the calling thread's last failure.
+ * A handle is used by one host thread at a time; different handles are
+ * independent.
+ *
+ * Beyond the reference's one-shot-at-a-time calls, sfwi_enqueue_shot /
+ * sfwi_run advance many shots (each with its own window width) in the same
+ * kernel launches, and sfwi_ot* compute the 1D optimal-transport misfit the
+ * reference only declares.
+ */
+#ifndef SFWI_GB300_H
+#define SFWI_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sfwi_handle sfwi_handle;
+
+enum {
+    SFWI_OK = 0,
+    SFWI_E_ARG = -1,      /* invalid argument (size, pointer, geometry outside the model) */
+    SFWI_E_CUDA = -2,     /* CUDA runtime error (message in sfwi_last_error) */
+    SFWI_E_NOMEM = -3,    /* device or host allocation failed */
+    SFWI_E_STATE = -4,    /* call out of order (e.g. no model uploaded) */
+    SFWI_E_NODEVICE = -5  /* no CUDA device */
+};
+
+/* misfit functions for the adjoint source */
+enum {
+    SFWI_MISFIT_L2 = 0,        /* sum r^2, adjoint source r (the reference's live misfit) */
+    SFWI_MISFIT_OT = 1,        /* 1D W2, exponential positivity transform, per-trace scale */
+    SFWI_MISFIT_OT_POWER = 2,  /* 1D W2, squared-amplitude transform */
+    SFWI_MISFIT_OT_ALLTRACE = 3 /* 1D W2, exponential transform, gather-wide scale */
+};
+
+/* Constructor: FD2DGPU_ELASTIC(sou, dx, dz, dt, nxpml, nzpml, allnx, allnz,
+ * scale, pml, nt, nop, ntr), sfwi-stage1/FD2DGPU.cuh:152-153.  Copies sou[nt].
+ * stage selects the reference program whose IMAGE_SINGLESHOT is reproduced:
+ *   1  sfwi-stage1: background forward, residual syn-obs, adjoint direction +1
+ *   2  sfwi-stage2: background + Born forward, residual (du-obs)+u0,
+ *      adjoint direction -1, density forced to 2000 kg/m^3
+ * nop must be 4 (the 8th-order stencil of FD2DGPU.cuh:16). */
+int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float dz, float dt, int nxpml, int nzpml,
+                int allnx, int allnz, int scale, int pml, int nt, int nop, int ntr);
+int sfwi_destroy(sfwi_handle *h);
+
+/* GPUbufferVPVS(vp_all, vs_all, rho_all), sfwi-stage1/FD2DGPU.cuh:296
+ * (stage 2's two-argument form: pass rho_all = NULL). */
+int sfwi_gpu_buffer_vpvs(sfwi_handle *h, const float *vp_all, const float *vs_all, const float *rho_all);
+/* GPUbufferM(dvp, dvs), sfwi-stage1/FD2DGPU.cuh:237: the stage-2 model perturbation. */
+int sfwi_gpu_buffer_m(sfwi_handle *h, const float *dvp_all, const float *dvs_all);
+/* bufferVpVsHtoD(ngx_min), FD2DGPU.cu:1348: window start column of the next shot. */
+int sfwi_buffer_vpvs_htod(sfwi_handle *h, int ngx_min);
+/* record_copytoGPU(record_z, record_x, gc), FD2DGPU.cu:3507-3533: observed
+ * records [ntr][nt] and receiver coordinates of the next shot. */
+int sfwi_record_copy_to_gpu(sfwi_handle *h, const float *rec_z, const float *rec_x, const int *gc);
+/* The public fields main.cpp:619-625 writes before IMAGE_SINGLESHOT. */
+int sfwi_set_shot_geometry(sfwi_handle *h, int isx, int isz, int igz, int ngx_left, int delta_left,
+                           int record_left_in_v, int ntr);
+/* misfit function used by the following gradient calls (default L2) */
+int sfwi_set_misfit(sfwi_handle *h, int misfit_kind);
+
+/* IMAGE_SINGLESHOT, sfwi-stage1/FD2DGPU.cuh:466-467 / sfwi-stage2/FD2DGPU.cuh:455:
+ * one shot-gradient.  misfit += this shot's misfit; the Vp/Vs gradients and
+ * the illumination accumulate on the device until sfwi_imagebuffer_resettozero. */
+int sfwi_image_singleshot(sfwi_handle *h, double *misfit);
+
+/* imagebuffer_resettozero(grad_pp, grad_ps, illum, b1, b2, b3, b4),
+ * FD2DGPU.cu:3646-3673: copy the accumulated gradients out and zero them.
+ * b1..b4 receive the reference's scattering-term buffers, which its live path
+ * leaves at zero; any of the seven pointers may be NULL. */
+int sfwi_imagebuffer_resettozero(sfwi_handle *h, float *grad_pp, float *grad_ps, float *illum, float *b1, float *b2,
+                                 float *b3, float *b4);
+/* FP64 copy of the accumulated gradients (no reset) */
+int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, double *illum);
+
+/* Records of the last shot-gradient call(s): forward records (stage 1:
+ * background; stage 2: scattered), stage-2 background records and the adjoint
+ * source, each [ntr][nt] of shot `i` of the last run (0 for the one-shot call).
+ * Any pointer may be NULL. */
+int sfwi_read_records(sfwi_handle *h, int i, float *syn_z, float *syn_x, float *syn2_z, float *syn2_x, float *res_z,
+                      float *res_x);
+
+/* ---- batched shots: many shots per kernel launch ---- */
+typedef struct {
+    int nx;               /* window width in nodes (may differ between shots) */
+    int isx, isz, igz;    /* as sfwi_set_shot_geometry */
+    int ngx_left, delta_left, record_left_in_v;
+    int ntr;
+    const int *gc;        /* [ntr] receiver coordinates */
+    const float *rec_z;   /* [ntr][nt] observed records (read when the shot is run) */
+    const float *rec_x;
+} sfwi_shot_desc;
+
+/* queue a shot; its arrays must stay valid until sfwi_run returns */
+int sfwi_enqueue_shot(sfwi_handle *h, const sfwi_shot_desc *shot);
+/* advance every queued shot together (forward, residual, backward, imaging)
+ * and clear the queue; misfit += the sum over the shots (in queue order);
+ * per_shot_misfit (may be NULL) receives each shot's misfit. */
+int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit);
+/* forward modelling only of the queued shots: records are read back with
+ * sfwi_read_records; clears the queue */
+int sfwi_run_forward(sfwi_handle *h);
+
+/* ---- optimal-transport misfit (declared, not implemented, in the reference:
+ *      OT / OT_power / OT_alltrace, sfwi-stage1/FD2DGPU.cuh:21-25) ----
+ * obs/cal/res are host [tracenum][length]; misfit += W2 over traces and both
+ * components; res = (1/2) dW2/dcal (the scaling of the L2 residual). */
+int sfwi_ot(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x, float *res_z,
+            int length, int tracenum, float dt, double *misfit);
+int sfwi_ot_power(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
+                  float *res_z, int length, int tracenum, float dt, double *misfit);
+int sfwi_ot_alltrace(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
+                     float *res_z, int length, int tracenum, float dt, double *misfit);
+/* normalize(matrix, length, tracenum), sfwi-stage1/main.cpp:24-32: divide by
+ * the gather's largest absolute value (host code, as in the reference). */
+int sfwi_normalize(float *matrix, int length, int tracenum);
+
+/* ---- diagnostics ---- */
+const char *sfwi_last_error(void);
+/* kernels launched by this handle so far (time-step, set-up and misfit kernels) */
+long long sfwi_kernel_launches(sfwi_handle *h);
+/* device-side durations (ms, CUDA events on the handle's stream) of the last
+ * run: forward loop, backward loop, misfit/adjoint-source kernels, and the
+ * whole run from the set-up kernel to the final gradient reduction */
+int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_ms, float *total_ms);
+/* average device duration (ms) of one launch of each time-step kernel on the
+ * last run's batch: out_ms[0..3] = forward velocity sweep, forward stress
+ * sweep, backward stress sweep, backward velocity sweep; each is launched
+ * `reps` times back to back between CUDA events on the handle's stream.  The
+ * launches overwrite the wavefields of the last run (its records and
+ * gradients, already read or accumulated, are untouched). */
+int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
+/* page-locked host buffers (cudaMallocHost) for records that are copied every
+ * iteration; free with sfwi_host_free */
+int sfwi_host_alloc(size_t bytes, void **ptr);
+int sfwi_host_free(void *ptr);
+/* library version string */
+const char *sfwi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,260 @@
+"""sfwi_gb300 — GB300 (sm_103a) engine for the SFWI per-shot gradient path.
+
+Python face of the C ABI (include/sfwi_gb300.h), shaped like the reference's
+per-shot engine so a driver written against it reads the same:
+
+    fd = FD2DGPU_ELASTIC(sou, dx, dz, dt, nxpml, nzpml, allnx, allnz,
+                         scale, pml, nt, nop, ntr, stage=1)   # FD2DGPU.cuh:152
+    fd.GPUbufferVPVS(vp_all, vs_all, rho_all)                 # :296
+    fd.ntr = ntr; fd.record_copytoGPU(rec_z, rec_x, gc)      # FD2DGPU.cu:3507
+    fd.bufferVpVsHtoD(delta_left + record_left_in_v)          # :1348
+    fd.isx, fd.isz, fd.igz = ...; fd.ngx_left = ...; fd.delta_left = ...
+    misfit = IMAGE_SINGLESHOT(fd, misfit)                     # FD2DGPU.cuh:466
+    grads = fd.imagebuffer_resettozero()                      # FD2DGPU.cu:3646
+
+plus batched entry points (enqueue_shot / run) that advance many shots in the
+same kernel launches.  Arrays are numpy float32 in the reference's layouts:
+models [allnx, allnz], records [ntr, nt].
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import SfwiError, ShotDesc
+
+__all__ = ["FD2DGPU_ELASTIC", "IMAGE_SINGLESHOT", "OT", "OT_power", "OT_alltrace", "normalize", "SfwiError",
+           "MISFIT_L2", "MISFIT_OT", "MISFIT_OT_POWER", "MISFIT_OT_ALLTRACE", "library_path"]
+
+MISFIT_L2, MISFIT_OT, MISFIT_OT_POWER, MISFIT_OT_ALLTRACE = 0, 1, 2, 3
+
+
+def library_path():
+    return _lib.LIB_PATH
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None and a.shape != tuple(shape):
+        a = a.reshape(shape)
+    return a
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class FD2DGPU_ELASTIC:
+    """One per-shot engine (the reference's FD2DGPU_ELASTIC object).
+
+    stage=1 reproduces sfwi-stage1's IMAGE_SINGLESHOT, stage=2 sfwi-stage2's
+    (Born forward, residual (du-obs)+u0, adjoint direction -1, rho = 2000)."""
+
+    def __init__(self, sou, dx, dz, dt, nxpml, nzpml, allnx, allnz, scale, pml, nt, nop, ntr, stage=1):
+        lib = _lib.load()
+        self._sou = _f32(sou)
+        h = C.c_void_p()
+        _lib.check(lib.sfwi_create(C.byref(h), stage, _fp(self._sou), dx, dz, dt, nxpml, nzpml, allnx, allnz, scale,
+                                   pml, nt, nop, ntr))
+        self._h = h
+        self.stage, self.dx, self.dz, self.dt = stage, dx, dz, dt
+        self.nxpml, self.nzpml, self.allnx, self.allnz = nxpml, nzpml, allnx, allnz
+        self.pml, self.nt, self.nop, self.scale = pml, nt, nop, scale
+        self.nx, self.nz = nxpml - 2 * pml, nzpml - 2 * pml
+        # public fields written by the driver before IMAGE_SINGLESHOT (main.cpp:619-625)
+        self.ntr = ntr
+        self.isx = self.isz = self.igz = 0
+        self.ngx_left = self.delta_left = self.record_left_in_v = 0
+        self._keep = []
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().sfwi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _sync(self):
+        _lib.check(_lib.load().sfwi_set_shot_geometry(self._h, self.isx, self.isz, self.igz, self.ngx_left,
+                                                      self.delta_left, self.record_left_in_v, self.ntr))
+
+    # -- the reference's methods --
+    def GPUbufferVPVS(self, vp_all, vs_all, rho_all=None):
+        shp = (self.allnx, self.allnz)
+        vp, vs = _f32(vp_all, shp), _f32(vs_all, shp)
+        rho = None if rho_all is None else _f32(rho_all, shp)
+        _lib.check(_lib.load().sfwi_gpu_buffer_vpvs(self._h, _fp(vp), _fp(vs), _fp(rho)))
+
+    def GPUbufferM(self, pp, ps):
+        shp = (self.allnx, self.allnz)
+        a, b = _f32(pp, shp), _f32(ps, shp)
+        _lib.check(_lib.load().sfwi_gpu_buffer_m(self._h, _fp(a), _fp(b)))
+
+    def bufferVpVsHtoD(self, ngx_min):
+        _lib.check(_lib.load().sfwi_buffer_vpvs_htod(self._h, int(ngx_min)))
+
+    def record_copytoGPU(self, record, record_x, gc):
+        self._sync()
+        rz, rx = _f32(record, (self.ntr, self.nt)), _f32(record_x, (self.ntr, self.nt))
+        g = np.ascontiguousarray(gc, dtype=np.int32)
+        _lib.check(_lib.load().sfwi_record_copy_to_gpu(self._h, _fp(rz), _fp(rx), _ip(g)))
+
+    def set_misfit(self, kind):
+        _lib.check(_lib.load().sfwi_set_misfit(self._h, int(kind)))
+
+    def image_singleshot(self):
+        """One shot-gradient; returns this shot's misfit."""
+        self._sync()
+        m = C.c_double(0.0)
+        _lib.check(_lib.load().sfwi_image_singleshot(self._h, C.byref(m)))
+        return m.value
+
+    def imagebuffer_resettozero(self):
+        """(grad_pp, grad_ps, illumination) as float32 [allnx, allnz]; the
+        device accumulators are zeroed."""
+        shp = (self.allnx, self.allnz)
+        out = [np.zeros(shp, np.float32) for _ in range(3)]
+        _lib.check(_lib.load().sfwi_imagebuffer_resettozero(self._h, _fp(out[0]), _fp(out[1]), _fp(out[2]), None,
+                                                            None, None, None))
+        return tuple(out)
+
+    def read_gradients_f64(self):
+        shp = (self.allnx, self.allnz)
+        out = [np.zeros(shp, np.float64) for _ in range(3)]
+        dp = C.POINTER(C.c_double)
+        _lib.check(_lib.load().sfwi_read_gradients_f64(self._h, *[o.ctypes.data_as(dp) for o in out]))
+        return tuple(out)
+
+    def read_records(self, i=0, ntr=None):
+        """dict of syn_z, syn_x, syn2_z, syn2_x, res_z, res_x ([ntr, nt]) of
+        shot i of the last run."""
+        ntr = self.ntr if ntr is None else ntr
+        names = ("syn_z", "syn_x", "syn2_z", "syn2_x", "res_z", "res_x")
+        out = {k: np.zeros((ntr, self.nt), np.float32) for k in names}
+        _lib.check(_lib.load().sfwi_read_records(self._h, i, *[_fp(out[k]) for k in names]))
+        return out
+
+    # -- batched shots --
+    def enqueue_shot(self, nx, isx, isz, igz, ngx_left, delta_left, record_left_in_v, gc, rec_z=None, rec_x=None):
+        g = np.ascontiguousarray(gc, dtype=np.int32)
+        ntr = int(g.size)
+        rz = _f32(rec_z if rec_z is not None else np.zeros((ntr, self.nt), np.float32), (ntr, self.nt))
+        rx = _f32(rec_x if rec_x is not None else np.zeros((ntr, self.nt), np.float32), (ntr, self.nt))
+        self._keep += [g, rz, rx]  # must outlive run()
+        d = ShotDesc(nx=nx, isx=isx, isz=isz, igz=igz, ngx_left=ngx_left, delta_left=delta_left,
+                     record_left_in_v=record_left_in_v, ntr=ntr, gc=_ip(g), rec_z=_fp(rz), rec_x=_fp(rx))
+        _lib.check(_lib.load().sfwi_enqueue_shot(self._h, C.byref(d)))
+
+    def run(self, nshots=None):
+        """Advance all queued shots together; returns (misfit, per-shot misfits)."""
+        n = nshots if nshots is not None else len(self._keep) // 3
+        per = np.zeros(max(n, 1), np.float64)
+        m = C.c_double(0.0)
+        try:
+            _lib.check(_lib.load().sfwi_run(self._h, C.byref(m), per.ctypes.data_as(C.POINTER(C.c_double))))
+        finally:
+            self._keep = []
+        return m.value, per[:n]
+
+    def run_forward(self):
+        try:
+            _lib.check(_lib.load().sfwi_run_forward(self._h))
+        finally:
+            self._keep = []
+
+    def time_kernels(self, reps=20):
+        """Average launch duration (ms) of each time-step kernel on the last
+        run's batch (overwrites that run's wavefields)."""
+        out = np.zeros(4, np.float32)
+        _lib.check(_lib.load().sfwi_time_kernels(self._h, int(reps), _fp(out)))
+        born = self.stage == 2
+        names = ["k_fwd_v<born>" if born else "k_fwd_v", "k_fwd_s<born>" if born else "k_fwd_s", "k_bwd_s", "k_bwd_v"]
+        return {n: float(v) for n, v in zip(names, out)}
+
+    def kernel_launches(self):
+        return int(_lib.load().sfwi_kernel_launches(self._h))
+
+    def last_timing(self):
+        f, b, o, t = C.c_float(), C.c_float(), C.c_float(), C.c_float()
+        _lib.check(_lib.load().sfwi_last_timing(self._h, C.byref(f), C.byref(b), C.byref(o), C.byref(t)))
+        return {"forward_ms": f.value, "backward_ms": b.value, "misfit_ms": o.value, "total_ms": t.value}
+
+
+def IMAGE_SINGLESHOT(fdtdgpu, misfit=0.0, *reference_args):
+    """IMAGE_SINGLESHOT(fd, misfit) -> misfit + this shot's misfit
+    (sfwi-stage1/FD2DGPU.cuh:466-467).  The reference's remaining arguments
+    (sxnum, nDim, myid, record, record_x, gc, rbc, cpu_mem, ntt, iter, ...)
+    select MPI bookkeeping, host offload and disabled options and are
+    accepted and ignored."""
+    return misfit + fdtdgpu.image_singleshot()
+
+
+def _ot(fn, obs_x, obs_z, cal_x, cal_z, dt):
+    obs_x, obs_z, cal_x, cal_z = (_f32(a) for a in (obs_x, obs_z, cal_x, cal_z))
+    tracenum, length = obs_x.shape
+    rx, rz = np.zeros_like(obs_x), np.zeros_like(obs_z)
+    m = C.c_double(0.0)
+    _lib.check(getattr(_lib.load(), fn)(_fp(obs_x), _fp(obs_z), _fp(cal_x), _fp(cal_z), _fp(rx), _fp(rz), length,
+                                        tracenum, dt, C.byref(m)))
+    return rx, rz, m.value
+
+
+def OT(obs_x, obs_z, cal_x, cal_z, dt):
+    """1D W2 misfit (exponential weights, per-trace scale) of [tracenum, length]
+    gathers; returns (res_x, res_z, misfit)."""
+    return _ot("sfwi_ot", obs_x, obs_z, cal_x, cal_z, dt)
+
+
+def OT_power(obs_x, obs_z, cal_x, cal_z, dt):
+    return _ot("sfwi_ot_power", obs_x, obs_z, cal_x, cal_z, dt)
+
+
+def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
+    return _ot("sfwi_ot_alltrace", obs_x, obs_z, cal_x, cal_z, dt)
+
+
+class PinnedArray:
+    """numpy float32 array in page-locked host memory (sfwi_host_alloc)."""
+
+    def __init__(self, shape):
+        n = int(np.prod(shape))
+        p = C.c_void_p()
+        _lib.check(_lib.load().sfwi_host_alloc(max(n, 1) * 4, C.byref(p)))
+        self._p = p
+        buf = (C.c_float * max(n, 1)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float32, count=n).reshape(shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            _lib.load().sfwi_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def normalize(matrix):
+    """In-place division by the largest absolute value (main.cpp:24-32)."""
+    a = np.ascontiguousarray(matrix, dtype=np.float32)
+    tracenum, length = a.shape
+    _lib.check(_lib.load().sfwi_normalize(_fp(a), length, tracenum))
+    return a

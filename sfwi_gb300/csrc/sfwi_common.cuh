@@ -1,0 +1,152 @@
+// sfwi_common.cuh — data layout and device helpers shared by the kernels.
+//
+// Layout in HBM.  A batch of shots is packed along x: every wavefield,
+// memory-variable and coefficient array is ONE 2-D array [X][P] (z fastest),
+// X = sum over shots of the shot's padded width nxpml_s, P = nzpml rounded up
+// to a multiple of 4 floats (16-byte rows, float4 access).  Shot s owns rows
+// [row0_s, row0_s + nxpml_s).  A cell updated by a stencil is at least nop=4
+// rows from its shot's first and last row, and the outer 4 rows/columns of a
+// shot are never written (they stay zero, as in the reference, where the
+// update kernels skip them: sfwi-stage1/born.cu:362), so no guard rows are
+// needed between shots.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sfwi {
+
+constexpr int NOP = 4;          // stencil half-width (8th order)
+constexpr int TX = 32;          // tile rows (x)
+constexpr int TZ = 32;          // tile columns (z)
+constexpr int HALO = 4;
+constexpr int BX = TX + 2 * HALO;  // staged box rows
+constexpr int BZ = TZ + 2 * HALO;  // staged box columns (multiple of 4)
+constexpr int BOX = BX * BZ;       // floats per staged box
+constexpr int NTHREADS = 256;      // 8 float4 columns x 32 rows
+
+// Arrays of the packed batch grid, in allocation order: one [X][P] array each,
+// consecutive in one allocation (array k starts at k*X*P floats), so a single
+// 3-D TMA tensor map [array][row][column] reaches all of them.
+enum GridArr {
+    BG_VX, BG_VZ, BG_TXX, BG_TZZ, BG_TXZ, BG_MVX, BG_MVZ, BG_MTXX, BG_MTZZ, BG_MTXZ,
+    SC_VX, SC_VZ, SC_TXX, SC_TZZ, SC_TXZ, SC_MVX, SC_MVZ, SC_MTXX, SC_MTZZ, SC_MTXZ,
+    AD_VX, AD_VZ, AD_TXX, AD_TZZ, AD_TXZ, AD_MVX, AD_MVZ, AD_MTXZ,
+    G_LAM, G_MU, G_ILL,
+    NSTATE,  // arrays above are zeroed per run
+    C_IB = NSTATE, C_LAM, C_MU, C_DX, C_DZ, C_BP, C_BS, C_VP, C_VS, C_RHO,
+    NGRID
+};
+
+// per-shot geometry (device-resident table)
+struct ShotGeo {
+    int row0;      // first packed row
+    int nxpml;     // padded width (rows)
+    int nx;        // interior width = nxpml - 2*pml
+    int isx, isz;  // source cell (local row, column)
+    int igz;       // receiver column (depth index)
+    int ntr;       // traces of this shot
+    int tr0;       // first trace in the packed trace arrays
+    int win0;      // global-model column of interior column 0 (delta_left + record_left_in_v)
+    int pad_;
+    long long strip0;  // float offset of this shot's edge-strip area
+    long long rec0;    // float offset of this shot's records in the trace-major arrays ([ntr][nt])
+    int csr0;          // offset of this shot's receiver-column CSR (nxpml+1 entries)
+    int pad2_;
+};
+
+// tile table entry: shot, first local row, first column, flags
+struct Tile {
+    int shot;
+    int x0;
+    int z0;
+    int flags;
+};
+enum TileFlags : int {
+    TILE_FRAME = 1,      // intersects the PML frame (damping != 0 somewhere)
+    TILE_STRIP = 2,      // core or halo touches an edge strip
+    TILE_RECV = 4,       // core or halo touches the receiver row
+    TILE_IMAGE = 8,      // core touches the imaging interior
+    TILE_SOURCE = 16,    // box contains the source cell
+};
+
+// arrays of one propagating field set (background, scattered or adjoint)
+struct FieldSet {
+    float *vx, *vz, *txx, *tzz, *txz;   // totals
+    float *mvx, *mvz;                   // x-parts of vx, vz (frame cells only)
+    float *mtxx, *mtzz, *mtxz;          // x-parts of txx, tzz, txz (frame cells only)
+};
+
+struct Coef {
+    const float *ib;      // 1/rho
+    const float *lam, *mu;
+    const float *dampx, *dampz;
+    const float *bp, *bs; // Born: 2 rho vp dvp, 2 rho vs dvs
+};
+
+struct Params {
+    int X, P;            // packed rows, pitch
+    int nzpml, pml, nt;
+    int born_lo;         // Born source region [born_lo, n-born_lo)
+    float dt, dtdx, dtdz, idx, idz;
+    FieldSet bg, sc, ad;
+    Coef c;
+    float *glam, *gmu, *illum;  // per-cell imaging accumulators
+    const ShotGeo *geo;
+    const Tile *tiles;
+    const float *sou;           // [nt]
+    float *strips;              // edge strips: shot s, step it at geo[s].strip0 + it*strip_floats(nx_s, nz)
+    float *syn_z, *syn_x;       // time-major [nt][ntr_tot] forward records
+    float *syn2_z, *syn2_x;     // stage 2 background records
+    const float *res_z, *res_x; // trace-major [ntr][nt] adjoint sources
+    const int *csr_start;       // receiver columns: per shot nxpml+1 offsets
+    const int *csr_trace;       // trace index (global) sorted by column then trace
+    int ntr_tot;
+    int ntiles;
+    int *err;                   // set to a nonzero code when a bounded device wait gives up
+    int *counters;              // tile counters, one per (time step, kernel): counters[4*it + kernel]
+};
+
+// Edge strips of vx and vz saved each forward step and restored in the
+// backward step (the reference's record_edge_wavefield/load_edge_wavefield,
+// sfwi-stage1/FD2DGPU.cu:3842-3899): 2*NOP-wide bands around the interior.
+// One step of one shot is [component vx|vz][top nx*8 | bottom nx*8 |
+// left 8*nz | right 8*nz].
+__host__ __device__ __forceinline__ long long strip_comp_floats(int nx, int nz) {
+    return 16LL * nx + 16LL * nz;
+}
+__host__ __device__ __forceinline__ long long strip_floats(int nx, int nz) { return 2 * strip_comp_floats(nx, nz); }
+
+// index of cell (lx, lz) inside one component block, or -1; where the top or
+// bottom band overlaps the left or right band the top/bottom slot is returned
+// (both slots always hold the same value)
+__host__ __device__ __forceinline__ int strip_index(int lx, int lz, int nxpml, int nzpml, int pml) {
+    const int nx = nxpml - 2 * pml, nz = nzpml - 2 * pml;
+    if (lx >= pml && lx < nxpml - pml) {
+        if (lz >= pml - NOP && lz < pml + NOP) return (lx - pml) * 8 + (lz - (pml - NOP));
+        if (lz >= nzpml - pml - NOP && lz < nzpml - pml + NOP)
+            return 8 * nx + (lx - pml) * 8 + (lz - (nzpml - pml - NOP));
+    }
+    if (lz >= pml && lz < nzpml - pml) {
+        if (lx >= pml - NOP && lx < pml + NOP) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
+        if (lx >= nxpml - pml - NOP && lx < nxpml - pml + NOP)
+            return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
+    }
+    return -1;
+}
+// second slot of a cell that lies in both a top/bottom and a left/right band
+__host__ __device__ __forceinline__ int strip_index2(int lx, int lz, int nxpml, int nzpml, int pml) {
+    const int nx = nxpml - 2 * pml, nz = nzpml - 2 * pml;
+    const bool tb = lx >= pml && lx < nxpml - pml &&
+                    ((lz >= pml - NOP && lz < pml + NOP) || (lz >= nzpml - pml - NOP && lz < nzpml - pml + NOP));
+    if (!tb || lz < pml || lz >= nzpml - pml) return -1;
+    if (lx >= pml - NOP && lx < pml + NOP) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
+    if (lx >= nxpml - pml - NOP && lx < nxpml - pml + NOP)
+        return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
+    return -1;
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+
+}  // namespace sfwi

@@ -1,0 +1,1045 @@
+// sfwi_engine.cu — host runtime behind include/sfwi_gb300.h.
+//
+// A handle is the counterpart of one FD2DGPU_ELASTIC object
+// (sfwi-stage1/FD2DGPU.cuh:146-459).  A run packs the queued shots into one
+// batch (see sfwi_common.cuh for the layout), computes their coefficients,
+// then advances all of them together: nt forward steps (2 launches each),
+// the residual or OT adjoint source, nt backward steps (2 launches each), and
+// the FP64 reduction into the global gradients.  The forward and backward
+// loops are captured once per batch shape as CUDA graphs and replayed.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cmath>
+
+#include "../../include/sfwi_gb300.h"
+#include <cudaTypedefs.h>
+
+#include "sfwi_launch.h"
+
+
+using namespace sfwi;
+
+namespace {
+
+constexpr int kTimeKernelsMaxReps = 64;
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(e_ == cudaErrorMemoryAllocation ? SFWI_E_NOMEM : SFWI_E_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t m) {
+        if (m <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
+        if (e == cudaSuccess) n = m;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct ShotIn {
+    int nx, win0, isx, isz, igz, ngx_left, ntr;
+    std::vector<int> gc;
+    const float *obs_z = nullptr, *obs_x = nullptr;  // host [ntr][nt]
+};
+
+enum RecArr { R_SYNT_Z, R_SYNT_X, R_SYN2T_Z, R_SYN2T_X, R_SYN_Z, R_SYN_X, R_SYN2_Z, R_SYN2_X, R_OBS_Z, R_OBS_X,
+              R_RES_Z, R_RES_X, NREC };
+
+struct Batch {
+    int nshots = 0, ntiles = 0, X = 0, P = 0, ntr_tot = 0, max_nxpml = 0;
+    std::vector<ShotGeo> geo;
+    std::vector<Tile> tiles;
+    std::vector<int> csr_start, csr_trace;
+    std::vector<double> sigma;  // OT scale per trace/component
+    long long strip_total = 0;
+    // device
+    DevBuf<float> grid;      // NGRID * X * P
+    DevBuf<float> strips;
+    DevBuf<float> recs;      // NREC * ntr_tot * nt
+    DevBuf<double> tmis;     // 2 * ntr_tot
+    DevBuf<double> dsigma;
+    DevBuf<ShotGeo> dgeo;
+    DevBuf<Tile> dtiles;
+    DevBuf<int> dcsr_start, dcsr_trace;
+    size_t cells = 0;        // X * P
+    DevBuf<int> derr;        // device-side error flag (bounded waits)
+    DevBuf<int> dctr;        // dynamic tile counters of the step kernels (zeroed per run)
+    TmaMaps tm;              // tensor maps of `grid` for the current X, P
+    // graphs of the time loops for the current shape
+    cudaGraphExec_t gfwd = nullptr, gbwd = nullptr;
+    std::vector<long long> gsig;  // shape signature of the captured graphs
+    float *g(int k) { return grid.p + (size_t)k * cells; }
+    float *r(int k, int nt) { return recs.p + (size_t)k * ntr_tot * nt; }
+    void drop_graphs() {
+        if (gfwd) cudaGraphExecDestroy(gfwd);
+        if (gbwd) cudaGraphExecDestroy(gbwd);
+        gfwd = gbwd = nullptr;
+        gsig.clear();
+    }
+};
+
+}  // namespace
+
+struct sfwi_handle {
+    int stage = 1;
+    int allnx = 0, allnz = 0, nxpml = 0, nzpml = 0, pml = 0, nt = 0, nop = 4, ntr = 0, scale = 1;
+    float dx = 0, dz = 0, dt = 0;
+    int misfit_kind = SFWI_MISFIT_L2;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    DevBuf<float> sou, vp_all, vs_all, rho_all, dvp_all, dvs_all;
+    bool have_model = false, have_rho = false, have_m = false;
+    DevBuf<double> gpp, gps, gil;
+    // one-shot state written by the reference-shaped calls
+    int ngx_min = 0;
+    std::vector<float> rec_z, rec_x;
+    std::vector<int> gc;
+    int isx = 0, isz = 0, igz = 0, ngx_left = 0, delta_left = 0, record_left_in_v = 0;
+    bool have_geom = false, have_rec = false;
+    std::vector<ShotIn> queue;
+    Batch b;
+    std::vector<int> last_ntr;   // traces of each shot of the last run
+    std::vector<int> last_tr0;
+    long long launches = 0;
+    float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
+    bool use_graphs = true;
+    bool last_forward_only = false;
+};
+
+namespace {
+
+int receiver_ix(int stage, int pml, int gc, int ngx_left, float dx) {
+    // GPUrecord_scatterwavefield, sfwi-stage1/FD2DGPU.cu:3161; stage 2 passes dx as int
+    if (stage == 2) return pml + (int)((float)(gc - ngx_left) / (int)dx);
+    return pml + (int)((float)(gc - ngx_left) / dx);
+}
+
+bool box_hits(int bx0, int bx1, int bz0, int bz1, int x0, int x1, int z0, int z1) {
+    return bx0 < x1 && x0 < bx1 && bz0 < z1 && z0 < bz1;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+// 3-D tiled map over the packed grid: dims (P, X, NGRID) floats, boxes of
+// bz x bx x 1; out-of-range elements of a box load arrive as zeros
+int encode_grid_map(CUtensorMap *m, float *base, int P, int X, int bz, int bx) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[3] = {(cuuint64_t)P, (cuuint64_t)X, (cuuint64_t)NGRID};
+    const cuuint64_t strides[2] = {(cuuint64_t)P * 4, (cuuint64_t)P * X * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SFWI_OK;
+}
+
+int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
+    Batch &b = h->b;
+    const int pml = h->pml, nzpml = h->nzpml, nt = h->nt, nz = h->allnz;
+    b.nshots = (int)shots.size();
+    b.P = (nzpml + 3) & ~3;
+    b.geo.assign(b.nshots, ShotGeo{});
+    b.tiles.clear();
+    b.csr_start.clear();
+    b.csr_trace.clear();
+    b.sigma.clear();
+    int row = 0, tr0 = 0;
+    long long strip0 = 0;
+    b.max_nxpml = 0;
+    for (int s = 0; s < b.nshots; s++) {
+        const ShotIn &in = shots[s];
+        ShotGeo &g = b.geo[s];
+        const int nxpml = in.nx + 2 * pml;
+        if (in.nx < 1 || in.win0 < 0 || in.win0 + in.nx > h->allnx)
+            return fail(SFWI_E_ARG, "shot %d: window [%d, %d) outside the model width %d", s, in.win0,
+                        in.win0 + in.nx, h->allnx);
+        if (in.isx < 0 || in.isx >= nxpml || in.isz < 0 || in.isz >= nzpml)
+            return fail(SFWI_E_ARG, "shot %d: source cell (%d, %d) outside the %d x %d grid", s, in.isx, in.isz, nxpml,
+                        nzpml);
+        if (in.igz < 0 || in.igz >= nzpml) return fail(SFWI_E_ARG, "shot %d: receiver depth %d outside the grid", s, in.igz);
+        if (in.ntr < 0 || (int)in.gc.size() != in.ntr) return fail(SFWI_E_ARG, "shot %d: bad trace count", s);
+        g.row0 = row;
+        g.nxpml = nxpml;
+        g.nx = in.nx;
+        g.isx = in.isx;
+        g.isz = in.isz;
+        g.igz = in.igz;
+        g.ntr = in.ntr;
+        g.tr0 = tr0;
+        g.win0 = in.win0;
+        g.strip0 = strip0;
+        g.rec0 = (long long)tr0 * nt;
+        g.csr0 = (int)b.csr_start.size();
+        // receiver columns, CSR sorted by column then trace
+        std::vector<int> rix(in.ntr);
+        std::vector<std::vector<int>> bycol(nxpml);
+        for (int t = 0; t < in.ntr; t++) {
+            rix[t] = receiver_ix(h->stage, pml, in.gc[t], in.ngx_left, h->dx);
+            if (rix[t] < 0 || rix[t] >= nxpml)
+                return fail(SFWI_E_ARG, "shot %d trace %d: receiver column %d outside the %d-wide grid", s, t, rix[t],
+                            nxpml);
+            bycol[rix[t]].push_back(tr0 + t);
+        }
+        int acc = (int)b.csr_trace.size();
+        for (int x = 0; x < nxpml; x++) {
+            b.csr_start.push_back(acc);
+            for (int t : bycol[x]) b.csr_trace.push_back(t);
+            acc += (int)bycol[x].size();
+        }
+        b.csr_start.push_back(acc);
+        // tiles over the update region [NOP, n-NOP)
+        for (int x0 = NOP; x0 < nxpml - NOP; x0 += TX)
+            for (int z0 = NOP; z0 < nzpml - NOP; z0 += TZ) {
+                const int cx1 = std::min(x0 + TX, nxpml - NOP), cz1 = std::min(z0 + TZ, nzpml - NOP);
+                const int bx0 = x0 - HALO, bx1 = x0 + TX + HALO, bz0 = z0 - HALO, bz1 = z0 + TZ + HALO;
+                int f = 0;
+                // frame: cells with lx < pml, lx > nxpml-pml, lz < pml or lz > nzpml-pml
+                if (x0 < pml || cx1 - 1 > nxpml - pml || z0 < pml || cz1 - 1 > nzpml - pml) f |= TILE_FRAME;
+                const int ix0 = pml, ix1 = nxpml - pml, iz0 = pml, iz1 = nzpml - pml;
+                if (box_hits(x0, cx1, z0, cz1, ix0, ix1, iz0, iz1)) f |= TILE_IMAGE;
+                if (box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, pml - NOP, pml + NOP) ||
+                    box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, nzpml - pml - NOP, nzpml - pml + NOP) ||
+                    box_hits(bx0, bx1, bz0, bz1, pml - NOP, pml + NOP, pml, nzpml - pml) ||
+                    box_hits(bx0, bx1, bz0, bz1, nxpml - pml - NOP, nxpml - pml + NOP, pml, nzpml - pml))
+                    f |= TILE_STRIP;
+                if (in.igz >= bz0 && in.igz < bz1)
+                    for (int t = 0; t < in.ntr; t++)
+                        if (rix[t] >= bx0 && rix[t] < bx1) {
+                            f |= TILE_RECV;
+                            break;
+                        }
+                if (in.isx >= bx0 && in.isx < bx1 && in.isz >= bz0 && in.isz < bz1) f |= TILE_SOURCE;
+                b.tiles.push_back(Tile{s, x0, z0, f});
+            }
+        // OT scales: max|obs| per trace and component, or over the gather
+        {
+            std::vector<double> sz(in.ntr, 0.0), sx(in.ntr, 0.0);
+            double gz = 0.0, gx = 0.0;
+            for (int t = 0; t < in.ntr; t++)
+                for (int k = 0; k < nt; k++) {
+                    if (in.obs_z) sz[t] = std::max(sz[t], (double)std::fabs(in.obs_z[(size_t)t * nt + k]));
+                    if (in.obs_x) sx[t] = std::max(sx[t], (double)std::fabs(in.obs_x[(size_t)t * nt + k]));
+                }
+            for (int t = 0; t < in.ntr; t++) {
+                gz = std::max(gz, sz[t]);
+                gx = std::max(gx, sx[t]);
+            }
+            for (int t = 0; t < in.ntr; t++) {
+                b.sigma.push_back(h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE ? gz : sz[t]);
+                b.sigma.push_back(h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE ? gx : sx[t]);
+            }
+        }
+        row += nxpml;
+        tr0 += in.ntr;
+        strip0 += strip_floats(in.nx, nz) * nt;
+        b.max_nxpml = std::max(b.max_nxpml, nxpml);
+    }
+    b.X = row;
+    b.ntr_tot = tr0;
+    b.ntiles = (int)b.tiles.size();
+    b.strip_total = strip0;
+    b.cells = (size_t)b.X * b.P;
+    h->last_ntr.clear();
+    h->last_tr0.clear();
+    for (auto &g : b.geo) {
+        h->last_ntr.push_back(g.ntr);
+        h->last_tr0.push_back(g.tr0);
+    }
+    return SFWI_OK;
+}
+
+Params make_params(sfwi_handle *h, bool forward_only) {
+    Batch &b = h->b;
+    Params p{};
+    p.X = b.X;
+    p.P = b.P;
+    p.nzpml = h->nzpml;
+    p.pml = h->pml;
+    p.nt = h->nt;
+    p.born_lo = h->stage == 2 ? NOP : h->pml;
+    p.dt = h->dt;
+    p.dtdx = h->dt / h->dx;
+    p.dtdz = h->dt / h->dz;
+    p.idx = 1.0f / h->dx;
+    p.idz = 1.0f / h->dz;
+    p.bg = FieldSet{b.g(BG_VX), b.g(BG_VZ), b.g(BG_TXX), b.g(BG_TZZ), b.g(BG_TXZ),
+                    b.g(BG_MVX), b.g(BG_MVZ), b.g(BG_MTXX), b.g(BG_MTZZ), b.g(BG_MTXZ)};
+    p.sc = FieldSet{b.g(SC_VX), b.g(SC_VZ), b.g(SC_TXX), b.g(SC_TZZ), b.g(SC_TXZ),
+                    b.g(SC_MVX), b.g(SC_MVZ), b.g(SC_MTXX), b.g(SC_MTZZ), b.g(SC_MTXZ)};
+    p.ad = FieldSet{b.g(AD_VX), b.g(AD_VZ), b.g(AD_TXX), b.g(AD_TZZ), b.g(AD_TXZ),
+                    b.g(AD_MVX), b.g(AD_MVZ), nullptr, nullptr, b.g(AD_MTXZ)};
+    p.c = Coef{b.g(C_IB), b.g(C_LAM), b.g(C_MU), b.g(C_DX), b.g(C_DZ), b.g(C_BP), b.g(C_BS)};
+    p.glam = b.g(G_LAM);
+    p.gmu = b.g(G_MU);
+    p.illum = b.g(G_ILL);
+    p.geo = b.dgeo.p;
+    p.tiles = b.dtiles.p;
+    p.sou = h->sou.p;
+    p.strips = forward_only ? nullptr : b.strips.p;  // modelling only: no strips saved
+    const int nt = h->nt;
+    p.syn_z = b.r(R_SYNT_Z, nt);
+    p.syn_x = b.r(R_SYNT_X, nt);
+    p.syn2_z = b.r(R_SYN2T_Z, nt);
+    p.syn2_x = b.r(R_SYN2T_X, nt);
+    p.res_z = b.r(R_RES_Z, nt);
+    p.res_x = b.r(R_RES_X, nt);
+    p.csr_start = b.dcsr_start.p;
+    p.csr_trace = b.dcsr_trace.p;
+    p.ntr_tot = b.ntr_tot;
+    p.ntiles = b.ntiles;
+    p.err = b.derr.p;
+    p.counters = b.dctr.p;
+    return p;
+}
+
+int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_only) {
+    Batch &b = h->b;
+    const int nt = h->nt;
+    const size_t recs = (size_t)NREC * std::max(b.ntr_tot, 1) * nt;
+    float *old_grid = b.grid.p, *old_strips = b.strips.p, *old_recs = b.recs.p;
+    CK(b.grid.ensure((size_t)NGRID * b.cells));
+    CK(b.strips.ensure(forward_only ? 1 : (size_t)std::max<long long>(b.strip_total, 1)));
+    CK(b.recs.ensure(recs));
+    CK(b.tmis.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
+    CK(b.dsigma.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
+    CK(b.dgeo.ensure(b.geo.size()));
+    CK(b.dtiles.ensure(b.tiles.size()));
+    CK(b.dcsr_start.ensure(b.csr_start.size()));
+    CK(b.dcsr_trace.ensure(std::max<size_t>(b.csr_trace.size(), 1)));
+    CK(b.derr.ensure(1));
+    CK(cudaMemsetAsync(b.derr.p, 0, sizeof(int), h->st));
+    const size_t nctr = 4 * (size_t)std::max(h->nt, kTimeKernelsMaxReps + 1);
+    CK(b.dctr.ensure(nctr));
+    CK(cudaMemsetAsync(b.dctr.p, 0, nctr * sizeof(int), h->st));
+    if (int rc = encode_grid_map(&b.tm.box, b.grid.p, b.P, b.X, BZ, BX)) return rc;
+    if (int rc = encode_grid_map(&b.tm.core, b.grid.p, b.P, b.X, TZ, TX)) return rc;
+    if (old_grid != b.grid.p || old_strips != b.strips.p || old_recs != b.recs.p) b.drop_graphs();
+    cudaStream_t st = h->st;
+    CK(cudaMemcpyAsync(b.dgeo.p, b.geo.data(), b.geo.size() * sizeof(ShotGeo), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(b.dcsr_start.p, b.csr_start.data(), b.csr_start.size() * sizeof(int), cudaMemcpyHostToDevice,
+                       st));
+    if (!b.csr_trace.empty())
+        CK(cudaMemcpyAsync(b.dcsr_trace.p, b.csr_trace.data(), b.csr_trace.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+    if (!b.sigma.empty())
+        CK(cudaMemcpyAsync(b.dsigma.p, b.sigma.data(), b.sigma.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    // zero the state (fields, memory variables, accumulators) and the records
+    CK(cudaMemsetAsync(b.grid.p, 0, (size_t)NSTATE * b.cells * sizeof(float), st));
+    CK(cudaMemsetAsync(b.recs.p, 0, recs * sizeof(float), st));
+    // observed records, trace-major
+    if (!forward_only) {
+        for (size_t s = 0; s < shots.size(); s++) {
+            const ShotIn &in = shots[s];
+            const size_t off = (size_t)b.geo[s].tr0 * nt, n = (size_t)in.ntr * nt;
+            if (!n) continue;
+            if (in.obs_z) CK(cudaMemcpyAsync(b.r(R_OBS_Z, nt) + off, in.obs_z, n * sizeof(float), cudaMemcpyHostToDevice, st));
+            if (in.obs_x) CK(cudaMemcpyAsync(b.r(R_OBS_X, nt) + off, in.obs_x, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        }
+    }
+    SetupArgs a{};
+    a.X = b.X;
+    a.P = b.P;
+    a.nzpml = h->nzpml;
+    a.pml = h->pml;
+    a.allnz = h->allnz;
+    a.stage = h->stage;
+    a.born_lo = h->stage == 2 ? NOP : h->pml;
+    a.dt = h->dt;
+    a.vp_all = h->vp_all.p;
+    a.vs_all = h->vs_all.p;
+    a.rho_all = h->have_rho ? h->rho_all.p : h->vp_all.p;
+    a.dvp_all = h->stage == 2 && h->have_m ? h->dvp_all.p : nullptr;
+    a.dvs_all = h->stage == 2 && h->have_m ? h->dvs_all.p : nullptr;
+    a.ib = b.g(C_IB);
+    a.lam = b.g(C_LAM);
+    a.mu = b.g(C_MU);
+    a.dampx = b.g(C_DX);
+    a.dampz = b.g(C_DZ);
+    a.bp = b.g(C_BP);
+    a.bs = b.g(C_BS);
+    a.vp = b.g(C_VP);
+    a.vs = b.g(C_VS);
+    a.rho = b.g(C_RHO);
+    a.geo = b.dgeo.p;
+    CK(cudaEventRecord(h->ev[4], st));
+    launch_setup(a, b.nshots, b.max_nxpml, st);
+    h->launches++;
+    CK(cudaGetLastError());
+    return SFWI_OK;
+}
+
+std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
+    Batch &b = h->b;
+    std::vector<long long> s = {h->nt, h->stage, forward_only, b.ntiles, b.X, b.P, b.ntr_tot,
+                                (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.strips.p,
+                                (long long)(uintptr_t)b.recs.p, (long long)(uintptr_t)b.dtiles.p,
+                                (long long)(uintptr_t)b.dgeo.p, (long long)(uintptr_t)b.dcsr_start.p,
+                                (long long)(uintptr_t)b.dcsr_trace.p, (long long)(uintptr_t)h->sou.p};
+    for (auto &t : b.tiles) s.push_back(((long long)t.shot << 40) ^ ((long long)t.x0 << 24) ^ (t.z0 << 8) ^ t.flags);
+    for (auto &g : b.geo) {
+        s.push_back(g.isx * 100003LL + g.isz);
+        s.push_back(g.igz * 1000003LL + g.nx);
+        s.push_back(g.strip0);
+    }
+    for (int v : b.csr_trace) s.push_back(v);
+    return s;
+}
+
+void enqueue_forward(sfwi_handle *h, const Params &p, bool forward_only) {
+    const bool born = h->stage == 2;
+    (void)forward_only;
+    for (int it = 0; it < h->nt; it++) launch_fwd_step(p, h->b.tm, it, born, h->st);
+}
+
+void enqueue_backward(sfwi_handle *h, const Params &p) {
+    const float adj = h->stage == 1 ? 1.f : -1.f;
+    for (int it = h->nt - 1; it >= 0; it--) launch_bwd_step(p, h->b.tm, it, adj, h->st);
+}
+
+int capture(sfwi_handle *h, cudaGraphExec_t *out, bool fwd, const Params &p, bool forward_only) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    if (fwd)
+        enqueue_forward(h, p, forward_only);
+    else
+        enqueue_backward(h, p);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(SFWI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(SFWI_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    return SFWI_OK;
+}
+
+int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_only, double *misfit,
+              double *per_shot) {
+    if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
+    if (shots.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    h->last_forward_only = forward_only;
+    CK(cudaSetDevice(h->device));
+    int rc = build_batch(h, shots);
+    if (rc) return rc;
+    if (!forward_only && h->misfit_kind != SFWI_MISFIT_L2 && ot_smem_bytes(h->nt) > 227 * 1024)
+        return fail(SFWI_E_ARG, "OT misfit supports nt <= %d", (int)(227 * 1024 / 32));
+    rc = upload_batch(h, shots, forward_only);
+    if (rc) return rc;
+    Batch &b = h->b;
+    const Params p = make_params(h, forward_only);
+    const int nt = h->nt;
+    cudaStream_t st = h->st;
+    std::vector<long long> sig = shape_signature(h, forward_only);
+    if (h->use_graphs && sig != b.gsig) {
+        b.drop_graphs();
+        rc = capture(h, &b.gfwd, true, p, forward_only);
+        if (rc) return rc;
+        if (!forward_only) {
+            rc = capture(h, &b.gbwd, false, p, false);
+            if (rc) return rc;
+        }
+        b.gsig = sig;
+    }
+    CK(cudaEventRecord(h->ev[0], st));
+    if (h->use_graphs)
+        CK(cudaGraphLaunch(b.gfwd, st));
+    else
+        enqueue_forward(h, p, forward_only);
+    h->launches += 2LL * nt;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[1], st));
+    // records to trace-major
+    launch_transpose(b.r(R_SYNT_Z, nt), b.r(R_SYN_Z, nt), nt, b.ntr_tot, st);
+    launch_transpose(b.r(R_SYNT_X, nt), b.r(R_SYN_X, nt), nt, b.ntr_tot, st);
+    h->launches += 2;
+    if (h->stage == 2) {
+        launch_transpose(b.r(R_SYN2T_Z, nt), b.r(R_SYN2_Z, nt), nt, b.ntr_tot, st);
+        launch_transpose(b.r(R_SYN2T_X, nt), b.r(R_SYN2_X, nt), nt, b.ntr_tot, st);
+        h->launches += 2;
+    }
+    CK(cudaGetLastError());
+    if (forward_only) {
+        CK(cudaEventRecord(h->ev[5], st));
+        int derr = 0;
+        CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
+        cudaEventElapsedTime(&h->fwd_ms, h->ev[0], h->ev[1]);
+        cudaEventElapsedTime(&h->total_ms, h->ev[4], h->ev[5]);
+        h->bwd_ms = 0.f;
+        h->other_ms = 0.f;
+        return SFWI_OK;
+    }
+    // adjoint source and misfit
+    if (h->misfit_kind == SFWI_MISFIT_L2) {
+        launch_residual_l2(h->stage, nt, b.ntr_tot, b.r(R_SYN_Z, nt), b.r(R_SYN_X, nt), b.r(R_SYN2_Z, nt),
+                           b.r(R_SYN2_X, nt), b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), b.r(R_RES_Z, nt), b.r(R_RES_X, nt),
+                           b.tmis.p, st);
+    } else {
+        OtArgs o{};
+        o.kind = h->misfit_kind;
+        o.nt = nt;
+        o.ntr = b.ntr_tot;
+        o.stage = h->stage;
+        o.dt = h->dt;
+        o.cal_z = b.r(R_SYN_Z, nt);
+        o.cal_x = b.r(R_SYN_X, nt);
+        o.cal2_z = h->stage == 2 ? b.r(R_SYN2_Z, nt) : nullptr;
+        o.cal2_x = h->stage == 2 ? b.r(R_SYN2_X, nt) : nullptr;
+        o.obs_z = b.r(R_OBS_Z, nt);
+        o.obs_x = b.r(R_OBS_X, nt);
+        o.res_z = b.r(R_RES_Z, nt);
+        o.res_x = b.r(R_RES_X, nt);
+        o.sigma = b.dsigma.p;
+        o.trace_misfit = b.tmis.p;
+        CK(launch_ot(o, st));
+    }
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[2], st));
+    if (h->use_graphs)
+        CK(cudaGraphLaunch(b.gbwd, st));
+    else
+        enqueue_backward(h, p);
+    h->launches += 2LL * nt;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[3], st));
+    FinalArgs fa{};
+    fa.allnx = h->allnx;
+    fa.allnz = h->allnz;
+    fa.P = b.P;
+    fa.pml = h->pml;
+    fa.nshots = b.nshots;
+    fa.geo = b.dgeo.p;
+    fa.glam = b.g(G_LAM);
+    fa.gmu = b.g(G_MU);
+    fa.illum = b.g(G_ILL);
+    fa.vp = b.g(C_VP);
+    fa.vs = b.g(C_VS);
+    fa.rho = b.g(C_RHO);
+    fa.gpp = h->gpp.p;
+    fa.gps = h->gps.p;
+    fa.gil = h->gil.p;
+    launch_finalize(fa, st);
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[5], st));
+    std::vector<double> tm(2 * (size_t)b.ntr_tot);
+    const size_t nm = h->misfit_kind == SFWI_MISFIT_L2 ? b.ntr_tot : 2 * (size_t)b.ntr_tot;
+    if (nm) CK(cudaMemcpyAsync(tm.data(), b.tmis.p, nm * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
+    cudaEventElapsedTime(&h->fwd_ms, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&h->other_ms, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&h->bwd_ms, h->ev[2], h->ev[3]);
+    cudaEventElapsedTime(&h->total_ms, h->ev[4], h->ev[5]);
+    double total = 0.0;
+    for (int s = 0; s < b.nshots; s++) {
+        double ms = 0.0;
+        const ShotGeo &g = b.geo[s];
+        for (int t = 0; t < g.ntr; t++) {
+            if (h->misfit_kind == SFWI_MISFIT_L2)
+                ms += tm[g.tr0 + t];
+            else
+                ms += tm[2 * (size_t)(g.tr0 + t)] + tm[2 * (size_t)(g.tr0 + t) + 1];
+        }
+        if (per_shot) per_shot[s] = ms;
+        total += ms;
+    }
+    if (misfit) *misfit += total;
+    return SFWI_OK;
+}
+
+int check(sfwi_handle *h) {
+    if (!h) return fail(SFWI_E_ARG, "null handle");
+    return SFWI_OK;
+}
+
+int ensure_grads(sfwi_handle *h) {
+    const size_t n = (size_t)h->allnx * h->allnz;
+    if (h->gpp.p) return SFWI_OK;
+    CK(h->gpp.ensure(n));
+    CK(h->gps.ensure(n));
+    CK(h->gil.ensure(n));
+    CK(cudaMemset(h->gpp.p, 0, n * sizeof(double)));
+    CK(cudaMemset(h->gps.p, 0, n * sizeof(double)));
+    CK(cudaMemset(h->gil.p, 0, n * sizeof(double)));
+    return SFWI_OK;
+}
+
+int upload_model(DevBuf<float> &d, const float *src, size_t n) {
+    CK(d.ensure(n));
+    CK(cudaMemcpy(d.p, src, n * sizeof(float), cudaMemcpyHostToDevice));
+    return SFWI_OK;
+}
+
+int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
+            float *res_z, int length, int tracenum, float dt, double *misfit) {
+    if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z || !misfit || length < 1 || tracenum < 0)
+        return fail(SFWI_E_ARG, "sfwi_ot: bad argument");
+    if (tracenum == 0) return SFWI_OK;
+    if (ot_smem_bytes(length) > 227 * 1024) return fail(SFWI_E_ARG, "sfwi_ot: length %d too long", length);
+    const size_t n = (size_t)length * tracenum;
+    float *d = nullptr;
+    double *dd = nullptr;
+    CK(cudaMalloc(&d, 6 * n * sizeof(float)));
+    cudaError_t e = cudaMalloc(&dd, 4 * (size_t)tracenum * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return fail(SFWI_E_NOMEM, "sfwi_ot: %s", cudaGetErrorString(e));
+    }
+    std::vector<double> sig(2 * (size_t)tracenum);
+    double gz = 0, gx = 0;
+    for (int t = 0; t < tracenum; t++) {
+        double mz = 0, mx = 0;
+        for (int k = 0; k < length; k++) {
+            mz = std::max(mz, (double)std::fabs(obs_z[(size_t)t * length + k]));
+            mx = std::max(mx, (double)std::fabs(obs_x[(size_t)t * length + k]));
+        }
+        sig[2 * t] = mz;
+        sig[2 * t + 1] = mx;
+        gz = std::max(gz, mz);
+        gx = std::max(gx, mx);
+    }
+    if (kind == SFWI_MISFIT_OT_ALLTRACE)
+        for (int t = 0; t < tracenum; t++) {
+            sig[2 * t] = gz;
+            sig[2 * t + 1] = gx;
+        }
+    int rc = SFWI_OK;
+    std::vector<double> tm(2 * (size_t)tracenum);
+    do {
+        if ((e = cudaMemcpy(d, obs_z, n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d + n, obs_x, n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d + 2 * n, cal_z, n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d + 3 * n, cal_x, n * 4, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(dd, sig.data(), sig.size() * 8, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        OtArgs o{};
+        o.kind = kind;
+        o.nt = length;
+        o.ntr = tracenum;
+        o.stage = 1;
+        o.dt = dt;
+        o.obs_z = d;
+        o.obs_x = d + n;
+        o.cal_z = d + 2 * n;
+        o.cal_x = d + 3 * n;
+        o.res_z = d + 4 * n;
+        o.res_x = d + 5 * n;
+        o.sigma = dd;
+        o.trace_misfit = dd + 2 * tracenum;
+        if ((e = launch_ot(o, 0)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(res_z, d + 4 * n, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(res_x, d + 5 * n, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(tm.data(), dd + 2 * tracenum, tm.size() * 8, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+    } while (0);
+    cudaFree(d);
+    cudaFree(dd);
+    if (e != cudaSuccess) return fail(SFWI_E_CUDA, "sfwi_ot: %s", cudaGetErrorString(e));
+    double w = 0;
+    for (double v : tm) w += v;
+    *misfit += w;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sfwi_last_error(void) { return g_err.c_str(); }
+const char *sfwi_version(void) { return "sfwi_gb300 0.1 (sm_103a)"; }
+
+int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float dz, float dt, int nxpml, int nzpml,
+                int allnx, int allnz, int scale, int pml, int nt, int nop, int ntr) {
+    if (!out) return fail(SFWI_E_ARG, "out is null");
+    *out = nullptr;
+    if (stage != 1 && stage != 2) return fail(SFWI_E_ARG, "stage must be 1 or 2");
+    if (nop != NOP) return fail(SFWI_E_ARG, "nop must be %d (8th-order stencil)", NOP);
+    if (!sou || nt < 1 || dx <= 0 || dz <= 0 || dt <= 0 || pml < NOP + 1 || allnx < 1 || allnz < 1 || ntr < 0)
+        return fail(SFWI_E_ARG, "bad size or spacing");
+    if (nzpml != allnz + 2 * pml) return fail(SFWI_E_ARG, "nzpml must be allnz + 2*pml");
+    if (nxpml < 2 * pml + 1) return fail(SFWI_E_ARG, "nxpml must exceed 2*pml");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(SFWI_E_NODEVICE, "no CUDA device");
+    sfwi_handle *h = new sfwi_handle();
+    h->stage = stage;
+    h->dx = dx;
+    h->dz = dz;
+    h->dt = dt;
+    h->nxpml = nxpml;
+    h->nzpml = nzpml;
+    h->allnx = allnx;
+    h->allnz = allnz;
+    h->scale = scale;
+    h->pml = pml;
+    h->nt = nt;
+    h->nop = nop;
+    h->ntr = ntr;
+    cudaGetDevice(&h->device);
+    int rc = SFWI_OK;
+    do {
+        cudaError_t e;
+        if ((e = configure_step_kernels()) != cudaSuccess) {
+            rc = fail(SFWI_E_CUDA, "kernel attributes: %s", cudaGetErrorString(e));
+            break;
+        }
+        if ((e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess) {
+            rc = fail(SFWI_E_CUDA, "stream: %s", cudaGetErrorString(e));
+            break;
+        }
+        for (auto &ev : h->ev)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+                rc = fail(SFWI_E_CUDA, "event: %s", cudaGetErrorString(e));
+                break;
+            }
+        if (rc) break;
+        if ((rc = upload_model(h->sou, sou, nt))) break;
+        rc = ensure_grads(h);
+    } while (0);
+    if (rc) {
+        sfwi_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return SFWI_OK;
+}
+
+int sfwi_destroy(sfwi_handle *h) {
+    if (!h) return SFWI_OK;
+    cudaSetDevice(h->device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    h->b.drop_graphs();
+    h->b.grid.release();
+    h->b.strips.release();
+    h->b.recs.release();
+    h->b.tmis.release();
+    h->b.dsigma.release();
+    h->b.dgeo.release();
+    h->b.dtiles.release();
+    h->b.dcsr_start.release();
+    h->b.dcsr_trace.release();
+    h->b.derr.release();
+    h->b.dctr.release();
+    for (auto *d : {&h->sou, &h->vp_all, &h->vs_all, &h->rho_all, &h->dvp_all, &h->dvs_all}) d->release();
+    h->gpp.release();
+    h->gps.release();
+    h->gil.release();
+    for (auto &ev : h->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return SFWI_OK;
+}
+
+int sfwi_gpu_buffer_vpvs(sfwi_handle *h, const float *vp_all, const float *vs_all, const float *rho_all) {
+    if (int rc = check(h)) return rc;
+    if (!vp_all || !vs_all) return fail(SFWI_E_ARG, "vp/vs null");
+    if (h->stage == 1 && !rho_all) return fail(SFWI_E_ARG, "stage 1 needs rho_all");
+    const size_t n = (size_t)h->allnx * h->allnz;
+    int rc;
+    if ((rc = upload_model(h->vp_all, vp_all, n))) return rc;
+    if ((rc = upload_model(h->vs_all, vs_all, n))) return rc;
+    h->have_rho = false;
+    if (rho_all) {
+        if ((rc = upload_model(h->rho_all, rho_all, n))) return rc;
+        h->have_rho = true;
+    }
+    h->have_model = true;
+    return SFWI_OK;
+}
+
+int sfwi_gpu_buffer_m(sfwi_handle *h, const float *dvp_all, const float *dvs_all) {
+    if (int rc = check(h)) return rc;
+    if (!dvp_all || !dvs_all) return fail(SFWI_E_ARG, "dvp/dvs null");
+    const size_t n = (size_t)h->allnx * h->allnz;
+    int rc;
+    if ((rc = upload_model(h->dvp_all, dvp_all, n))) return rc;
+    if ((rc = upload_model(h->dvs_all, dvs_all, n))) return rc;
+    h->have_m = true;
+    return SFWI_OK;
+}
+
+int sfwi_buffer_vpvs_htod(sfwi_handle *h, int ngx_min) {
+    if (int rc = check(h)) return rc;
+    const int nx = h->nxpml - 2 * h->pml;
+    if (ngx_min < 0 || ngx_min + nx > h->allnx)
+        return fail(SFWI_E_ARG, "window [%d, %d) outside the model width %d", ngx_min, ngx_min + nx, h->allnx);
+    h->ngx_min = ngx_min;
+    return SFWI_OK;
+}
+
+int sfwi_record_copy_to_gpu(sfwi_handle *h, const float *rec_z, const float *rec_x, const int *gc) {
+    if (int rc = check(h)) return rc;
+    if ((!rec_z || !rec_x || !gc) && h->ntr > 0) return fail(SFWI_E_ARG, "null record or coordinates");
+    const size_t n = (size_t)h->ntr * h->nt;
+    h->rec_z.assign(rec_z, rec_z + n);
+    h->rec_x.assign(rec_x, rec_x + n);
+    h->gc.assign(gc, gc + h->ntr);
+    h->have_rec = true;
+    return SFWI_OK;
+}
+
+int sfwi_set_shot_geometry(sfwi_handle *h, int isx, int isz, int igz, int ngx_left, int delta_left,
+                           int record_left_in_v, int ntr) {
+    if (int rc = check(h)) return rc;
+    if (ntr < 0) return fail(SFWI_E_ARG, "ntr < 0");
+    if (ntr != h->ntr) h->have_rec = false;  // the records must be copied again for a new trace count
+    h->isx = isx;
+    h->isz = isz;
+    h->igz = igz;
+    h->ngx_left = ngx_left;
+    h->delta_left = delta_left;
+    h->record_left_in_v = record_left_in_v;
+    h->ntr = ntr;
+    h->have_geom = true;
+    return SFWI_OK;
+}
+
+int sfwi_set_misfit(sfwi_handle *h, int kind) {
+    if (int rc = check(h)) return rc;
+    if (kind < SFWI_MISFIT_L2 || kind > SFWI_MISFIT_OT_ALLTRACE) return fail(SFWI_E_ARG, "unknown misfit %d", kind);
+    h->misfit_kind = kind;
+    return SFWI_OK;
+}
+
+int sfwi_image_singleshot(sfwi_handle *h, double *misfit) {
+    if (int rc = check(h)) return rc;
+    if (!h->have_geom || !h->have_rec) return fail(SFWI_E_STATE, "shot geometry and records must be set first");
+    ShotIn s;
+    s.nx = h->nxpml - 2 * h->pml;
+    // the window is the one bufferVpVsHtoD cut; the gradient lands at delta_left + record_left_in_v
+    s.win0 = h->delta_left + h->record_left_in_v;
+    if (s.win0 != h->ngx_min)
+        return fail(SFWI_E_ARG, "bufferVpVsHtoD(%d) and delta_left+record_left_in_v=%d differ", h->ngx_min, s.win0);
+    s.isx = h->isx;
+    s.isz = h->isz;
+    s.igz = h->igz;
+    s.ngx_left = h->ngx_left;
+    s.ntr = h->ntr;
+    s.gc = h->gc;
+    s.obs_z = h->rec_z.data();
+    s.obs_x = h->rec_x.data();
+    std::vector<ShotIn> v{std::move(s)};
+    double m = 0.0;
+    int rc = run_batch(h, v, false, &m, nullptr);
+    if (rc) return rc;
+    if (misfit) *misfit += m;
+    return SFWI_OK;
+}
+
+int sfwi_imagebuffer_resettozero(sfwi_handle *h, float *grad_pp, float *grad_ps, float *illum, float *b1, float *b2,
+                                 float *b3, float *b4) {
+    if (int rc = check(h)) return rc;
+    const size_t n = (size_t)h->allnx * h->allnz;
+    std::vector<double> tmp(n);
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->st));
+    float *outs[3] = {grad_pp, grad_ps, illum};
+    DevBuf<double> *src[3] = {&h->gpp, &h->gps, &h->gil};
+    for (int k = 0; k < 3; k++) {
+        if (outs[k]) {
+            CK(cudaMemcpy(tmp.data(), src[k]->p, n * sizeof(double), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < n; i++) outs[k][i] = (float)tmp[i];
+        }
+        CK(cudaMemset(src[k]->p, 0, n * sizeof(double)));
+    }
+    for (float *bb : {b1, b2, b3, b4})
+        if (bb) std::memset(bb, 0, n * sizeof(float));
+    return SFWI_OK;
+}
+
+int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, double *illum) {
+    if (int rc = check(h)) return rc;
+    const size_t n = (size_t)h->allnx * h->allnz;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->st));
+    if (grad_pp) CK(cudaMemcpy(grad_pp, h->gpp.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad_ps) CK(cudaMemcpy(grad_ps, h->gps.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (illum) CK(cudaMemcpy(illum, h->gil.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return SFWI_OK;
+}
+
+int sfwi_read_records(sfwi_handle *h, int i, float *syn_z, float *syn_x, float *syn2_z, float *syn2_x, float *res_z,
+                      float *res_x) {
+    if (int rc = check(h)) return rc;
+    if (i < 0 || i >= (int)h->last_ntr.size()) return fail(SFWI_E_ARG, "shot %d not in the last run", i);
+    const int nt = h->nt;
+    const size_t off = (size_t)h->last_tr0[i] * nt, n = (size_t)h->last_ntr[i] * nt;
+    Batch &b = h->b;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->st));
+    struct {
+        float *dst;
+        int k;
+    } items[6] = {{syn_z, R_SYN_Z}, {syn_x, R_SYN_X}, {syn2_z, R_SYN2_Z}, {syn2_x, R_SYN2_X}, {res_z, R_RES_Z},
+                  {res_x, R_RES_X}};
+    for (auto &it : items)
+        if (it.dst && n) CK(cudaMemcpy(it.dst, b.r(it.k, nt) + off, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return SFWI_OK;
+}
+
+int sfwi_enqueue_shot(sfwi_handle *h, const sfwi_shot_desc *d) {
+    if (int rc = check(h)) return rc;
+    if (!d) return fail(SFWI_E_ARG, "null shot");
+    if (d->ntr < 0 || (d->ntr > 0 && (!d->gc || !d->rec_z || !d->rec_x)))
+        return fail(SFWI_E_ARG, "shot needs gc and records");
+    ShotIn s;
+    s.nx = d->nx;
+    s.win0 = d->delta_left + d->record_left_in_v;
+    s.isx = d->isx;
+    s.isz = d->isz;
+    s.igz = d->igz;
+    s.ngx_left = d->ngx_left;
+    s.ntr = d->ntr;
+    s.gc.assign(d->gc, d->gc + d->ntr);
+    s.obs_z = d->rec_z;
+    s.obs_x = d->rec_x;
+    h->queue.push_back(std::move(s));
+    return SFWI_OK;
+}
+
+int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit) {
+    if (int rc = check(h)) return rc;
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    double m = 0.0;
+    int rc = run_batch(h, q, false, &m, per_shot_misfit);
+    if (rc) return rc;
+    if (misfit) *misfit += m;
+    return SFWI_OK;
+}
+
+int sfwi_run_forward(sfwi_handle *h) {
+    if (int rc = check(h)) return rc;
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    return run_batch(h, q, true, nullptr, nullptr);
+}
+
+int sfwi_ot(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x, float *res_z,
+            int length, int tracenum, float dt, double *misfit) {
+    return ot_host(SFWI_MISFIT_OT, obs_x, obs_z, cal_x, cal_z, res_x, res_z, length, tracenum, dt, misfit);
+}
+int sfwi_ot_power(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
+                  float *res_z, int length, int tracenum, float dt, double *misfit) {
+    return ot_host(SFWI_MISFIT_OT_POWER, obs_x, obs_z, cal_x, cal_z, res_x, res_z, length, tracenum, dt, misfit);
+}
+int sfwi_ot_alltrace(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
+                     float *res_z, int length, int tracenum, float dt, double *misfit) {
+    return ot_host(SFWI_MISFIT_OT_ALLTRACE, obs_x, obs_z, cal_x, cal_z, res_x, res_z, length, tracenum, dt, misfit);
+}
+
+int sfwi_normalize(float *matrix, int length, int tracenum) {
+    // sfwi-stage1/main.cpp:24-32
+    if (!matrix || length < 0 || tracenum < 0) return fail(SFWI_E_ARG, "bad argument");
+    const size_t n = (size_t)length * tracenum;
+    float mx = 0;
+    for (size_t i = 0; i < n; i++) mx = (std::fabs(matrix[i]) > mx) ? std::fabs(matrix[i]) : mx;
+    for (size_t i = 0; i < n; i++) matrix[i] = matrix[i] / mx;
+    return SFWI_OK;
+}
+
+long long sfwi_kernel_launches(sfwi_handle *h) { return h ? h->launches : 0; }
+
+int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_ms, float *total_ms) {
+    if (int rc = check(h)) return rc;
+    if (fwd_ms) *fwd_ms = h->fwd_ms;
+    if (bwd_ms) *bwd_ms = h->bwd_ms;
+    if (other_ms) *other_ms = h->other_ms;
+    if (total_ms) *total_ms = h->total_ms;
+    return SFWI_OK;
+}
+
+int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
+    if (int rc = check(h)) return rc;
+    if (!out_ms || reps < 1) return fail(SFWI_E_ARG, "bad argument");
+    if (h->b.ntiles == 0 || !h->b.grid.p) return fail(SFWI_E_STATE, "no batch has been run");
+    CK(cudaSetDevice(h->device));
+    const Params p = make_params(h, false);
+    const bool born = h->stage == 2;
+    const float adj = h->stage == 1 ? 1.f : -1.f;
+    if (h->last_forward_only) return fail(SFWI_E_STATE, "the last run was forward-only (no edge strips)");
+    if (reps > kTimeKernelsMaxReps) reps = kTimeKernelsMaxReps;
+    if (reps > h->nt - 1) reps = h->nt - 1;  // step indices 0..reps must exist
+    if (reps < 1) return fail(SFWI_E_ARG, "nt too small to time the kernels");
+    for (int k = 0; k < 4; k++) {
+        // step indices 0..reps select fresh tile counters; the kernels read
+        // records and strips at those steps, which exist for every run
+        CK(cudaMemsetAsync(h->b.dctr.p, 0, 4 * (size_t)(reps + 1) * sizeof(int), h->st));
+        launch_step_kernel(k, p, h->b.tm, reps, born, adj, h->st);  // warm
+        CK(cudaEventRecord(h->ev[0], h->st));
+        for (int r = 0; r < reps; r++) launch_step_kernel(k, p, h->b.tm, r, born, adj, h->st);
+        CK(cudaEventRecord(h->ev[1], h->st));
+        CK(cudaEventSynchronize(h->ev[1]));
+        CK(cudaGetLastError());
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+        out_ms[k] = ms / reps;
+        h->launches += reps + 1;
+    }
+    return SFWI_OK;
+}
+
+int sfwi_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return fail(SFWI_E_ARG, "null pointer");
+    *ptr = nullptr;
+    cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 1);
+    if (e != cudaSuccess) return fail(SFWI_E_NOMEM, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    return SFWI_OK;
+}
+
+int sfwi_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+    return SFWI_OK;
+}
+
+}  // extern "C"

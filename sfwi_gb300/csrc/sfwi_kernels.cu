@@ -1,0 +1,1074 @@
+// sfwi_kernels.cu — the time-step kernels of the shot-gradient path.
+//
+// One launch advances every shot of a batch by one sweep.  The work is cut
+// into TX x TZ tiles (32 x 32 cells of one shot).  Each kernel is persistent:
+// one CTA per SM walks the tile list, and a two-stage TMA pipeline
+// (cp.async.bulk.tensor into shared memory, completion on an mbarrier) loads
+// tile k+1 while tile k is computed.  Per tile the pipeline stages
+//   - the fields read by the stencils as (TX+8) x (TZ+8) boxes (4-cell halo;
+//     cells outside the packed arrays arrive as zeros), and
+//   - the cell's own state and coefficients as TX x TZ core tiles,
+// and the threads write their updated cells with float4 stores.  A single
+// 3-D tensor map [array][row][column] over the packed grid addresses every
+// array (sfwi_common.cuh).
+//
+//   k_fwd_v   forward velocity sweep  (update_vx_vz, sfwi-stage1/born.cu:355-394)
+//             of the background and, for the Born forward, the scattered field
+//   k_fwd_s   forward stress sweep (update_txx_tzz_txz, born.cu:399-440), the Born
+//             virtual source (add_born_source_components, sfwi-stage2/born.cu:749-801)
+//             and the scattered stress sweep; receiver capture
+//             (GPUrecord_scatterwavefield, FD2DGPU.cu:3158-3166) and edge-strip save
+//             (record_edge_wavefield, FD2DGPU.cu:3842-3869)
+//   k_bwd_s   reconstruction stress sweep with strains (update_txx_tzz_txz_grad,
+//             born.cu:451-499), adjoint stress sweep
+//             (GPUcalculate_elastic_txx_tzz_txz_back, born.cu:565-603) and the
+//             zero-lag imaging condition (doimage_gradient, FD2DGPU.cu:3350-3382)
+//   k_bwd_v   reconstruction velocity sweep (update_vx_vz, direction -1),
+//             illumination (doimage_illum, FD2DGPU.cu:3324-3331) and adjoint
+//             velocity sweep (GPUcalculate_elastic_vx_vz_back, born.cu:504-562)
+//
+// State representation.  In the reference every field carries two PML split
+// parts over the whole grid and the total is their sum.  Here the total is the
+// state everywhere and only cells of the PML frame (where dampx or dampz is
+// nonzero) also keep the x-part; the z-part is total minus x-part.  Away from
+// the frame the split update reduces to total += dir*coef*(Dx + Dz).
+//
+// Three writes of the reference touch only the total field, never the split
+// parts, so the next split update discards them: the source added to txx/tzz
+// (GPUapplysource, FD2DGPU.cu:2104-2114), the residual assigned into the
+// adjoint velocity (GPUapplysource_backward_from_record, FD2DGPU.cu:3425-3441)
+// and the edge strips restored into vx/vz (load_edge_wavefield,
+// FD2DGPU.cu:3873-3899).  Each is seen by exactly one stencil sweep, so here
+// each is applied to the staged shared-memory box of that sweep only and the
+// stored state is left untouched — the same arithmetic with no extra kernel.
+#include "sfwi_launch.h"
+
+namespace sfwi {
+
+// 8th-order staggered first-derivative weights, sfwi-stage1/FD2DGPU.cuh:16
+constexpr float K1 = (float)(1225.0 / 1024.0);
+constexpr float K2 = (float)(-245.0 / 3072.0);
+constexpr float K3 = (float)(49.0 / 5120.0);
+constexpr float K4 = (float)(-5.0 / 7168.0);
+
+constexpr int NSTAGE = 2;
+constexpr int CORE = TX * TZ;  // floats of a core tile
+constexpr uint32_t BOX_BYTES = BOX * 4u, CORE_BYTES = CORE * 4u;
+// iterations of mbarrier.try_wait before a wait is declared lost (each try
+// may suspend the thread for a while; the bound is several seconds)
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+// ----------------------------------------------------------------------------
+// TMA / mbarrier primitives
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false when the phase did not complete within WAIT_LIMIT tries
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// 3-D tiled bulk tensor load global -> shared, completion counted on `bar`
+__device__ __forceinline__ void tma_load(float *dst, const CUtensorMap *map, int col, int row, int arr,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(col), "r"(row), "r"(arr), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// ----------------------------------------------------------------------------
+// stencils on staged boxes (row pitch BZ)
+// ----------------------------------------------------------------------------
+struct V4 {
+    float v[4];
+};
+
+__device__ __forceinline__ void acc4(V4 &a, float k, float4 p, float4 m) {
+    a.v[0] += k * (p.x - m.x);
+    a.v[1] += k * (p.y - m.y);
+    a.v[2] += k * (p.z - m.z);
+    a.v[3] += k * (p.w - m.w);
+}
+// D+x: sum_k K_k (f[r+k] - f[r-k+1])   (txx in update_vx, vz in txz update)
+__device__ __forceinline__ V4 dxp(const float *f, int r, int c) {
+    const float *q = f + r * BZ + c;
+    V4 a = {{0.f, 0.f, 0.f, 0.f}};
+    acc4(a, K1, ld4(q + 1 * BZ), ld4(q));
+    acc4(a, K2, ld4(q + 2 * BZ), ld4(q - 1 * BZ));
+    acc4(a, K3, ld4(q + 3 * BZ), ld4(q - 2 * BZ));
+    acc4(a, K4, ld4(q + 4 * BZ), ld4(q - 3 * BZ));
+    return a;
+}
+// D-x: sum_k K_k (f[r+k-1] - f[r-k])   (txz in update_vz, vx in txx update)
+__device__ __forceinline__ V4 dxm(const float *f, int r, int c) {
+    const float *q = f + r * BZ + c;
+    V4 a = {{0.f, 0.f, 0.f, 0.f}};
+    acc4(a, K1, ld4(q), ld4(q - 1 * BZ));
+    acc4(a, K2, ld4(q + 1 * BZ), ld4(q - 2 * BZ));
+    acc4(a, K3, ld4(q + 2 * BZ), ld4(q - 3 * BZ));
+    acc4(a, K4, ld4(q + 3 * BZ), ld4(q - 4 * BZ));
+    return a;
+}
+struct W12 {
+    float w[12];
+};
+__device__ __forceinline__ W12 loadw(const float *f, int r, int c) {
+    const float *q = f + r * BZ + c;
+    float4 a = ld4(q - 4), b = ld4(q), d = ld4(q + 4);
+    W12 o = {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z, d.w}};
+    return o;
+}
+// D+z: sum_k K_k (f[c+k] - f[c-k+1])
+__device__ __forceinline__ V4 dzp(const W12 &s) {
+    V4 a;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int c = 4 + i;
+        float t = 0.f;
+        t += K1 * (s.w[c + 1] - s.w[c]);
+        t += K2 * (s.w[c + 2] - s.w[c - 1]);
+        t += K3 * (s.w[c + 3] - s.w[c - 2]);
+        t += K4 * (s.w[c + 4] - s.w[c - 3]);
+        a.v[i] = t;
+    }
+    return a;
+}
+// D-z: sum_k K_k (f[c+k-1] - f[c-k])
+__device__ __forceinline__ V4 dzm(const W12 &s) {
+    V4 a;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int c = 4 + i;
+        float t = 0.f;
+        t += K1 * (s.w[c] - s.w[c - 1]);
+        t += K2 * (s.w[c + 1] - s.w[c - 2]);
+        t += K3 * (s.w[c + 2] - s.w[c - 3]);
+        t += K4 * (s.w[c + 3] - s.w[c - 4]);
+        a.v[i] = t;
+    }
+    return a;
+}
+
+__device__ __forceinline__ void f4_to(const float4 &a, float o[4]) {
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = a.z;
+    o[3] = a.w;
+}
+__device__ __forceinline__ float4 to_f4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
+
+// thread -> cells: 8 float4 columns x 32 rows per tile
+struct CellMap {
+    int r, c;     // box coordinates of the first of the four cells
+    int ci;       // core-tile index of the first cell
+    int lx, lz;   // local row / column of the first cell
+    size_t gi;    // packed index of the first cell
+    bool live;    // the row is updated and the first cell's column < nzpml-NOP
+    bool ok[4];   // cell inside the update region
+    bool frame[4];
+    bool image[4];  // inside the imaging interior [pml, n-pml)
+};
+
+__device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, const ShotGeo &g) {
+    CellMap m;
+    const int tz = threadIdx.x & 7, tr = threadIdx.x >> 3;
+    m.r = tr + HALO;
+    m.c = 4 * tz + HALO;
+    m.ci = tr * TZ + 4 * tz;
+    m.lx = t.x0 + tr;
+    m.lz = t.z0 + 4 * tz;
+    m.gi = (size_t)(g.row0 + m.lx) * p.P + m.lz;
+    const bool row_ok = m.lx >= NOP && m.lx < g.nxpml - NOP;
+    m.live = row_ok && m.lz < p.nzpml - NOP;  // lz, P are multiples of 4, so lz+3 < P
+    const int pml = p.pml, nzpml = p.nzpml, nxpml = g.nxpml;
+    const bool xf = m.lx < pml || m.lx > nxpml - pml;
+    const bool xi = m.lx >= pml && m.lx < nxpml - pml;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int z = m.lz + j;
+        m.ok[j] = row_ok && z >= NOP && z < nzpml - NOP;
+        m.frame[j] = xf || z < pml || z > nzpml - pml;
+        m.image[j] = m.ok[j] && xi && z >= pml && z < nzpml - pml;
+    }
+    return m;
+}
+
+__device__ __forceinline__ void core4(const float *core, int slot, int ci, float o[4]) {
+    f4_to(ld4(core + slot * CORE + ci), o);
+}
+
+struct Damp {
+    float d1[4], d2[4], d3[4], d4[4];
+};
+__device__ __forceinline__ Damp make_damp(const Params &p, const float x[4], const float z[4]) {
+    Damp d;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        d.d1[j] = 1.f - p.dt * x[j] / 2;
+        d.d2[j] = 1.f + p.dt * x[j] / 2;
+        d.d3[j] = 1.f - p.dt * z[j] / 2;
+        d.d4[j] = 1.f + p.dt * z[j] / 2;
+    }
+    return d;
+}
+
+struct VState {
+    float vx[4], vz[4], mx[4], mz[4];
+};
+struct SState {
+    float xx[4], zz[4], xz[4], mxx[4], mzz[4], mxz[4];
+};
+
+// velocity update of one field set on this thread's four cells:
+//   vx += dir*ib*(dtdx*ax + dtdz*bz),  vz += dir*ib*(dtdx*dx_ + dtdz*cz)
+// with the split form in frame cells; stores the new state.
+template <bool FRAME>
+__device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const FieldSet &f, VState &s,
+                                        const float ib[4], const Damp &d, float dir, const V4 &ax, const V4 &bz,
+                                        const V4 &dx_, const V4 &cz) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (!m.ok[j]) continue;
+        const float cx = dir * ib[j] * p.dtdx, cz_ = dir * ib[j] * p.dtdz;
+        if (FRAME && m.frame[j]) {
+            const float xx = (d.d1[j] * s.mx[j] + cx * ax.v[j]) / d.d2[j];
+            const float xz = (d.d3[j] * (s.vx[j] - s.mx[j]) + cz_ * bz.v[j]) / d.d4[j];
+            const float zx = (d.d1[j] * s.mz[j] + cx * dx_.v[j]) / d.d2[j];
+            const float zz = (d.d3[j] * (s.vz[j] - s.mz[j]) + cz_ * cz.v[j]) / d.d4[j];
+            s.mx[j] = xx;
+            s.mz[j] = zx;
+            s.vx[j] = xx + xz;
+            s.vz[j] = zx + zz;
+        } else {
+            s.vx[j] = s.vx[j] + (cx * ax.v[j] + cz_ * bz.v[j]);
+            s.vz[j] = s.vz[j] + (cx * dx_.v[j] + cz_ * cz.v[j]);
+        }
+    }
+    st4(f.vx + m.gi, to_f4(s.vx));
+    st4(f.vz + m.gi, to_f4(s.vz));
+    if (FRAME) {
+        st4(f.mvx + m.gi, to_f4(s.mx));
+        st4(f.mvz + m.gi, to_f4(s.mz));
+    }
+}
+
+// stress update of one field set from velocity derivatives
+//   a = D-x vx, b = D-z vz, c = D+z vx, d = D+x vz
+// with optional Born terms added to the split parts first (born != nullptr).
+template <bool FRAME>
+__device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const FieldSet &f, SState &s,
+                                        const float lam[4], const float mu[4], const Damp &dm, float dir, const V4 &a,
+                                        const V4 &b, const V4 &c, const V4 &d, const float (*born)[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (!m.ok[j]) continue;
+        const float l2m = lam[j] + 2 * mu[j];
+        const float ax = dir * p.dtdx * a.v[j], bz = dir * p.dtdz * b.v[j];
+        const float cz = dir * p.dtdz * c.v[j], dx_ = dir * p.dtdx * d.v[j];
+        // Born increments of the six split parts (xx_x, xx_z, zz_x, zz_z, xz_x, xz_z)
+        float bxx_x = 0.f, bxx_z = 0.f, bzz_x = 0.f, bzz_z = 0.f, bxz_x = 0.f, bxz_z = 0.f;
+        if (born) {
+            bxx_x = born[0][j];
+            bxx_z = born[1][j];
+            bzz_x = born[2][j];
+            bzz_z = born[3][j];
+            bxz_x = born[4][j];
+            bxz_z = born[5][j];
+        }
+        if (FRAME && m.frame[j]) {
+            const float d1 = dm.d1[j], d2 = dm.d2[j], d3 = dm.d3[j], d4 = dm.d4[j];
+            const float nxx_x = (d1 * (s.mxx[j] + bxx_x) + l2m * ax) / d2;
+            const float nxx_z = (d3 * ((s.xx[j] - s.mxx[j]) + bxx_z) + lam[j] * bz) / d4;
+            const float nzz_x = (d1 * (s.mzz[j] + bzz_x) + lam[j] * ax) / d2;
+            const float nzz_z = (d3 * ((s.zz[j] - s.mzz[j]) + bzz_z) + l2m * bz) / d4;
+            const float nxz_x = (d1 * (s.mxz[j] + bxz_x) + mu[j] * dx_) / d2;
+            const float nxz_z = (d3 * ((s.xz[j] - s.mxz[j]) + bxz_z) + mu[j] * cz) / d4;
+            s.mxx[j] = nxx_x;
+            s.mzz[j] = nzz_x;
+            s.mxz[j] = nxz_x;
+            s.xx[j] = nxx_x + nxx_z;
+            s.zz[j] = nzz_x + nzz_z;
+            s.xz[j] = nxz_x + nxz_z;
+        } else {
+            s.xx[j] = s.xx[j] + (bxx_x + bxx_z) + (l2m * ax + lam[j] * bz);
+            s.zz[j] = s.zz[j] + (bzz_x + bzz_z) + (lam[j] * ax + l2m * bz);
+            s.xz[j] = s.xz[j] + (bxz_x + bxz_z) + mu[j] * (dx_ + cz);
+        }
+    }
+    st4(f.txx + m.gi, to_f4(s.xx));
+    st4(f.tzz + m.gi, to_f4(s.zz));
+    st4(f.txz + m.gi, to_f4(s.xz));
+    if (FRAME) {
+        st4(f.mtxx + m.gi, to_f4(s.mxx));
+        st4(f.mtzz + m.gi, to_f4(s.mzz));
+        st4(f.mtxz + m.gi, to_f4(s.mxz));
+    }
+}
+
+// ----------------------------------------------------------------------------
+// the tile pipeline shared by the four kernels
+// ----------------------------------------------------------------------------
+// Shared-memory stage: NB halo boxes followed by NC core tiles.
+__device__ __forceinline__ float *smem_base() {
+    extern __shared__ __align__(1024) unsigned char sfwi_smem[];
+    return reinterpret_cast<float *>(sfwi_smem);
+}
+
+struct TileCtx {
+    Tile t;
+    ShotGeo g;
+    int brow, bcol;  // packed row / column of box element (0,0)
+    int crow, ccol;  // packed row / column of core element (0,0)
+};
+__device__ __forceinline__ TileCtx tile_ctx(const Params &p, int ti) {
+    TileCtx c;
+    c.t = p.tiles[ti];
+    c.g = p.geo[c.t.shot];
+    c.brow = c.g.row0 + c.t.x0 - HALO;
+    c.bcol = c.t.z0 - HALO;
+    c.crow = c.g.row0 + c.t.x0;
+    c.ccol = c.t.z0;
+    return c;
+}
+
+// Runs the pipeline over tiles handed out dynamically: thread 0 takes the
+// next tile index from this launch's counter (atomicAdd) when it starts that
+// tile's loads, and publishes it in s_tile[stage] for the other threads, so
+// SMs that drew cheap tiles simply take more of them.
+//   issue(ctx, stage_ptr, bar): thread 0 starts the loads of one tile (it arms
+//                               `bar` with expect_tx first);
+//   body(ctx, stage_ptr):       all threads, once the tile has landed.
+template <int STAGE_FLOATS, class Issue, class Body>
+__device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body) {
+    __shared__ uint64_t bar[NSTAGE];
+    __shared__ int s_tile[NSTAGE];
+    float *sm = smem_base();
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NSTAGE; s++) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+        const int t0 = atomicAdd(counter, 1);
+        s_tile[0] = t0;
+        if (t0 < p.ntiles) issue(tile_ctx(p, t0), sm, &bar[0]);
+    }
+    __syncthreads();
+    for (int k = 0;; k++) {
+        const int st = k % NSTAGE, nst = (k + 1) % NSTAGE;
+        const int ti = s_tile[st];
+        if (ti >= p.ntiles) break;
+        bool next = false;
+        if (threadIdx.x == 0) {
+            const int tn = atomicAdd(counter, 1);
+            s_tile[nst] = tn;
+            next = tn < p.ntiles;
+            if (next) issue(tile_ctx(p, tn), sm + nst * STAGE_FLOATS, &bar[nst]);
+        }
+        const bool ok = mbar_wait(&bar[st], (uint32_t)((k / NSTAGE) & 1));
+        if (__syncthreads_or(!ok)) {
+            // a tile never landed: flag it, let the copy already issued for the
+            // next tile finish (bounded) so no copy targets freed shared
+            // memory, and leave together
+            if (threadIdx.x == 0) {
+                atomicExch(p.err, 1);
+                if (next) mbar_wait(&bar[nst], (uint32_t)(((k + 1) / NSTAGE) & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        body(tile_ctx(p, ti), sm + st * STAGE_FLOATS);
+        // this stage is refilled by the asynchronous proxy two tiles later
+        fence_proxy_async();
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward velocity sweep
+// ---------------------------------------------------------------------------
+template <bool BORN>
+struct FwdV {
+    static constexpr int NB = BORN ? 6 : 3;
+    // core slots: 0 ib, 1 vx, 2 vz, 3 dampx, 4 dampz, 5 mvx, 6 mvz, [7 svx, 8 svz, 9 smvx, 10 smvz]
+    static constexpr int NC = BORN ? 11 : 7;
+    static constexpr int STAGE = NB * BOX + NC * CORE;
+};
+
+template <bool BORN>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_fwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
+            int it) {
+    using S = FwdV<BORN>;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME;
+        uint32_t bytes = S::NB * BOX_BYTES + (BORN ? 5 : 3) * CORE_BYTES;
+        if (frame) bytes += (BORN ? 6 : 4) * CORE_BYTES;
+        mbar_expect_tx(bar, bytes);
+        float *core = s + S::NB * BOX;
+        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_TXX, bar);
+        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_TZZ, bar);
+        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, BG_TXZ, bar);
+        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_IB, bar);
+        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, BG_VX, bar);
+        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_VZ, bar);
+        if (frame) {
+            tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
+            tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
+            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, BG_MVX, bar);
+            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, BG_MVZ, bar);
+        }
+        if (BORN) {
+            tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, SC_TXX, bar);
+            tma_load(s + 4 * BOX, &tbox, c.bcol, c.brow, SC_TZZ, bar);
+            tma_load(s + 5 * BOX, &tbox, c.bcol, c.brow, SC_TXZ, bar);
+            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, SC_VX, bar);
+            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, SC_VZ, bar);
+            if (frame) {
+                tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, SC_MVX, bar);
+                tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, SC_MVZ, bar);
+            }
+        }
+    };
+    auto body = [&](const TileCtx &c, float *s) {
+        float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
+        const float *core = s + S::NB * BOX;
+        if ((c.t.flags & TILE_SOURCE) && threadIdx.x == 0) {
+            // explosive source into the total txx and tzz (seen by this sweep only)
+            const int r = c.g.isx - (c.t.x0 - HALO), cc = c.g.isz - c.bcol;
+            const float sv = p.sou[it];
+            s_xx[r * BZ + cc] += sv;
+            s_zz[r * BZ + cc] += sv;
+        }
+        __syncthreads();
+        const CellMap m = cell_map(p, c.t, c.g);
+        if (!m.live) return;
+        const bool frame = c.t.flags & TILE_FRAME;
+        float ib[4];
+        core4(core, 0, m.ci, ib);
+        Damp d;
+        if (frame) {
+            float x[4], z[4];
+            core4(core, 3, m.ci, x);
+            core4(core, 4, m.ci, z);
+            d = make_damp(p, x, z);
+        }
+        {
+            VState st;
+            core4(core, 1, m.ci, st.vx);
+            core4(core, 2, m.ci, st.vz);
+            const V4 ax = dxp(s_xx, m.r, m.c);
+            const V4 bz = dzm(loadw(s_xz, m.r, m.c));
+            const V4 dx_ = dxm(s_xz, m.r, m.c);
+            const V4 cz = dzp(loadw(s_zz, m.r, m.c));
+            if (frame) {
+                core4(core, 5, m.ci, st.mx);
+                core4(core, 6, m.ci, st.mz);
+                v_apply<true>(p, m, p.bg, st, ib, d, 1.f, ax, bz, dx_, cz);
+            } else {
+                v_apply<false>(p, m, p.bg, st, ib, d, 1.f, ax, bz, dx_, cz);
+            }
+        }
+        if (BORN) {
+            const float *b_xx = s + 3 * BOX, *b_zz = s + 4 * BOX, *b_xz = s + 5 * BOX;
+            VState st;
+            core4(core, 7, m.ci, st.vx);
+            core4(core, 8, m.ci, st.vz);
+            const V4 ax = dxp(b_xx, m.r, m.c);
+            const V4 bz = dzm(loadw(b_xz, m.r, m.c));
+            const V4 dx_ = dxm(b_xz, m.r, m.c);
+            const V4 cz = dzp(loadw(b_zz, m.r, m.c));
+            if (frame) {
+                core4(core, 9, m.ci, st.mx);
+                core4(core, 10, m.ci, st.mz);
+                v_apply<true>(p, m, p.sc, st, ib, d, 1.f, ax, bz, dx_, cz);
+            } else {
+                v_apply<false>(p, m, p.sc, st, ib, d, 1.f, ax, bz, dx_, cz);
+            }
+        }
+    };
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body);
+}
+
+// ---------------------------------------------------------------------------
+// forward stress sweep (+ Born source + scattered stress), records, strips
+// ---------------------------------------------------------------------------
+template <bool BORN>
+struct FwdS {
+    static constexpr int NB = BORN ? 4 : 2;
+    // core: 0 lam, 1 mu, 2 txx, 3 tzz, 4 txz, 5 dampx, 6 dampz, 7 mtxx, 8 mtzz, 9 mtxz,
+    //       [10 bp, 11 bs, 12 stxx, 13 stzz, 14 stxz, 15 smtxx, 16 smtzz, 17 smtxz]
+    static constexpr int NC = BORN ? 18 : 10;
+    static constexpr int STAGE = NB * BOX + NC * CORE;
+};
+
+// the cells of one edge-strip band (0 top, 1 bottom, 2 left, 3 right) and the
+// slot of a cell inside one step's component block (sfwi_common.cuh layout)
+struct Band {
+    int x0, x1, z0, z1;
+};
+__device__ __forceinline__ Band band_rect(int band, int pml, int nxpml, int nzpml) {
+    Band b;
+    if (band < 2) {
+        b.x0 = pml;
+        b.x1 = nxpml - pml;
+        b.z0 = band == 0 ? pml - NOP : nzpml - pml - NOP;
+        b.z1 = b.z0 + 2 * NOP;
+    } else {
+        b.z0 = pml;
+        b.z1 = nzpml - pml;
+        b.x0 = band == 2 ? pml - NOP : nxpml - pml - NOP;
+        b.x1 = b.x0 + 2 * NOP;
+    }
+    return b;
+}
+__device__ __forceinline__ int band_slot(int band, int lx, int lz, int pml, int nxpml, int nzpml, int nx, int nz) {
+    if (band == 0) return (lx - pml) * 8 + (lz - (pml - NOP));
+    if (band == 1) return 8 * nx + (lx - pml) * 8 + (lz - (nzpml - pml - NOP));
+    if (band == 2) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
+    return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
+}
+
+template <bool BORN>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_fwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
+            int it) {
+    using S = FwdS<BORN>;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME;
+        uint32_t bytes = S::NB * BOX_BYTES + (BORN ? 10 : 5) * CORE_BYTES;
+        if (frame) bytes += (BORN ? 8 : 5) * CORE_BYTES;
+        mbar_expect_tx(bar, bytes);
+        float *core = s + S::NB * BOX;
+        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_VX, bar);
+        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_VZ, bar);
+        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_LAM, bar);
+        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, C_MU, bar);
+        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_TXX, bar);
+        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, BG_TZZ, bar);
+        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, BG_TXZ, bar);
+        if (frame) {
+            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
+            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
+            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, BG_MTXX, bar);
+            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, BG_MTZZ, bar);
+            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, BG_MTXZ, bar);
+        }
+        if (BORN) {
+            tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, SC_VX, bar);
+            tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, SC_VZ, bar);
+            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, C_BP, bar);
+            tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, C_BS, bar);
+            tma_load(core + 12 * CORE, &tcore, c.ccol, c.crow, SC_TXX, bar);
+            tma_load(core + 13 * CORE, &tcore, c.ccol, c.crow, SC_TZZ, bar);
+            tma_load(core + 14 * CORE, &tcore, c.ccol, c.crow, SC_TXZ, bar);
+            if (frame) {
+                tma_load(core + 15 * CORE, &tcore, c.ccol, c.crow, SC_MTXX, bar);
+                tma_load(core + 16 * CORE, &tcore, c.ccol, c.crow, SC_MTZZ, bar);
+                tma_load(core + 17 * CORE, &tcore, c.ccol, c.crow, SC_MTXZ, bar);
+            }
+        }
+    };
+    auto body = [&](const TileCtx &c, float *s) {
+        const float *s_vx = s, *s_vz = s + BOX;
+        const float *b_vx = s + 2 * BOX, *b_vz = s + 3 * BOX;
+        const float *core = s + S::NB * BOX;
+        const CellMap m = cell_map(p, c.t, c.g);
+        const bool frame = c.t.flags & TILE_FRAME;
+        if (m.live) {
+            float lam[4], mu[4];
+            core4(core, 0, m.ci, lam);
+            core4(core, 1, m.ci, mu);
+            Damp dm;
+            if (frame) {
+                float x[4], z[4];
+                core4(core, 5, m.ci, x);
+                core4(core, 6, m.ci, z);
+                dm = make_damp(p, x, z);
+            }
+            const V4 a = dxm(s_vx, m.r, m.c);
+            const V4 cc = dzp(loadw(s_vx, m.r, m.c));
+            const V4 b = dzm(loadw(s_vz, m.r, m.c));
+            const V4 d = dxp(s_vz, m.r, m.c);
+            {
+                SState st;
+                core4(core, 2, m.ci, st.xx);
+                core4(core, 3, m.ci, st.zz);
+                core4(core, 4, m.ci, st.xz);
+                if (frame) {
+                    core4(core, 7, m.ci, st.mxx);
+                    core4(core, 8, m.ci, st.mzz);
+                    core4(core, 9, m.ci, st.mxz);
+                    s_apply<true>(p, m, p.bg, st, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
+                } else {
+                    s_apply<false>(p, m, p.bg, st, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
+                }
+            }
+            if (BORN) {
+                // Born virtual source from the updated background velocity
+                // (add_born_source_components, sfwi-stage2/born.cu:788-798); bp/bs
+                // are zero outside the Born region
+                float bp[4], bs[4], born[6][4];
+                core4(core, 10, m.ci, bp);
+                core4(core, 11, m.ci, bs);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float mix = bp[j] - 2 * bs[j];
+                    born[0][j] = p.dt * (bp[j] * a.v[j] * p.idx);
+                    born[1][j] = p.dt * (mix * b.v[j] * p.idz);
+                    born[2][j] = p.dt * (mix * a.v[j] * p.idx);
+                    born[3][j] = p.dt * (bp[j] * b.v[j] * p.idz);
+                    born[4][j] = p.dt * (bs[j] * d.v[j] * p.idx);
+                    born[5][j] = p.dt * (bs[j] * cc.v[j] * p.idz);
+                }
+                const V4 as = dxm(b_vx, m.r, m.c);
+                const V4 cs = dzp(loadw(b_vx, m.r, m.c));
+                const V4 bs_ = dzm(loadw(b_vz, m.r, m.c));
+                const V4 ds = dxp(b_vz, m.r, m.c);
+                SState st;
+                core4(core, 12, m.ci, st.xx);
+                core4(core, 13, m.ci, st.zz);
+                core4(core, 14, m.ci, st.xz);
+                if (frame) {
+                    core4(core, 15, m.ci, st.mxx);
+                    core4(core, 16, m.ci, st.mzz);
+                    core4(core, 17, m.ci, st.mxz);
+                    s_apply<true>(p, m, p.sc, st, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
+                } else {
+                    s_apply<false>(p, m, p.sc, st, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
+                }
+            }
+        }
+        // receivers on this tile's core: syn[it][trace] (time-major)
+        if ((c.t.flags & TILE_RECV) && threadIdx.x < TX) {
+            const int lx = c.t.x0 + threadIdx.x;
+            const int zc = c.g.igz - c.t.z0;
+            if (lx < c.g.nxpml && zc >= 0 && zc < TZ) {
+                const int r = threadIdx.x + HALO, col = zc + HALO;
+                const int b0 = p.csr_start[c.g.csr0 + lx], b1 = p.csr_start[c.g.csr0 + lx + 1];
+                for (int k = b0; k < b1; k++) {
+                    const int tr = p.csr_trace[k];
+                    const size_t o = (size_t)it * p.ntr_tot + tr;
+                    if (BORN) {
+                        p.syn_z[o] = b_vz[r * BZ + col];
+                        p.syn_x[o] = b_vx[r * BZ + col];
+                        p.syn2_z[o] = s_vz[r * BZ + col];
+                        p.syn2_x[o] = s_vx[r * BZ + col];
+                    } else {
+                        p.syn_z[o] = s_vz[r * BZ + col];
+                        p.syn_x[o] = s_vx[r * BZ + col];
+                    }
+                }
+            }
+        }
+        // edge strips of the background velocity after this step: the core
+        // cells of this tile inside each of the four bands
+        if ((c.t.flags & TILE_STRIP) && p.strips) {
+            const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml, nz = nzpml - 2 * pml;
+            float *sb = p.strips + c.g.strip0 + (long long)it * strip_floats(c.g.nx, nz);
+            const long long cb = strip_comp_floats(c.g.nx, nz);
+            for (int band = 0; band < 4; band++) {
+                const Band bb = band_rect(band, pml, nxpml, nzpml);
+                const int rx0 = max(bb.x0, c.t.x0), rx1 = min(bb.x1, c.t.x0 + TX);
+                const int rz0 = max(bb.z0, c.t.z0), rz1 = min(bb.z1, c.t.z0 + TZ);
+                if (rx0 >= rx1 || rz0 >= rz1) continue;
+                const int w = rz1 - rz0, n = (rx1 - rx0) * w;
+                for (int i = threadIdx.x; i < n; i += NTHREADS) {
+                    const int lx = rx0 + i / w, lz = rz0 + i % w;
+                    const int bi = (lx - c.t.x0 + HALO) * BZ + (lz - c.t.z0 + HALO);
+                    const int slot = band_slot(band, lx, lz, pml, nxpml, nzpml, c.g.nx, nz);
+                    sb[slot] = s_vx[bi];
+                    sb[cb + slot] = s_vz[bi];
+                }
+            }
+        }
+    };
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body);
+}
+
+// ---------------------------------------------------------------------------
+// backward stress sweeps + imaging
+// ---------------------------------------------------------------------------
+struct BwdS {
+    static constexpr int NB = 4;  // vx, vz, avx, avz
+    // core: 0 lam, 1 mu, 2 txx, 3 tzz, 4 txz, 5 atxx, 6 atzz, 7 atxz,
+    //       8 dampx, 9 dampz, 10 mtxx, 11 mtzz, 12 mtxz, 13 amtxz, 14 glam, 15 gmu
+    static constexpr int NC = 16;
+    static constexpr int STAGE = NB * BOX + NC * CORE;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_bwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
+            int it, float adj_dir) {
+    using S = BwdS;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
+        const uint32_t bytes =
+            S::NB * BOX_BYTES + (8 + (frame ? 6 : 0) + (image ? 2 : 0)) * CORE_BYTES;
+        mbar_expect_tx(bar, bytes);
+        float *core = s + S::NB * BOX;
+        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_VX, bar);
+        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_VZ, bar);
+        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, AD_VX, bar);
+        tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, AD_VZ, bar);
+        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_LAM, bar);
+        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, C_MU, bar);
+        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_TXX, bar);
+        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, BG_TZZ, bar);
+        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, BG_TXZ, bar);
+        tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, AD_TXX, bar);
+        tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, AD_TZZ, bar);
+        tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, AD_TXZ, bar);
+        if (frame) {
+            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
+            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
+            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, BG_MTXX, bar);
+            tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, BG_MTZZ, bar);
+            tma_load(core + 12 * CORE, &tcore, c.ccol, c.crow, BG_MTXZ, bar);
+            tma_load(core + 13 * CORE, &tcore, c.ccol, c.crow, AD_MTXZ, bar);
+        }
+        if (image) {
+            tma_load(core + 14 * CORE, &tcore, c.ccol, c.crow, G_LAM, bar);
+            tma_load(core + 15 * CORE, &tcore, c.ccol, c.crow, G_MU, bar);
+        }
+    };
+    auto body = [&](const TileCtx &c, float *s) {
+        float *s_vx = s, *s_vz = s + BOX, *a_vx = s + 2 * BOX, *a_vz = s + 3 * BOX;
+        const float *core = s + S::NB * BOX;
+        const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml, nz = nzpml - 2 * pml;
+        if (c.t.flags & TILE_STRIP) {
+            // the saved strips of step `it` replace vx, vz in this sweep's view:
+            // the box cells inside each band (a cell in two bands holds the
+            // same value in both)
+            const float *sb = p.strips + c.g.strip0 + (long long)it * strip_floats(c.g.nx, nz);
+            const long long cb = strip_comp_floats(c.g.nx, nz);
+            const int bx = c.t.x0 - HALO, bz = c.bcol;
+            for (int band = 0; band < 4; band++) {
+                const Band bb = band_rect(band, pml, nxpml, nzpml);
+                const int rx0 = max(bb.x0, bx), rx1 = min(bb.x1, bx + BX);
+                const int rz0 = max(bb.z0, bz), rz1 = min(bb.z1, bz + BZ);
+                if (rx0 >= rx1 || rz0 >= rz1) continue;
+                const int w = rz1 - rz0, n = (rx1 - rx0) * w;
+                for (int i = threadIdx.x; i < n; i += NTHREADS) {
+                    const int lx = rx0 + i / w, lz = rz0 + i % w;
+                    const int bi = (lx - bx) * BZ + (lz - bz);
+                    const int slot = band_slot(band, lx, lz, pml, nxpml, nzpml, c.g.nx, nz);
+                    s_vx[bi] = sb[slot];
+                    s_vz[bi] = sb[cb + slot];
+                }
+            }
+        }
+        if ((c.t.flags & TILE_RECV) && threadIdx.x < BX) {
+            // the residual of step `it` replaces the adjoint velocity at the
+            // receivers in this sweep's view (the highest trace index wins
+            // where several traces share a cell)
+            const int lx = c.t.x0 - HALO + threadIdx.x;
+            const int zc = c.g.igz - c.bcol;
+            if (lx >= 0 && lx < nxpml && zc >= 0 && zc < BZ) {
+                const int b0 = p.csr_start[c.g.csr0 + lx], b1 = p.csr_start[c.g.csr0 + lx + 1];
+                if (b1 > b0) {
+                    const int tr = p.csr_trace[b1 - 1];
+                    const size_t o = (size_t)tr * p.nt + it;
+                    a_vz[threadIdx.x * BZ + zc] = p.res_z[o];
+                    a_vx[threadIdx.x * BZ + zc] = p.res_x[o];
+                }
+            }
+        }
+        __syncthreads();
+        const CellMap m = cell_map(p, c.t, c.g);
+        if (!m.live) return;
+        const bool frame = c.t.flags & TILE_FRAME;
+        float lam[4], mu[4];
+        core4(core, 0, m.ci, lam);
+        core4(core, 1, m.ci, mu);
+        Damp dm;
+        if (frame) {
+            float x[4], z[4];
+            core4(core, 8, m.ci, x);
+            core4(core, 9, m.ci, z);
+            dm = make_damp(p, x, z);
+        }
+        // reconstruction (direction -1) with strains
+        const V4 a = dxm(s_vx, m.r, m.c);
+        const V4 cc = dzp(loadw(s_vx, m.r, m.c));
+        const V4 b = dzm(loadw(s_vz, m.r, m.c));
+        const V4 d = dxp(s_vz, m.r, m.c);
+        {
+            SState st;
+            core4(core, 2, m.ci, st.xx);
+            core4(core, 3, m.ci, st.zz);
+            core4(core, 4, m.ci, st.xz);
+            if (frame) {
+                core4(core, 10, m.ci, st.mxx);
+                core4(core, 11, m.ci, st.mzz);
+                core4(core, 12, m.ci, st.mxz);
+                s_apply<true>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
+            } else {
+                s_apply<false>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
+            }
+        }
+        // adjoint stresses: txx' = x-part only, tzz' = z-part only, txz split
+        float axx[4], azz[4], axz[4], amxz[4];
+        core4(core, 5, m.ci, axx);
+        core4(core, 6, m.ci, azz);
+        core4(core, 7, m.ci, axz);
+        if (frame) core4(core, 13, m.ci, amxz);
+        const V4 aa = dxm(a_vx, m.r, m.c);
+        const V4 ca = dzp(loadw(a_vx, m.r, m.c));
+        const V4 ba = dzm(loadw(a_vz, m.r, m.c));
+        const V4 da = dxp(a_vz, m.r, m.c);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (!m.ok[j]) continue;
+            const float ax = adj_dir * p.dtdx * aa.v[j], bz = adj_dir * p.dtdz * ba.v[j];
+            const float cz = adj_dir * p.dtdz * ca.v[j], dx_ = adj_dir * p.dtdx * da.v[j];
+            if (frame && m.frame[j]) {
+                const float d1 = dm.d1[j], d2 = dm.d2[j], d3 = dm.d3[j], d4 = dm.d4[j];
+                axx[j] = (d1 * axx[j] + ax) / d2;
+                azz[j] = (d3 * azz[j] + bz) / d4;
+                const float nx_ = (d1 * amxz[j] + dx_) / d2;
+                const float nz_ = (d3 * (axz[j] - amxz[j]) + cz) / d4;
+                amxz[j] = nx_;
+                axz[j] = nx_ + nz_;
+            } else {
+                axx[j] = axx[j] + ax;
+                azz[j] = azz[j] + bz;
+                axz[j] = axz[j] + (dx_ + cz);
+            }
+        }
+        st4(p.ad.txx + m.gi, to_f4(axx));
+        st4(p.ad.tzz + m.gi, to_f4(azz));
+        st4(p.ad.txz + m.gi, to_f4(axz));
+        if (frame) st4(p.ad.mtxz + m.gi, to_f4(amxz));
+        // zero-lag imaging of the lambda and mu kernels (interior cells)
+        if (c.t.flags & TILE_IMAGE) {
+            float gl[4], gm[4];
+            core4(core, 14, m.ci, gl);
+            core4(core, 15, m.ci, gm);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (!m.image[j]) continue;
+                const float gxx = a.v[j] * p.idx, gzz = b.v[j] * p.idz;
+                const float gxz = cc.v[j] * p.idz, gzx = d.v[j] * p.idx;
+                const float lg = -((gxx + gzz) * (axx[j] + azz[j]));
+                const float mg = -2 * (gxx * axx[j] + gzz * azz[j]) - (gxz + gzx) * axz[j];
+                gl[j] += lg;
+                gm[j] += mg;
+            }
+            st4(p.glam + m.gi, to_f4(gl));
+            st4(p.gmu + m.gi, to_f4(gm));
+        }
+    };
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
+}
+
+// ---------------------------------------------------------------------------
+// backward velocity sweeps + illumination
+// ---------------------------------------------------------------------------
+struct BwdV {
+    static constexpr int NB = 8;  // txx, tzz, txz, atxx->P, atzz->Q, atxz->R, lam, mu
+    // core: 0 ib, 1 vx, 2 vz, 3 avx, 4 avz, 5 dampx, 6 dampz, 7 mvx, 8 mvz, 9 amvx, 10 amvz, 11 illum
+    static constexpr int NC = 12;
+    static constexpr int STAGE = NB * BOX + NC * CORE;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_bwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
+            int it, float adj_dir) {
+    using S = BwdV;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
+        const uint32_t bytes = S::NB * BOX_BYTES + (5 + (frame ? 6 : 0) + (image ? 1 : 0)) * CORE_BYTES;
+        mbar_expect_tx(bar, bytes);
+        float *core = s + S::NB * BOX;
+        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_TXX, bar);
+        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_TZZ, bar);
+        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, BG_TXZ, bar);
+        tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, AD_TXX, bar);
+        tma_load(s + 4 * BOX, &tbox, c.bcol, c.brow, AD_TZZ, bar);
+        tma_load(s + 5 * BOX, &tbox, c.bcol, c.brow, AD_TXZ, bar);
+        tma_load(s + 6 * BOX, &tbox, c.bcol, c.brow, C_LAM, bar);
+        tma_load(s + 7 * BOX, &tbox, c.bcol, c.brow, C_MU, bar);
+        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_IB, bar);
+        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, BG_VX, bar);
+        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_VZ, bar);
+        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, AD_VX, bar);
+        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, AD_VZ, bar);
+        if (frame) {
+            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
+            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
+            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, BG_MVX, bar);
+            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, BG_MVZ, bar);
+            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, AD_MVX, bar);
+            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, AD_MVZ, bar);
+        }
+        if (image) tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, G_ILL, bar);
+    };
+    auto body = [&](const TileCtx &c, float *s) {
+        const float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
+        float *s_P = s + 3 * BOX, *s_Q = s + 4 * BOX, *s_R = s + 5 * BOX;
+        const float *s_l = s + 6 * BOX, *s_u = s + 7 * BOX;
+        const float *core = s + S::NB * BOX;
+        // Lame-weighted adjoint stresses, in place:
+        //   P = (l+2m) txx + l tzz,  Q = l txx + (l+2m) tzz,  R = m txz
+        for (int i = threadIdx.x; i < BOX / 4; i += NTHREADS) {
+            float xx[4], zz[4], xz[4], l[4], u[4], P_[4], Q_[4], R_[4];
+            f4_to(ld4(s_P + 4 * i), xx);
+            f4_to(ld4(s_Q + 4 * i), zz);
+            f4_to(ld4(s_R + 4 * i), xz);
+            f4_to(ld4(s_l + 4 * i), l);
+            f4_to(ld4(s_u + 4 * i), u);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float l2m = l[j] + 2 * u[j];
+                P_[j] = l2m * xx[j] + l[j] * zz[j];
+                Q_[j] = l[j] * xx[j] + l2m * zz[j];
+                R_[j] = u[j] * xz[j];
+            }
+            st4(s_P + 4 * i, to_f4(P_));
+            st4(s_Q + 4 * i, to_f4(Q_));
+            st4(s_R + 4 * i, to_f4(R_));
+        }
+        __syncthreads();
+        const CellMap m = cell_map(p, c.t, c.g);
+        if (!m.live) return;
+        const bool frame = c.t.flags & TILE_FRAME;
+        float ib[4];
+        core4(core, 0, m.ci, ib);
+        Damp dm;
+        if (frame) {
+            float x[4], z[4];
+            core4(core, 5, m.ci, x);
+            core4(core, 6, m.ci, z);
+            dm = make_damp(p, x, z);
+        }
+        {
+            VState st;
+            core4(core, 1, m.ci, st.vx);
+            core4(core, 2, m.ci, st.vz);
+            const V4 ax = dxp(s_xx, m.r, m.c);
+            const V4 bz = dzm(loadw(s_xz, m.r, m.c));
+            const V4 dx_ = dxm(s_xz, m.r, m.c);
+            const V4 cz = dzp(loadw(s_zz, m.r, m.c));
+            if (frame) {
+                core4(core, 7, m.ci, st.mx);
+                core4(core, 8, m.ci, st.mz);
+                v_apply<true>(p, m, p.bg, st, ib, dm, -1.f, ax, bz, dx_, cz);
+            } else {
+                v_apply<false>(p, m, p.bg, st, ib, dm, -1.f, ax, bz, dx_, cz);
+            }
+            if (c.t.flags & TILE_IMAGE) {
+                float il[4];
+                core4(core, 11, m.ci, il);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (m.image[j]) il[j] += st.vx[j] * st.vx[j] + st.vz[j] * st.vz[j];
+                st4(p.illum + m.gi, to_f4(il));
+            }
+        }
+        {
+            VState st;
+            core4(core, 3, m.ci, st.vx);
+            core4(core, 4, m.ci, st.vz);
+            const V4 ax = dxp(s_P, m.r, m.c);
+            const V4 bz = dzm(loadw(s_R, m.r, m.c));
+            const V4 dx_ = dxm(s_R, m.r, m.c);
+            const V4 cz = dzp(loadw(s_Q, m.r, m.c));
+            if (frame) {
+                core4(core, 9, m.ci, st.mx);
+                core4(core, 10, m.ci, st.mz);
+                v_apply<true>(p, m, p.ad, st, ib, dm, adj_dir, ax, bz, dx_, cz);
+            } else {
+                v_apply<false>(p, m, p.ad, st, ib, dm, adj_dir, ax, bz, dx_, cz);
+            }
+        }
+    };
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+constexpr size_t SMEM_ALIGN_SLACK = 1024;
+template <int STAGE>
+constexpr size_t stage_smem() {
+    return (size_t)NSTAGE * STAGE * sizeof(float) + SMEM_ALIGN_SLACK;
+}
+
+static int g_nsm = 0;
+
+cudaError_t configure_step_kernels() {
+    cudaError_t e;
+#define SET_SMEM(K, BYTES) \
+    if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(BYTES))) != cudaSuccess) return e;
+    SET_SMEM(k_fwd_v<true>, stage_smem<FwdV<true>::STAGE>());
+    SET_SMEM(k_fwd_v<false>, stage_smem<FwdV<false>::STAGE>());
+    SET_SMEM(k_fwd_s<true>, stage_smem<FwdS<true>::STAGE>());
+    SET_SMEM(k_fwd_s<false>, stage_smem<FwdS<false>::STAGE>());
+    SET_SMEM(k_bwd_s, stage_smem<BwdS::STAGE>());
+    SET_SMEM(k_bwd_v, stage_smem<BwdV::STAGE>());
+#undef SET_SMEM
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+static int persistent_grid(int ntiles) { return ntiles < g_nsm ? ntiles : g_nsm; }
+
+void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
+                        cudaStream_t st) {
+    const int grid = persistent_grid(p.ntiles);
+    switch (which) {
+        case 0:
+            if (born)
+                k_fwd_v<true><<<grid, NTHREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+            else
+                k_fwd_v<false><<<grid, NTHREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+            break;
+        case 1:
+            if (born)
+                k_fwd_s<true><<<grid, NTHREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+            else
+                k_fwd_s<false><<<grid, NTHREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+            break;
+        case 2:
+            k_bwd_s<<<grid, NTHREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            break;
+        default:
+            k_bwd_v<<<grid, NTHREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            break;
+    }
+}
+
+void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st) {
+    launch_step_kernel(0, p, tm, it, born, 1.f, st);
+    launch_step_kernel(1, p, tm, it, born, 1.f, st);
+}
+
+void launch_bwd_step(const Params &p, const TmaMaps &tm, int it, float adj_dir, cudaStream_t st) {
+    launch_step_kernel(2, p, tm, it, false, adj_dir, st);
+    launch_step_kernel(3, p, tm, it, false, adj_dir, st);
+}
+
+}  // namespace sfwi

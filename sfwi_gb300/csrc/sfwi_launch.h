@@ -1,0 +1,58 @@
+// sfwi_launch.h — host-side launch interface of the kernels (one definition
+// of each argument block, shared by the kernel files and the engine).
+#pragma once
+#include <cuda.h>  // CUtensorMap (types only; the driver is reached through cudaGetDriverEntryPoint)
+
+#include "sfwi_common.cuh"
+
+namespace sfwi {
+
+// sfwi_kernels.cu
+// TMA descriptors of the packed grid: 3-D [array][row][column], boxes of
+// (TX+2*HALO) x (TZ+2*HALO) and TX x TZ floats
+struct TmaMaps {
+    CUtensorMap box, core;
+};
+cudaError_t configure_step_kernels();
+void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st);
+void launch_bwd_step(const Params &p, const TmaMaps &tm, int it, float adj_dir, cudaStream_t st);
+// one kernel of a step: 0 fwd v, 1 fwd s, 2 bwd s, 3 bwd v
+void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
+                        cudaStream_t st);
+
+// sfwi_aux.cu
+struct SetupArgs {
+    int X, P, nzpml, pml, allnz, stage, born_lo;
+    float dt;
+    const float *vp_all, *vs_all, *rho_all, *dvp_all, *dvs_all;
+    float *ib, *lam, *mu, *dampx, *dampz, *bp, *bs, *vp, *vs, *rho;
+    const ShotGeo *geo;
+};
+void launch_setup(const SetupArgs &a, int nshots, int max_nxpml, cudaStream_t st);
+void launch_transpose(const float *in, float *out, int nt, int ntr, cudaStream_t st);
+void launch_residual_l2(int stage, int nt, int ntr_tot, const float *syn_z, const float *syn_x, const float *syn2_z,
+                        const float *syn2_x, const float *obs_z, const float *obs_x, float *res_z, float *res_x,
+                        double *trace_misfit, cudaStream_t st);
+struct FinalArgs {
+    int allnx, allnz, P, pml, nshots;
+    const ShotGeo *geo;
+    const float *glam, *gmu, *illum, *vp, *vs, *rho;
+    double *gpp, *gps, *gil;
+};
+void launch_finalize(const FinalArgs &a, cudaStream_t st);
+
+// sfwi_ot.cu
+struct OtArgs {
+    int kind, nt, ntr, stage;
+    double dt;
+    const float *cal_z, *cal_x;    // [ntr][nt] prediction (stage 2: scattered part)
+    const float *cal2_z, *cal2_x;  // stage 2: background part added to cal (may be null)
+    const float *obs_z, *obs_x;
+    float *res_z, *res_x;
+    const double *sigma;          // [ntr][2] (z, x)
+    double *trace_misfit;         // [ntr][2]
+};
+cudaError_t launch_ot(const OtArgs &a, cudaStream_t st);
+size_t ot_smem_bytes(int nt);
+
+}  // namespace sfwi

@@ -1,0 +1,186 @@
+// sfwi_ot.cu — per-trace 1D quadratic-Wasserstein misfit and adjoint source.
+//
+// The reference declares OT, OT_power and OT_alltrace (sfwi-stage1/FD2DGPU.cuh:
+// 21-25, argument order obs_x, obs_z, cal_x, cal_z, res_x, res_z, length,
+// tracenum, misfit) and defines none of them.  This is the 1D W2 misfit
+// between positive-normalised traces, written from its definition:
+//   weights   p(u) = exp((u - max u)/sigma)          (OT, OT_alltrace)
+//             p(u) = u^2 + 1e-3 sigma^2              (OT_power)
+//             sigma = max|obs| of the trace (OT, OT_power) or of the gather
+//   densities f = p(cal)/sum p(cal), g = p(obs)/sum p(obs)
+//   CDFs      F_k = sum_{j<=k} f_j,  G_k likewise
+//   transport T_k = G^-1(F_k) = dt (m + (F_k - G_{m-1})/g_m), G_{m-1} <= F_k < G_m
+//   misfit    W = sum_k ((k+1) dt - T_k)^2 f_k
+//   adjoint   A_j = ((j+1)dt - T_j)^2 - 2 sum_{k>=j} ((k+1)dt - T_k) f_k dt / g_m(k)
+//             res_i = (1/2) (A_i - sum_j f_j A_j) / sum p(cal) * p'(cal_i)
+// res is (1/2) dW/dcal, the scaling of the L2 residual (misfit sum r^2,
+// adjoint source r).  The CDFs, the quantile search and every sum are FP64.
+// One CTA handles one (trace, component); prefix and suffix sums are block
+// scans built on warp shuffles.
+#include <cfloat>
+
+#include "sfwi_launch.h"
+
+namespace sfwi {
+
+constexpr int OT_THREADS = 256;
+
+__device__ __forceinline__ double warp_incl_scan(double v) {
+    const int l = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, v, o);
+        if (l >= o) v += u;
+    }
+    return v;
+}
+
+// exclusive block scan of one value per thread (thread order)
+__device__ double block_excl_scan(double v, double *wsum) {
+    const double inc = warp_incl_scan(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        double t = l < nw ? wsum[l] : 0.0;
+        const double ti = warp_incl_scan(t);
+        if (l < nw) wsum[l] = ti - t;
+    }
+    __syncthreads();
+    const double r = wsum[w] + inc - v;
+    __syncthreads();
+    return r;
+}
+
+__device__ double block_reduce(double v, double *wsum) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) wsum[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += wsum[i];
+    __syncthreads();
+    return t;
+}
+
+__device__ double block_max(double v, double *wsum) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) wsum[w] = v;
+    __syncthreads();
+    double t = -DBL_MAX;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t = fmax(t, wsum[i]);
+    __syncthreads();
+    return t;
+}
+
+// in-place inclusive prefix (reverse=false) or suffix (reverse=true) sums of a[0..n)
+__device__ void block_scan_array(double *a, int n, bool reverse, double *wsum) {
+    const int chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * chunk, e = min(n, b + chunk);
+    double s = 0.0;
+    for (int i = b; i < e; i++) s += a[reverse ? n - 1 - i : i];
+    const double off = block_excl_scan(s, wsum);
+    double run = off;
+    for (int i = b; i < e; i++) {
+        const int k = reverse ? n - 1 - i : i;
+        run += a[k];
+        a[k] = run;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
+    extern __shared__ double ot_sm[];
+    __shared__ double wsum[32];
+    const int n = a.nt;
+    double *F = ot_sm, *G = F + n, *R = G + n, *Q = R + n;
+    const int tr = blockIdx.x >> 1, comp = blockIdx.x & 1;
+    const size_t o = (size_t)tr * n;
+    const float *cal = (comp ? a.cal_x : a.cal_z) + o;
+    const float *cal2 = a.cal2_z ? (comp ? a.cal2_x : a.cal2_z) + o : nullptr;
+    const float *obs = (comp ? a.obs_x : a.obs_z) + o;
+    float *res = (comp ? a.res_x : a.res_z) + o;
+    double sigma = a.sigma[2 * tr + comp];
+    if (!(sigma > 0.0)) sigma = 1.0;
+    const bool pw = a.kind == 2;
+    auto pred = [&](int k) -> double { return cal2 ? (double)(cal[k] + cal2[k]) : (double)cal[k]; };
+
+    double mc = -DBL_MAX, mo = -DBL_MAX;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        mc = fmax(mc, pred(k));
+        mo = fmax(mo, (double)obs[k]);
+    }
+    const double cmax = block_max(mc, wsum), omax = block_max(mo, wsum);
+    const double eps = 1e-3 * sigma * sigma;
+    auto pf = [&](double u) { return pw ? u * u + eps : exp((u - cmax) / sigma); };
+    auto pg = [&](double u) { return pw ? u * u + eps : exp((u - omax) / sigma); };
+
+    double sf = 0.0, sg = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double x = pf(pred(k)), y = pg((double)obs[k]);
+        F[k] = x;
+        G[k] = y;
+        sf += x;
+        sg += y;
+    }
+    const double Sf = block_reduce(sf, wsum), Sg = block_reduce(sg, wsum);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        F[k] /= Sf;
+        G[k] /= Sg;
+    }
+    __syncthreads();
+    block_scan_array(F, n, false, wsum);
+    block_scan_array(G, n, false, wsum);
+
+    double w = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double y = F[k];
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (G[mid] > y)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        const int m = lo;
+        const double gm = pg((double)obs[m]) / Sg;
+        const double Gm1 = m > 0 ? G[m - 1] : 0.0;
+        const double T = a.dt * (m + (y - Gm1) / gm);
+        const double r = (k + 1) * a.dt - T;
+        const double fk = pf(pred(k)) / Sf;
+        w += r * r * fk;
+        R[k] = r;
+        Q[k] = r * fk * a.dt / gm;
+    }
+    __syncthreads();
+    block_scan_array(Q, n, true, wsum);
+    double fa = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double A = R[k] * R[k] - 2.0 * Q[k];
+        fa += pf(pred(k)) / Sf * A;
+    }
+    const double FA = block_reduce(fa, wsum);
+    const double W = block_reduce(w, wsum);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double A = R[k] * R[k] - 2.0 * Q[k];
+        const double u = pred(k);
+        const double dp = pw ? 2.0 * u : exp((u - cmax) / sigma) / sigma;
+        res[k] = (float)(0.5 * (A - FA) / Sf * dp);
+    }
+    if (threadIdx.x == 0) a.trace_misfit[2 * tr + comp] = W;
+}
+
+size_t ot_smem_bytes(int nt) { return (size_t)4 * nt * sizeof(double); }
+
+cudaError_t launch_ot(const OtArgs &a, cudaStream_t st) {
+    const size_t sm = ot_smem_bytes(a.nt);
+    cudaError_t e = cudaFuncSetAttribute(k_ot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_ot<<<2 * a.ntr, OT_THREADS, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace sfwi

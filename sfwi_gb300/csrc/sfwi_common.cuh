@@ -16,13 +16,14 @@
 namespace sfwi {
 
 constexpr int NOP = 4;          // stencil half-width (8th order)
-constexpr int TX = 32;          // tile rows (x)
+constexpr int TX = 16;          // tile rows (x)
 constexpr int TZ = 32;          // tile columns (z)
 constexpr int HALO = 4;
 constexpr int BX = TX + 2 * HALO;  // staged box rows
 constexpr int BZ = TZ + 2 * HALO;  // staged box columns (multiple of 4)
 constexpr int BOX = BX * BZ;       // floats per staged box
-constexpr int NTHREADS = 256;      // 8 float4 columns x 32 rows
+constexpr int NTHREADS = TX * TZ / 4;  // compute threads of a tile: one float4 of cells each
+constexpr int CTAS_PER_SM = 2;         // persistent CTAs per SM (two independent tile pipelines)
 
 // Arrays of the packed batch grid, in allocation order: one [X][P] array each,
 // consecutive in one allocation (array k starts at k*X*P floats), so a single

@@ -83,6 +83,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// barrier 1 over the NTHREADS consumer threads (the producer warp is not in it)
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NTHREADS) : "memory"); }
+__device__ __forceinline__ bool consumer_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(NTHREADS)
+        : "memory");
+    return r != 0;
+}
 // bounded wait: false when the phase did not complete within WAIT_LIMIT tries
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     for (uint32_t i = 0; i < WAIT_LIMIT; i++)
@@ -106,11 +123,18 @@ struct V4 {
     float v[4];
 };
 
+// a += k*(p - m) on four cells as two packed FP32x2 pairs (cells 0-1, 2-3);
+// p - m is formed as fma(m, -1, p), which rounds exactly like a subtraction
 __device__ __forceinline__ void acc4(V4 &a, float k, float4 p, float4 m) {
-    a.v[0] += k * (p.x - m.x);
-    a.v[1] += k * (p.y - m.y);
-    a.v[2] += k * (p.z - m.z);
-    a.v[3] += k * (p.w - m.w);
+    const float2 kk = make_float2(k, k), neg = make_float2(-1.f, -1.f);
+    const float2 d0 = __ffma2_rn(make_float2(m.x, m.y), neg, make_float2(p.x, p.y));
+    const float2 d1 = __ffma2_rn(make_float2(m.z, m.w), neg, make_float2(p.z, p.w));
+    const float2 r0 = __ffma2_rn(kk, d0, make_float2(a.v[0], a.v[1]));
+    const float2 r1 = __ffma2_rn(kk, d1, make_float2(a.v[2], a.v[3]));
+    a.v[0] = r0.x;
+    a.v[1] = r0.y;
+    a.v[2] = r1.x;
+    a.v[3] = r1.y;
 }
 // D+x: sum_k K_k (f[r+k] - f[r-k+1])   (txx in update_vx, vz in txz update)
 __device__ __forceinline__ V4 dxp(const float *f, int r, int c) {
@@ -141,18 +165,25 @@ __device__ __forceinline__ W12 loadw(const float *f, int r, int c) {
     W12 o = {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z, d.w}};
     return o;
 }
-// D+z: sum_k K_k (f[c+k] - f[c-k+1])
+__device__ __forceinline__ float2 pr(const W12 &s, int i) { return make_float2(s.w[i], s.w[i + 1]); }
+// k*(p - q) + a on a pair
+__device__ __forceinline__ float2 kdiff2(float k, float2 p, float2 q, float2 a) {
+    const float2 d = __ffma2_rn(q, make_float2(-1.f, -1.f), p);
+    return __ffma2_rn(make_float2(k, k), d, a);
+}
+// D+z: sum_k K_k (f[c+k] - f[c-k+1]) on cells (0,1) and (2,3) as FP32x2 pairs
 __device__ __forceinline__ V4 dzp(const W12 &s) {
     V4 a;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int c = 4 + i;
-        float t = 0.f;
-        t += K1 * (s.w[c + 1] - s.w[c]);
-        t += K2 * (s.w[c + 2] - s.w[c - 1]);
-        t += K3 * (s.w[c + 3] - s.w[c - 2]);
-        t += K4 * (s.w[c + 4] - s.w[c - 3]);
-        a.v[i] = t;
+    for (int h = 0; h < 2; h++) {
+        const int c = 4 + 2 * h;  // first cell of the pair
+        float2 t = make_float2(0.f, 0.f);
+        t = kdiff2(K1, pr(s, c + 1), pr(s, c), t);
+        t = kdiff2(K2, pr(s, c + 2), pr(s, c - 1), t);
+        t = kdiff2(K3, pr(s, c + 3), pr(s, c - 2), t);
+        t = kdiff2(K4, pr(s, c + 4), pr(s, c - 3), t);
+        a.v[2 * h] = t.x;
+        a.v[2 * h + 1] = t.y;
     }
     return a;
 }
@@ -160,14 +191,15 @@ __device__ __forceinline__ V4 dzp(const W12 &s) {
 __device__ __forceinline__ V4 dzm(const W12 &s) {
     V4 a;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int c = 4 + i;
-        float t = 0.f;
-        t += K1 * (s.w[c] - s.w[c - 1]);
-        t += K2 * (s.w[c + 1] - s.w[c - 2]);
-        t += K3 * (s.w[c + 2] - s.w[c - 3]);
-        t += K4 * (s.w[c + 3] - s.w[c - 4]);
-        a.v[i] = t;
+    for (int h = 0; h < 2; h++) {
+        const int c = 4 + 2 * h;
+        float2 t = make_float2(0.f, 0.f);
+        t = kdiff2(K1, pr(s, c), pr(s, c - 1), t);
+        t = kdiff2(K2, pr(s, c + 1), pr(s, c - 2), t);
+        t = kdiff2(K3, pr(s, c + 2), pr(s, c - 3), t);
+        t = kdiff2(K4, pr(s, c + 3), pr(s, c - 4), t);
+        a.v[2 * h] = t.x;
+        a.v[2 * h + 1] = t.y;
     }
     return a;
 }
@@ -180,7 +212,7 @@ __device__ __forceinline__ void f4_to(const float4 &a, float o[4]) {
 }
 __device__ __forceinline__ float4 to_f4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
 
-// thread -> cells: 8 float4 columns x 32 rows per tile
+// thread -> cells: TZ/4 float4 columns x TX rows per tile
 struct CellMap {
     int r, c;     // box coordinates of the first of the four cells
     int ci;       // core-tile index of the first cell
@@ -220,17 +252,20 @@ __device__ __forceinline__ void core4(const float *core, int slot, int ci, float
     f4_to(ld4(core + slot * CORE + ci), o);
 }
 
+// PML factors of a frame cell: the split update (d1*m + c*D)/d2 is evaluated
+// as (d1*m + c*D) * (1/d2) with a correctly rounded reciprocal, one rounding
+// more than a division
 struct Damp {
-    float d1[4], d2[4], d3[4], d4[4];
+    float d1[4], r2[4], d3[4], r4[4];
 };
 __device__ __forceinline__ Damp make_damp(const Params &p, const float x[4], const float z[4]) {
     Damp d;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         d.d1[j] = 1.f - p.dt * x[j] / 2;
-        d.d2[j] = 1.f + p.dt * x[j] / 2;
+        d.r2[j] = __frcp_rn(1.f + p.dt * x[j] / 2);
         d.d3[j] = 1.f - p.dt * z[j] / 2;
-        d.d4[j] = 1.f + p.dt * z[j] / 2;
+        d.r4[j] = __frcp_rn(1.f + p.dt * z[j] / 2);
     }
     return d;
 }
@@ -242,6 +277,17 @@ struct SState {
     float xx[4], zz[4], xz[4], mxx[4], mzz[4], mxz[4];
 };
 
+// FP32x2 helpers on the cells (2h, 2h+1) of a four-cell group
+__device__ __forceinline__ float2 P2(const float v[4], int h) { return make_float2(v[2 * h], v[2 * h + 1]); }
+__device__ __forceinline__ void S2(float v[4], int h, float2 x) {
+    v[2 * h] = x.x;
+    v[2 * h + 1] = x.y;
+}
+__device__ __forceinline__ float2 B2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
 // velocity update of one field set on this thread's four cells:
 //   vx += dir*ib*(dtdx*ax + dtdz*bz),  vz += dir*ib*(dtdx*dx_ + dtdz*cz)
 // with the split form in frame cells; stores the new state.
@@ -249,15 +295,29 @@ template <bool FRAME>
 __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const FieldSet &f, VState &s,
                                         const float ib[4], const Damp &d, float dir, const V4 &ax, const V4 &bz,
                                         const V4 &dx_, const V4 &cz) {
+    if (!FRAME) {
+        // tile without PML cells: all four cells are updated (FP32x2)
+        const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 i2 = P2(ib, h);
+            const float2 cx = mul2(i2, tx), cz2 = mul2(i2, tz);
+            S2(s.vx, h, add2(P2(s.vx, h), fma2(cx, P2(ax.v, h), mul2(cz2, P2(bz.v, h)))));
+            S2(s.vz, h, add2(P2(s.vz, h), fma2(cx, P2(dx_.v, h), mul2(cz2, P2(cz.v, h)))));
+        }
+        st4(f.vx + m.gi, to_f4(s.vx));
+        st4(f.vz + m.gi, to_f4(s.vz));
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (!m.ok[j]) continue;
         const float cx = dir * ib[j] * p.dtdx, cz_ = dir * ib[j] * p.dtdz;
         if (FRAME && m.frame[j]) {
-            const float xx = (d.d1[j] * s.mx[j] + cx * ax.v[j]) / d.d2[j];
-            const float xz = (d.d3[j] * (s.vx[j] - s.mx[j]) + cz_ * bz.v[j]) / d.d4[j];
-            const float zx = (d.d1[j] * s.mz[j] + cx * dx_.v[j]) / d.d2[j];
-            const float zz = (d.d3[j] * (s.vz[j] - s.mz[j]) + cz_ * cz.v[j]) / d.d4[j];
+            const float xx = (d.d1[j] * s.mx[j] + cx * ax.v[j]) * d.r2[j];
+            const float xz = (d.d3[j] * (s.vx[j] - s.mx[j]) + cz_ * bz.v[j]) * d.r4[j];
+            const float zx = (d.d1[j] * s.mz[j] + cx * dx_.v[j]) * d.r2[j];
+            const float zz = (d.d3[j] * (s.vz[j] - s.mz[j]) + cz_ * cz.v[j]) * d.r4[j];
             s.mx[j] = xx;
             s.mz[j] = zx;
             s.vx[j] = xx + xz;
@@ -282,6 +342,30 @@ template <bool FRAME>
 __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const FieldSet &f, SState &s,
                                         const float lam[4], const float mu[4], const Damp &dm, float dir, const V4 &a,
                                         const V4 &b, const V4 &c, const V4 &d, const float (*born)[4]) {
+    if (!FRAME) {
+        // tile without PML cells: all four cells are updated (FP32x2)
+        const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 l = P2(lam, h), u = P2(mu, h);
+            const float2 l2m = fma2(u, B2(2.f), l);
+            const float2 ax = mul2(tx, P2(a.v, h)), bz = mul2(tz, P2(b.v, h));
+            const float2 cz = mul2(tz, P2(c.v, h)), dx_ = mul2(tx, P2(d.v, h));
+            float2 xx = P2(s.xx, h), zz = P2(s.zz, h), xz = P2(s.xz, h);
+            if (born) {
+                xx = add2(xx, add2(P2(born[0], h), P2(born[1], h)));
+                zz = add2(zz, add2(P2(born[2], h), P2(born[3], h)));
+                xz = add2(xz, add2(P2(born[4], h), P2(born[5], h)));
+            }
+            S2(s.xx, h, add2(xx, fma2(l2m, ax, mul2(l, bz))));
+            S2(s.zz, h, add2(zz, fma2(l, ax, mul2(l2m, bz))));
+            S2(s.xz, h, add2(xz, mul2(u, add2(dx_, cz))));
+        }
+        st4(f.txx + m.gi, to_f4(s.xx));
+        st4(f.tzz + m.gi, to_f4(s.zz));
+        st4(f.txz + m.gi, to_f4(s.xz));
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (!m.ok[j]) continue;
@@ -299,13 +383,13 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             bxz_z = born[5][j];
         }
         if (FRAME && m.frame[j]) {
-            const float d1 = dm.d1[j], d2 = dm.d2[j], d3 = dm.d3[j], d4 = dm.d4[j];
-            const float nxx_x = (d1 * (s.mxx[j] + bxx_x) + l2m * ax) / d2;
-            const float nxx_z = (d3 * ((s.xx[j] - s.mxx[j]) + bxx_z) + lam[j] * bz) / d4;
-            const float nzz_x = (d1 * (s.mzz[j] + bzz_x) + lam[j] * ax) / d2;
-            const float nzz_z = (d3 * ((s.zz[j] - s.mzz[j]) + bzz_z) + l2m * bz) / d4;
-            const float nxz_x = (d1 * (s.mxz[j] + bxz_x) + mu[j] * dx_) / d2;
-            const float nxz_z = (d3 * ((s.xz[j] - s.mxz[j]) + bxz_z) + mu[j] * cz) / d4;
+            const float d1 = dm.d1[j], r2 = dm.r2[j], d3 = dm.d3[j], r4 = dm.r4[j];
+            const float nxx_x = (d1 * (s.mxx[j] + bxx_x) + l2m * ax) * r2;
+            const float nxx_z = (d3 * ((s.xx[j] - s.mxx[j]) + bxx_z) + lam[j] * bz) * r4;
+            const float nzz_x = (d1 * (s.mzz[j] + bzz_x) + lam[j] * ax) * r2;
+            const float nzz_z = (d3 * ((s.zz[j] - s.mzz[j]) + bzz_z) + l2m * bz) * r4;
+            const float nxz_x = (d1 * (s.mxz[j] + bxz_x) + mu[j] * dx_) * r2;
+            const float nxz_z = (d3 * ((s.xz[j] - s.mxz[j]) + bxz_z) + mu[j] * cz) * r4;
             s.mxx[j] = nxx_x;
             s.mzz[j] = nzz_x;
             s.mxz[j] = nxz_x;
@@ -354,53 +438,69 @@ __device__ __forceinline__ TileCtx tile_ctx(const Params &p, int ti) {
     return c;
 }
 
-// Runs the pipeline over tiles handed out dynamically: thread 0 takes the
-// next tile index from this launch's counter (atomicAdd) when it starts that
-// tile's loads, and publishes it in s_tile[stage] for the other threads, so
-// SMs that drew cheap tiles simply take more of them.
-//   issue(ctx, stage_ptr, bar): thread 0 starts the loads of one tile (it arms
-//                               `bar` with expect_tx first);
-//   body(ctx, stage_ptr):       all threads, once the tile has landed.
+// Warp-specialised tile pipeline.  Warp NTHREADS/32 is the producer: its lane
+// 0 takes the next tile index from this launch's counter (atomicAdd; SMs that
+// drew cheap tiles take more of them), stores the tile's context in shared
+// memory, and starts the tile's TMA loads on full[stage] once the consumers
+// have released that stage (empty[stage]).  The NTHREADS consumer threads
+// wait on full[stage], run body(ctx, stage_ptr), and release the stage one
+// arrival per warp.  Every wait is bounded; a wait that gives up sets the
+// error flag and the CTA winds down without leaving a copy in flight.
+//   issue(ctx, stage_ptr, bar): producer lane 0, arms `bar` with expect_tx first
+//   body(ctx, stage_ptr):       consumers; may use consumer_sync()
+constexpr int PRODUCER_WARP = NTHREADS / 32;
+constexpr int BLOCK_THREADS = NTHREADS + 32;
+
 template <int STAGE_FLOATS, class Issue, class Body>
 __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body) {
-    __shared__ uint64_t bar[NSTAGE];
+    __shared__ uint64_t full[NSTAGE], empty[NSTAGE];
+    __shared__ TileCtx s_ctx[NSTAGE];
     __shared__ int s_tile[NSTAGE];
     float *sm = smem_base();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; s++) mbar_init(&bar[s], 1);
+        for (int s = 0; s < NSTAGE; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], NTHREADS / 32);
+        }
         fence_mbar_init();
-        const int t0 = atomicAdd(counter, 1);
-        s_tile[0] = t0;
-        if (t0 < p.ntiles) issue(tile_ctx(p, t0), sm, &bar[0]);
     }
     __syncthreads();
-    for (int k = 0;; k++) {
-        const int st = k % NSTAGE, nst = (k + 1) % NSTAGE;
-        const int ti = s_tile[st];
-        if (ti >= p.ntiles) break;
-        bool next = false;
-        if (threadIdx.x == 0) {
-            const int tn = atomicAdd(counter, 1);
-            s_tile[nst] = tn;
-            next = tn < p.ntiles;
-            if (next) issue(tile_ctx(p, tn), sm + nst * STAGE_FLOATS, &bar[nst]);
+    if (warp == PRODUCER_WARP) {
+        if (lane != 0) return;
+        for (int k = 0;; k++) {
+            const int s = k % NSTAGE;
+            if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1))) {
+                atomicExch(p.err, 2);
+                return;  // consumers give up on full[s] the same way
+            }
+            const int t = atomicAdd(counter, 1);
+            s_tile[s] = t;
+            if (t >= p.ntiles) {
+                mbar_arrive(&full[s]);  // no tile: complete the phase with no bytes
+                return;
+            }
+            s_ctx[s] = tile_ctx(p, t);
+            issue(s_ctx[s], sm + s * STAGE_FLOATS, &full[s]);
         }
-        const bool ok = mbar_wait(&bar[st], (uint32_t)((k / NSTAGE) & 1));
-        if (__syncthreads_or(!ok)) {
-            // a tile never landed: flag it, let the copy already issued for the
-            // next tile finish (bounded) so no copy targets freed shared
-            // memory, and leave together
+    }
+    for (int k = 0;; k++) {
+        const int s = k % NSTAGE;
+        const bool ok = mbar_wait(&full[s], (uint32_t)((k / NSTAGE) & 1));
+        if (consumer_any(!ok)) {
             if (threadIdx.x == 0) {
                 atomicExch(p.err, 1);
-                if (next) mbar_wait(&bar[nst], (uint32_t)(((k + 1) / NSTAGE) & 1));
+                // the other stage may still be loading: let it land (bounded)
+                mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1));
             }
-            __syncthreads();
             return;
         }
-        body(tile_ctx(p, ti), sm + st * STAGE_FLOATS);
-        // this stage is refilled by the asynchronous proxy two tiles later
+        if (s_tile[s] >= p.ntiles) return;
+        body(s_ctx[s], sm + s * STAGE_FLOATS);
+        // this stage is refilled by the asynchronous proxy after the release
         fence_proxy_async();
-        __syncthreads();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
     }
 }
 
@@ -416,7 +516,7 @@ struct FwdV {
 };
 
 template <bool BORN>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
             int it) {
     using S = FwdV<BORN>;
@@ -460,7 +560,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             s_xx[r * BZ + cc] += sv;
             s_zz[r * BZ + cc] += sv;
         }
-        __syncthreads();
+        consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
@@ -550,7 +650,7 @@ __device__ __forceinline__ int band_slot(int band, int lx, int lz, int pml, int 
 }
 
 template <bool BORN>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
             int it) {
     using S = FwdS<BORN>;
@@ -632,14 +732,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 core4(core, 10, m.ci, bp);
                 core4(core, 11, m.ci, bs);
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const float mix = bp[j] - 2 * bs[j];
-                    born[0][j] = p.dt * (bp[j] * a.v[j] * p.idx);
-                    born[1][j] = p.dt * (mix * b.v[j] * p.idz);
-                    born[2][j] = p.dt * (mix * a.v[j] * p.idx);
-                    born[3][j] = p.dt * (bp[j] * b.v[j] * p.idz);
-                    born[4][j] = p.dt * (bs[j] * d.v[j] * p.idx);
-                    born[5][j] = p.dt * (bs[j] * cc.v[j] * p.idz);
+                for (int h = 0; h < 2; h++) {
+                    const float2 bp2 = P2(bp, h), bs2 = P2(bs, h);
+                    const float2 mix = fma2(bs2, B2(-2.f), bp2);
+                    const float2 ax = mul2(P2(a.v, h), B2(p.idx)), bz = mul2(P2(b.v, h), B2(p.idz));
+                    const float2 dx_ = mul2(P2(d.v, h), B2(p.idx)), cz = mul2(P2(cc.v, h), B2(p.idz));
+                    const float2 dt2 = B2(p.dt);
+                    S2(born[0], h, mul2(dt2, mul2(bp2, ax)));
+                    S2(born[1], h, mul2(dt2, mul2(mix, bz)));
+                    S2(born[2], h, mul2(dt2, mul2(mix, ax)));
+                    S2(born[3], h, mul2(dt2, mul2(bp2, bz)));
+                    S2(born[4], h, mul2(dt2, mul2(bs2, dx_)));
+                    S2(born[5], h, mul2(dt2, mul2(bs2, cz)));
                 }
                 const V4 as = dxm(b_vx, m.r, m.c);
                 const V4 cs = dzp(loadw(b_vx, m.r, m.c));
@@ -717,7 +821,7 @@ struct BwdS {
     static constexpr int STAGE = NB * BOX + NC * CORE;
 };
 
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
             int it, float adj_dir) {
     using S = BwdS;
@@ -794,7 +898,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
             }
         }
-        __syncthreads();
+        consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
@@ -837,17 +941,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const V4 ca = dzp(loadw(a_vx, m.r, m.c));
         const V4 ba = dzm(loadw(a_vz, m.r, m.c));
         const V4 da = dxp(a_vz, m.r, m.c);
+        if (!frame) {
+            const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                S2(axx, h, fma2(tx, P2(aa.v, h), P2(axx, h)));
+                S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
+                S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
+            }
+        } else
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             if (!m.ok[j]) continue;
             const float ax = adj_dir * p.dtdx * aa.v[j], bz = adj_dir * p.dtdz * ba.v[j];
             const float cz = adj_dir * p.dtdz * ca.v[j], dx_ = adj_dir * p.dtdx * da.v[j];
-            if (frame && m.frame[j]) {
-                const float d1 = dm.d1[j], d2 = dm.d2[j], d3 = dm.d3[j], d4 = dm.d4[j];
-                axx[j] = (d1 * axx[j] + ax) / d2;
-                azz[j] = (d3 * azz[j] + bz) / d4;
-                const float nx_ = (d1 * amxz[j] + dx_) / d2;
-                const float nz_ = (d3 * (axz[j] - amxz[j]) + cz) / d4;
+            if (m.frame[j]) {
+                const float d1 = dm.d1[j], r2 = dm.r2[j], d3 = dm.d3[j], r4 = dm.r4[j];
+                axx[j] = (d1 * axx[j] + ax) * r2;
+                azz[j] = (d3 * azz[j] + bz) * r4;
+                const float nx_ = (d1 * amxz[j] + dx_) * r2;
+                const float nz_ = (d3 * (axz[j] - amxz[j]) + cz) * r4;
                 amxz[j] = nx_;
                 axz[j] = nx_ + nz_;
             } else {
@@ -866,14 +979,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             core4(core, 14, m.ci, gl);
             core4(core, 15, m.ci, gm);
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                if (!m.image[j]) continue;
-                const float gxx = a.v[j] * p.idx, gzz = b.v[j] * p.idz;
-                const float gxz = cc.v[j] * p.idz, gzx = d.v[j] * p.idx;
-                const float lg = -((gxx + gzz) * (axx[j] + azz[j]));
-                const float mg = -2 * (gxx * axx[j] + gzz * azz[j]) - (gxz + gzx) * axz[j];
-                gl[j] += lg;
-                gm[j] += mg;
+            for (int h = 0; h < 2; h++) {
+                const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
+                const float2 gxz = mul2(P2(cc.v, h), B2(p.idz)), gzx = mul2(P2(d.v, h), B2(p.idx));
+                const float2 x2 = P2(axx, h), z2 = P2(azz, h);
+                const float2 lg = mul2(B2(-1.f), mul2(add2(gxx, gzz), add2(x2, z2)));
+                const float2 mg = fma2(B2(-2.f), fma2(gxx, x2, mul2(gzz, z2)),
+                                       mul2(B2(-1.f), mul2(add2(gxz, gzx), P2(axz, h))));
+                const float2 ngl = add2(P2(gl, h), lg), ngm = add2(P2(gm, h), mg);
+                if (m.image[2 * h]) {
+                    gl[2 * h] = ngl.x;
+                    gm[2 * h] = ngm.x;
+                }
+                if (m.image[2 * h + 1]) {
+                    gl[2 * h + 1] = ngl.y;
+                    gm[2 * h + 1] = ngm.y;
+                }
             }
             st4(p.glam + m.gi, to_f4(gl));
             st4(p.gmu + m.gi, to_f4(gm));
@@ -892,7 +1013,7 @@ struct BwdV {
     static constexpr int STAGE = NB * BOX + NC * CORE;
 };
 
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
             int it, float adj_dir) {
     using S = BwdV;
@@ -949,7 +1070,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             st4(s_Q + 4 * i, to_f4(Q_));
             st4(s_R + 4 * i, to_f4(R_));
         }
-        __syncthreads();
+        consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
@@ -1034,7 +1155,7 @@ cudaError_t configure_step_kernels() {
     return cudaSuccess;
 }
 
-static int persistent_grid(int ntiles) { return ntiles < g_nsm ? ntiles : g_nsm; }
+static int persistent_grid(int ntiles) { return ntiles < CTAS_PER_SM * g_nsm ? ntiles : CTAS_PER_SM * g_nsm; }
 
 void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
                         cudaStream_t st) {
@@ -1042,21 +1163,21 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
     switch (which) {
         case 0:
             if (born)
-                k_fwd_v<true><<<grid, NTHREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_v<true><<<grid, BLOCK_THREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
             else
-                k_fwd_v<false><<<grid, NTHREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_v<false><<<grid, BLOCK_THREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
             break;
         case 1:
             if (born)
-                k_fwd_s<true><<<grid, NTHREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_s<true><<<grid, BLOCK_THREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
             else
-                k_fwd_s<false><<<grid, NTHREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_s<false><<<grid, BLOCK_THREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
             break;
         case 2:
-            k_bwd_s<<<grid, NTHREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
             break;
         default:
-            k_bwd_v<<<grid, NTHREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
             break;
     }
 }

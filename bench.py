@@ -41,14 +41,16 @@ METRIC = "shot-gradients/s"
 
 # algorithmic bytes per padded cell per time step of each kernel (FP32; each
 # array read once and written once per sweep, stencil neighbours reused on
-# chip)
+# chip, PML memory variables not counted)
 KERNEL_BYTES = {
     "k_fwd_v<born>": 60,   # read sigma(3) + sigma_s(3) + 1/rho; RMW v(2) + v_s(2)
     "k_fwd_s<born>": 80,   # read v(2) + v_s(2) + lam, mu, bp, bs; RMW sigma(3) + sigma_s(3)
     "k_bwd_s": 88,         # read v(2) + v_adj(2) + lam, mu; RMW sigma(3) + sigma_adj(3) + G_lam, G_mu
     "k_bwd_v": 76,         # read sigma(3) + sigma_adj(3) + lam, mu, 1/rho; RMW v(2) + v_adj(2) + illum
 }
-SURVEY_BYTES_PER_CELL_STEP = 328  # forward 72 + reconstruction 72 + adjoint 72 + imaging 32 + Born 80
+# algorithmic bytes per padded cell per time step of a Born shot-gradient:
+# forward 72 + reconstruction 72 + adjoint 72 + imaging 32 + Born add-on 80
+PASS_BYTES_PER_CELL_STEP = 328
 
 
 def log(*a):
@@ -63,7 +65,6 @@ def dist_info():
 
 def build_workload(w):
     from sfwi_gb300 import synth
-    from oracle import pyoracle  # noqa: F401  (wavelet only through the package below)
     vp, vs, rho = synth.layered_model(w["allnx"], w["allnz"], w["dx"])
     vp0 = synth.smooth_z(vp, 10)
     vs0 = (vp0 / 1.73).astype(np.float32)
@@ -126,6 +127,17 @@ class Clocks:
                 pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_per_cell(kernel):
+    """DRAM bytes per padded cell per launch of `kernel` from the committed
+    ncu capture summary (profiles/traffic_per_cell.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_per_cell.json")) as f:
+            v = json.load(f).get(kernel)
+        return float(v) if v is not None else None
+    except (OSError, ValueError):
+        return None
 
 
 def measured_peak_hbm():
@@ -305,10 +317,13 @@ def main():
         shares = {k: v for k, v in kt.items()}
         dom = max(shares, key=shares.get)
         achieved = KERNEL_BYTES[dom] * cells / (kt[dom] / 1000.0) / 1e9
+        tpc = traffic_per_cell(dom)
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "frac": round(achieved / peak, 4), "traffic": round(tpc * cells) if tpc else None,
+                "traffic_note": "DRAM bytes per launch: ncu capture of a 16-shot launch scaled by cells",
+                "alg_bytes_per_launch": KERNEL_BYTES[dom] * cells, "peak_source": peak_kind,
                 "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()}}
-    alg_bytes_step = SURVEY_BYTES_PER_CELL_STEP * cells * nt
+    alg_bytes_step = PASS_BYTES_PER_CELL_STEP * cells * nt
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, el = cpu_baseline_sample(w, data, 1, 150, "port")

@@ -114,9 +114,16 @@ def build_stage(src_root, stage, cxx="g++"):
     return lib
 
 
+DEFAULT_SRC = "/root/reference"
+
+
+def sources_present(src=DEFAULT_SRC):
+    return os.path.isdir(os.path.join(src, "sfwi-stage1"))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=DEFAULT_SRC)
     a = ap.parse_args(argv)
     if not os.path.isdir(os.path.join(a.src, "sfwi-stage1")):
         print("reference sources not found at %s; oracle/_ref not built" % a.src)

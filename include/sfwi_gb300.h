@@ -127,6 +127,23 @@ int sfwi_ot_power(const float *obs_x, const float *obs_z, const float *cal_x, co
                   float *res_z, int length, int tracenum, float dt, double *misfit);
 int sfwi_ot_alltrace(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
                      float *res_z, int length, int tracenum, float dt, double *misfit);
+/* Allocation-free OT on device buffers.  No counterpart in the reference.
+ * For callers that must not allocate device memory: code recording a CUDA
+ * graph (cudaMalloc is not allowed while a stream is captured), programs
+ * whose allocator owns all device memory, and latency-bound loops where an
+ * allocation may stall the GPU.  obs/cal/res are DEVICE pointers
+ * [tracenum][length] on the current device; kind is SFWI_MISFIT_OT,
+ * SFWI_MISFIT_OT_POWER or SFWI_MISFIT_OT_ALLTRACE; misfit (host) += W2;
+ * stream may be NULL (default stream).  The call waits for its stream.
+ * Working memory is a fixed 256 KB array that every device loading the
+ * library keeps until the process exits: at most 8192 traces per call (larger
+ * calls fail with SFWI_E_ARG) and length <= 7264.  The first call on a device
+ * looks up that array's device address, so make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap on the
+ * GPU (other streams or threads at the same time) race and must be serialised
+ * by the caller. */
+int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z,
+                    float *res_x, float *res_z, int length, int tracenum, float dt, double *misfit, void *stream);
 /* normalize(matrix, length, tracenum), sfwi-stage1/main.cpp:24-32: divide by
  * the gather's largest absolute value (host code, as in the reference). */
 int sfwi_normalize(float *matrix, int length, int tracenum);

@@ -41,6 +41,8 @@ SIGNATURES = {
     "sfwi_ot": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),
     "sfwi_ot_power": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),
     "sfwi_ot_alltrace": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),
+    "sfwi_ot_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_int, C.c_int, C.c_float, _dp, C.c_void_p]),
     "sfwi_normalize": (C.c_int, [_fp, C.c_int, C.c_int]),
     "sfwi_last_error": (C.c_char_p, []),
     "sfwi_kernel_launches": (C.c_longlong, [_h]),

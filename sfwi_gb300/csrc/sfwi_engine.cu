@@ -693,6 +693,18 @@ int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x
 
 }  // namespace
 
+namespace sfwi {
+int record_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+}  // namespace sfwi
+
 extern "C" {
 
 const char *sfwi_last_error(void) { return g_err.c_str(); }

@@ -55,4 +55,7 @@ struct OtArgs {
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st);
 size_t ot_smem_bytes(int nt);
 
+// sfwi_engine.cu: set the calling thread's sfwi_last_error() message; returns code
+int record_error(int code, const char *fmt, ...);
+
 }  // namespace sfwi

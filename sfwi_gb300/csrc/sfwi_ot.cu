@@ -18,6 +18,7 @@
 // One CTA handles one (trace, component); prefix and suffix sums are block
 // scans built on warp shuffles.
 #include <cfloat>
+#include <mutex>
 
 #include "sfwi_launch.h"
 
@@ -183,4 +184,115 @@ cudaError_t launch_ot(const OtArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free OT entry point (sfwi_ot_noalloc in include/sfwi_gb300.h).
+//
+// Its working memory -- the per-trace scale of the positivity transform, the
+// per-trace misfits and their sum -- lives in the fixed array below instead
+// of buffers from cudaMalloc, for callers that may not allocate: code that
+// runs while a stream is being captured into a CUDA graph (cudaMalloc is not
+// allowed there), allocators that own every device byte of a process, and
+// latency-bound loops where an allocation may synchronise the device.
+// Every device that loads this library holds the array (256 KB) until the
+// process exits.  All calls on a device share it, so calls that overlap on the
+// GPU (different streams or threads at the same time) race on it.
+// ---------------------------------------------------------------------------
+constexpr int OT_NOALLOC_MAX_TRACES = 8192;
+// [0, 2*max): scale per (trace, component); [2*max, 4*max): misfit per
+// (trace, component); [4*max]: the summed misfit
+static __device__ __align__(256) double g_ot_noalloc_scratch[4 * OT_NOALLOC_MAX_TRACES + 32];
+
+// scale of trace `blockIdx.x>>1`, component `blockIdx.x&1`: max |obs|
+__global__ void k_ot_trace_scale(const float *obs_z, const float *obs_x, int nt, double *sigma) {
+    __shared__ double wsum[32];
+    const int tr = blockIdx.x >> 1, comp = blockIdx.x & 1;
+    const float *o = (comp ? obs_x : obs_z) + (size_t)tr * nt;
+    double m = 0.0;
+    for (int k = threadIdx.x; k < nt; k += blockDim.x) m = fmax(m, fabs((double)o[k]));
+    const double t = block_max(m, wsum);
+    if (threadIdx.x == 0) sigma[blockIdx.x] = t;
+}
+
+// gather-wide scale (kind 3): every trace of a component takes the largest
+__global__ void k_ot_gather_scale(double *sigma, int ntr) {
+    __shared__ double wsum[32];
+    const int comp = blockIdx.x;
+    double m = 0.0;
+    for (int t = threadIdx.x; t < ntr; t += blockDim.x) m = fmax(m, sigma[2 * t + comp]);
+    const double g = block_max(m, wsum);
+    __syncthreads();
+    for (int t = threadIdx.x; t < ntr; t += blockDim.x) sigma[2 * t + comp] = g;
+}
+
+// misfit = sum over traces of the two components, in trace order
+__global__ void k_ot_sum(const double *trace_misfit, int ntr, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double w = 0.0;
+        for (int i = 0; i < 2 * ntr; i++) w += trace_misfit[i];
+        *out = w;
+    }
+}
+
 }  // namespace sfwi
+
+namespace {
+// device address of g_ot_noalloc_scratch per device, looked up on the first
+// call on that device with the device current
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[128] = {};
+}  // namespace
+
+extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z, const float *cal_x,
+                               const float *cal_z, float *res_x, float *res_z, int length, int tracenum, float dt,
+                               double *misfit, void *stream) {
+    using namespace sfwi;
+    if (kind < 1 || kind > 3) return record_error(-1, "sfwi_ot_noalloc: kind must be 1, 2 or 3");
+    if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z || !misfit || length < 1 || tracenum < 1)
+        return record_error(-1, "sfwi_ot_noalloc: bad argument");
+    if (tracenum > OT_NOALLOC_MAX_TRACES)
+        return record_error(-1, "sfwi_ot_noalloc: %d traces exceed the fixed scratch of %d traces", tracenum,
+                            OT_NOALLOC_MAX_TRACES);
+    if (ot_smem_bytes(length) > 227 * 1024)
+        return record_error(-1, "sfwi_ot_noalloc: length %d exceeds %d samples", length, (int)(227 * 1024 / 32));
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return record_error(-2, "sfwi_ot_noalloc: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= 128) return record_error(-1, "sfwi_ot_noalloc: device %d out of range", dev);
+    double *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_ot_noalloc_scratch);
+            if (e != cudaSuccess) return record_error(-2, "sfwi_ot_noalloc: scratch address: %s", cudaGetErrorString(e));
+            g_noalloc_addr[dev] = static_cast<double *>(p);
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double *sigma = scratch, *tmis = scratch + 2 * OT_NOALLOC_MAX_TRACES, *sum = scratch + 4 * OT_NOALLOC_MAX_TRACES;
+    k_ot_trace_scale<<<2 * tracenum, 256, 0, st>>>(obs_z, obs_x, length, sigma);
+    if (kind == 3) k_ot_gather_scale<<<2, 256, 0, st>>>(sigma, tracenum);
+    OtArgs o{};
+    o.kind = kind;
+    o.nt = length;
+    o.ntr = tracenum;
+    o.stage = 1;
+    o.dt = dt;
+    o.obs_z = obs_z;
+    o.obs_x = obs_x;
+    o.cal_z = cal_z;
+    o.cal_x = cal_x;
+    o.res_z = res_z;
+    o.res_x = res_x;
+    o.sigma = sigma;
+    o.trace_misfit = tmis;
+    if ((e = launch_ot(o, st)) != cudaSuccess) return record_error(-2, "sfwi_ot_noalloc: %s", cudaGetErrorString(e));
+    k_ot_sum<<<1, 32, 0, st>>>(tmis, tracenum, sum);
+    double w = 0.0;
+    if ((e = cudaMemcpyAsync(&w, sum, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return record_error(-2, "sfwi_ot_noalloc: %s", cudaGetErrorString(e));
+    *misfit += w;
+    return 0;
+}

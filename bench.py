@@ -217,6 +217,7 @@ def main():
     ap.add_argument("--nt", type=int, default=None, help="override the number of time steps (testing)")
     ap.add_argument("--shots", type=int, default=None, help="override the number of shots (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-shots", type=int, default=4, help="shots timed one at a time for the plain form")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     args = ap.parse_args()
     w = dict(WORKLOAD)
@@ -324,6 +325,24 @@ def main():
                 "alg_bytes_per_launch": KERNEL_BYTES[dom] * cells, "peak_source": peak_kind,
                 "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()}}
     alg_bytes_step = PASS_BYTES_PER_CELL_STEP * cells * nt
+
+    # plain form: the same engine, one shot per run (the reference's per-shot
+    # call pattern), device-timed on an evenly spread sample of the shots
+    plain = None
+    if args.plain_shots > 0:
+        pick = shots[:: max(1, len(shots) // args.plain_shots)][: args.plain_shots]
+        plain_ms = []
+        for j, d in enumerate(pick[:1] + pick):  # the first run warms the one-shot graph shape
+            i = shots.index(d)
+            fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[i][0].array,
+                            obs[i][1].array)
+            fd.run()
+            if j > 0:
+                plain_ms.append(fd.last_timing()["total_ms"])
+        fd.imagebuffer_resettozero()
+        pv = len(pick) / (sum(plain_ms) / 1000.0)
+        plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick),
+                 "ms_per_shot": round(float(np.mean(plain_ms)), 2), "batched_over_plain": round(value / pv, 2)}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, el = cpu_baseline_sample(w, data, 1, 150, "port")
@@ -346,7 +365,7 @@ def main():
                        "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain,
             "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2)}}
     print(json.dumps(line), flush=True)
     return 0

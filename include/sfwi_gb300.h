@@ -89,6 +89,17 @@ int sfwi_imagebuffer_resettozero(sfwi_handle *h, float *grad_pp, float *grad_ps,
 /* FP64 copy of the accumulated gradients (no reset) */
 int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, double *illum);
 
+/* Density gradient.  No reference counterpart: the reference images Vp and Vs
+ * only (doimage_gradient, FD2DGPU.cu:3350-3382).  When switched on, every
+ * later gradient run also accumulates the density kernel
+ *     G_rho += -sum_t v_adj(t) . (v(t) - v(t-1)) / dt
+ * over the interior cells, with v(t) - v(t-1) the velocity step of the
+ * background reconstruction and v_adj the adjoint velocity, into an FP64
+ * [allnx][allnz] buffer.  sfwi_read_density_gradient_f64 copies it out (no
+ * reset); sfwi_imagebuffer_resettozero zeroes it with the others. */
+int sfwi_set_density_gradient(sfwi_handle *h, int on);
+int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho);
+
 /* Records of the last shot-gradient call(s): forward records (stage 1:
  * background; stage 2: scattered), stage-2 background records and the adjoint
  * source, each [ntr][nt] of shot `i` of the last run (0 for the one-shot call).

@@ -20,8 +20,9 @@
  * Additions with no reference counterpart (parity unpinned):
  *   - misfit_kind 1..3: per-trace 1D quadratic-Wasserstein misfit and its
  *     adjoint source (orc*_ot_trace below);
- *   - grad_rho: a density kernel -sum_t v_adj . dv/dt (the reference computes
- *     no density gradient).
+ *   - grad_rho: a density kernel -sum_t v_adj . dv/dt, with dv the velocity
+ *     step of the reconstruction (the reference computes no density
+ *     gradient).
  */
 #include <math.h>
 #include <stdlib.h>
@@ -603,14 +604,18 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
          *grh = gil + (size_t)s.allnx * s.allnz;
     const int off = s.delta_left + s.record_left_in_v;
     for (int it = nt - 1; it >= 0; it--) {
-        edge_strips(g, F_(VX), F_(VZ), up_x, up_z, dn_x, dn_z, lf_x, lf_z, rt_x, rt_z, it, 0);
-        /* born_modeling(-1, 6): reconstruct sigma (with strains) then v */
-        update_s(g, F_(TXX), F_(TZZ), F_(TXXX), F_(TXXZ), F_(TZZX), F_(TZZZ), F_(TXZ), F_(TXZX), F_(TXZZ), F_(VX),
-                 F_(VZ), F_(LAM), F_(MU), F_(DX_), F_(DZ_), -1, F_(GXX), F_(GZZ), F_(GXZ), F_(GZX));
+        /* density kernel: the velocity step of the reconstruction itself,
+         * taken before the edge strips are restored into the totals (the
+         * restore is not part of the step: update_v rebuilds the totals from
+         * the split parts) */
         if (io->grad_rho) {
             memcpy(F_(VPREV_X), F_(VX), nD * sizeof(real));
             memcpy(F_(VPREV_Z), F_(VZ), nD * sizeof(real));
         }
+        edge_strips(g, F_(VX), F_(VZ), up_x, up_z, dn_x, dn_z, lf_x, lf_z, rt_x, rt_z, it, 0);
+        /* born_modeling(-1, 6): reconstruct sigma (with strains) then v */
+        update_s(g, F_(TXX), F_(TZZ), F_(TXXX), F_(TXXZ), F_(TZZX), F_(TZZZ), F_(TXZ), F_(TXZX), F_(TXZZ), F_(VX),
+                 F_(VZ), F_(LAM), F_(MU), F_(DX_), F_(DZ_), -1, F_(GXX), F_(GZZ), F_(GXZ), F_(GZX));
         update_v(g, F_(TXX), F_(TZZ), F_(TXZ), F_(VX), F_(VXX), F_(VXZ), F_(VZ), F_(VZX), F_(VZZ), F_(RHO), F_(DX_),
                  F_(DZ_), -1);
         /* elastic_rotation_addS_bac: assign (stack=false), FD2DGPU.cu:3425-3441 */

@@ -140,6 +140,16 @@ class FD2DGPU_ELASTIC:
         _lib.check(_lib.load().sfwi_read_gradients_f64(self._h, *[o.ctypes.data_as(dp) for o in out]))
         return tuple(out)
 
+    def set_density_gradient(self, on=True):
+        """Also accumulate the density kernel -sum_t v_adj . dv/dt (no
+        reference counterpart) in later gradient runs."""
+        _lib.check(_lib.load().sfwi_set_density_gradient(self._h, 1 if on else 0))
+
+    def read_density_gradient_f64(self):
+        out = np.zeros((self.allnx, self.allnz), np.float64)
+        _lib.check(_lib.load().sfwi_read_density_gradient_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def read_records(self, i=0, ntr=None):
         """dict of syn_z, syn_x, syn2_z, syn2_x, res_z, res_x ([ntr, nt]) of
         shot i of the last run."""

@@ -60,24 +60,52 @@ void launch_setup(const SetupArgs &a, int nshots, int max_nxpml, cudaStream_t st
     k_setup<<<dim3(bx, nshots), 256, 0, st>>>(a);
 }
 
-// time-major [nt][ntr] -> trace-major [ntr][nt]
-__global__ void k_transpose(const float *__restrict__ in, float *__restrict__ out, int nt, int ntr) {
+// Receiver-row records [nt][nrc][X] -> trace-major records [nrc][ntr][nt]:
+// trace tr reads packed row trow[tr] (-1: a cell outside the update region,
+// which the reference records as zero).  32 traces x 32 steps per block,
+// transposed through shared memory so both sides are coalesced.
+__global__ void k_record_gather(const float *__restrict__ rrow, const int *__restrict__ trow, int nt, int nrc, int X,
+                                int ntr, float *__restrict__ out, size_t cstride) {
     __shared__ float tile[32][33];
-    const int t0 = blockIdx.y * 32, r0 = blockIdx.x * 32;
+    const int c = blockIdx.z, r0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+    const int tr = r0 + threadIdx.x;
+    const int row = tr < ntr ? trow[tr] : -1;
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        const int t = t0 + k, r = r0 + threadIdx.x;
-        tile[k][threadIdx.x] = (t < nt && r < ntr) ? in[(size_t)t * ntr + r] : 0.f;
+        const int t = t0 + k;
+        tile[k][threadIdx.x] = (row >= 0 && t < nt) ? rrow[((size_t)t * nrc + c) * X + row] : 0.f;
     }
     __syncthreads();
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
         const int r = r0 + k, t = t0 + threadIdx.x;
-        if (r < ntr && t < nt) out[(size_t)r * nt + t] = tile[threadIdx.x][k];
+        if (r < ntr && t < nt) out[c * cstride + (size_t)r * nt + t] = tile[threadIdx.x][k];
     }
 }
 
-void launch_transpose(const float *in, float *out, int nt, int ntr, cudaStream_t st) {
-    dim3 grid((ntr + 31) / 32, (nt + 31) / 32), block(32, 8);
-    k_transpose<<<grid, block, 0, st>>>(in, out, nt, ntr);
+void launch_record_gather(const float *rrow, const int *trow, int nt, int nrc, int X, int ntr, float *out,
+                          size_t cstride, cudaStream_t st) {
+    dim3 grid((ntr + 31) / 32, (nt + 31) / 32, nrc), block(32, 8);
+    k_record_gather<<<grid, block, 0, st>>>(rrow, trow, nt, nrc, X, ntr, out, cstride);
+}
+
+// Residual source per packed row: rs[row][2 it + 0|1] = res_z|res_x of the
+// trace rtr[row] at step it, or the all-ones pattern where no trace injects
+// (and in the padding past 2 nt).  One block per row.
+__global__ void k_recv_source(const float *__restrict__ res_z, const float *__restrict__ res_x,
+                              const int *__restrict__ rtr, int nt, int rsp, float *__restrict__ rs) {
+    const int row = blockIdx.x;
+    const int tr = rtr[row];
+    float *o = rs + (size_t)row * rsp;
+    for (int i = threadIdx.x; i < rsp; i += blockDim.x) {
+        const int t = i >> 1;
+        float v = __uint_as_float(0xFFFFFFFFu);
+        if (tr >= 0 && t < nt) v = (i & 1) ? res_x[(size_t)tr * nt + t] : res_z[(size_t)tr * nt + t];
+        o[i] = v;
+    }
+}
+
+void launch_recv_source(const float *res_z, const float *res_x, const int *rtr, int nt, int X, int rsp, float *rs,
+                        cudaStream_t st) {
+    if (X > 0) k_recv_source<<<X, 256, 0, st>>>(res_z, res_x, rtr, nt, rsp, rs);
 }
 
 __device__ __forceinline__ double block_sum(double v, double *red) {
@@ -134,7 +162,9 @@ void launch_residual_l2(int stage, int nt, int ntr_tot, const float *syn_z, cons
 // gradients, in FP64 and in shot order (deterministic).  The chain rule of
 // doimage_gradient (FD2DGPU.cu:3372-3373) is applied here once:
 //   g_vp += 2 vp rho G_lambda,  g_vs += -4 vs rho G_lambda + 2 vs rho G_mu
-// with G_* the time sums of the lambda and mu kernels.
+// with G_* the time sums of the lambda and mu kernels.  When requested the
+// density kernel G_rho = -sum_t v_adj . dv/dt is reduced the same way, as is.
+
 __global__ void k_finalize(FinalArgs a) {
     const long long n = (long long)a.allnx * a.allnz;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -142,7 +172,7 @@ __global__ void k_finalize(FinalArgs a) {
         // running sums start from the accumulated totals and add one rounded
         // term per shot (no fused multiply-add into the sum), so a batch of
         // shots gives bit-for-bit the totals of the same shots run one by one
-        double pp = a.gpp[i], ps = a.gps[i], il = a.gil[i];
+        double pp = a.gpp[i], ps = a.gps[i], il = a.gil[i], rh = a.grho ? a.grh[i] : 0.0;
         bool any = false;
         for (int s = 0; s < a.nshots; s++) {
             const ShotGeo g = a.geo[s];
@@ -156,12 +186,14 @@ __global__ void k_finalize(FinalArgs a) {
             pp = __dadd_rn(pp, tpp);
             ps = __dadd_rn(ps, tps);
             il = __dadd_rn(il, (double)a.illum[o]);
+            if (a.grho) rh = __dadd_rn(rh, (double)a.grho[o]);
             any = true;
         }
         if (any) {
             a.gpp[i] = pp;
             a.gps[i] = ps;
             a.gil[i] = il;
+            if (a.grho) a.grh[i] = rh;
         }
     }
 }

@@ -32,7 +32,7 @@ enum GridArr {
     BG_VX, BG_VZ, BG_TXX, BG_TZZ, BG_TXZ, BG_MVX, BG_MVZ, BG_MTXX, BG_MTZZ, BG_MTXZ,
     SC_VX, SC_VZ, SC_TXX, SC_TZZ, SC_TXZ, SC_MVX, SC_MVZ, SC_MTXX, SC_MTZZ, SC_MTXZ,
     AD_VX, AD_VZ, AD_TXX, AD_TZZ, AD_TXZ, AD_MVX, AD_MVZ, AD_MTXZ,
-    G_LAM, G_MU, G_ILL,
+    G_LAM, G_MU, G_ILL, G_RHO,
     NSTATE,  // arrays above are zeroed per run
     C_IB = NSTATE, C_LAM, C_MU, C_DX, C_DZ, C_BP, C_BS, C_VP, C_VS, C_RHO,
     NGRID
@@ -49,10 +49,6 @@ struct ShotGeo {
     int tr0;       // first trace in the packed trace arrays
     int win0;      // global-model column of interior column 0 (delta_left + record_left_in_v)
     int pad_;
-    long long strip0;  // float offset of this shot's edge-strip area
-    long long rec0;    // float offset of this shot's records in the trace-major arrays ([ntr][nt])
-    int csr0;          // offset of this shot's receiver-column CSR (nxpml+1 entries)
-    int pad2_;
 };
 
 // tile table entry: shot, first local row, first column, flags
@@ -92,16 +88,14 @@ struct Params {
     FieldSet bg, sc, ad;
     Coef c;
     float *glam, *gmu, *illum;  // per-cell imaging accumulators
+    float *grho;                // density kernel accumulator, null unless requested
     const ShotGeo *geo;
     const Tile *tiles;
     const float *sou;           // [nt]
-    float *strips;              // edge strips: shot s, step it at geo[s].strip0 + it*strip_floats(nx_s, nz)
-    float *syn_z, *syn_x;       // time-major [nt][ntr_tot] forward records
-    float *syn2_z, *syn2_x;     // stage 2 background records
-    const float *res_z, *res_x; // trace-major [ntr][nt] adjoint sources
-    const int *csr_start;       // receiver columns: per shot nxpml+1 offsets
-    const int *csr_trace;       // trace index (global) sorted by column then trace
-    int ntr_tot;
+    float *tb, *lr;             // edge strips (layout below); null in modelling-only runs
+    float *rrow;                // receiver-row records [nt][nrc][X]
+    int nrc;                    // record components: vz, vx (+ background vz, vx in stage 2)
+    int nshots;
     int ntiles;
     int *err;                   // set to a nonzero code when a bounded device wait gives up
     int *counters;              // tile counters, one per (time step, kernel): counters[4*it + kernel]
@@ -109,41 +103,40 @@ struct Params {
 
 // Edge strips of vx and vz saved each forward step and restored in the
 // backward step (the reference's record_edge_wavefield/load_edge_wavefield,
-// sfwi-stage1/FD2DGPU.cu:3842-3899): 2*NOP-wide bands around the interior.
-// One step of one shot is [component vx|vz][top nx*8 | bottom nx*8 |
-// left 8*nz | right 8*nz].
-__host__ __device__ __forceinline__ long long strip_comp_floats(int nx, int nz) {
-    return 16LL * nx + 16LL * nz;
+// sfwi-stage1/FD2DGPU.cu:3842-3899): 2*NOP-wide bands around the interior,
+//   top/bottom (band 0/1): rows [pml, nxpml-pml), columns [z0, z0+8),
+//       z0 = pml-NOP or nzpml-pml-NOP;
+//   left/right (band 0/1): rows [x0, x0+8), x0 = pml-NOP or nxpml-pml-NOP,
+//       columns [pml, nzpml-pml).
+// They are stored batch-wide and time-major, shaped so that the part of a
+// band inside one tile's staged box is a single 2-D TMA box:
+//   TB[tb_row(it, comp, band, X, packed row)][column - z0]   (8 floats a row)
+//   LR[lr_row(it, comp, band, nshots, shot, row - x0)][column] (P floats a row)
+// with comp 0 = vx, 1 = vz.  A cell in two bands is stored in both.
+__host__ __device__ __forceinline__ long long tb_row(int it, int comp, int band, int X, int prow) {
+    return ((long long)(it * 2 + comp) * 2 + band) * X + prow;
 }
-__host__ __device__ __forceinline__ long long strip_floats(int nx, int nz) { return 2 * strip_comp_floats(nx, nz); }
-
-// index of cell (lx, lz) inside one component block, or -1; where the top or
-// bottom band overlaps the left or right band the top/bottom slot is returned
-// (both slots always hold the same value)
-__host__ __device__ __forceinline__ int strip_index(int lx, int lz, int nxpml, int nzpml, int pml) {
-    const int nx = nxpml - 2 * pml, nz = nzpml - 2 * pml;
-    if (lx >= pml && lx < nxpml - pml) {
-        if (lz >= pml - NOP && lz < pml + NOP) return (lx - pml) * 8 + (lz - (pml - NOP));
-        if (lz >= nzpml - pml - NOP && lz < nzpml - pml + NOP)
-            return 8 * nx + (lx - pml) * 8 + (lz - (nzpml - pml - NOP));
-    }
-    if (lz >= pml && lz < nzpml - pml) {
-        if (lx >= pml - NOP && lx < pml + NOP) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
-        if (lx >= nxpml - pml - NOP && lx < nxpml - pml + NOP)
-            return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
-    }
-    return -1;
+__host__ __device__ __forceinline__ long long lr_row(int it, int comp, int band, int nshots, int shot, int r) {
+    return (((long long)(it * 2 + comp) * 2 + band) * nshots + shot) * 8 + r;
 }
-// second slot of a cell that lies in both a top/bottom and a left/right band
-__host__ __device__ __forceinline__ int strip_index2(int lx, int lz, int nxpml, int nzpml, int pml) {
-    const int nx = nxpml - 2 * pml, nz = nzpml - 2 * pml;
-    const bool tb = lx >= pml && lx < nxpml - pml &&
-                    ((lz >= pml - NOP && lz < pml + NOP) || (lz >= nzpml - pml - NOP && lz < nzpml - pml + NOP));
-    if (!tb || lz < pml || lz >= nzpml - pml) return -1;
-    if (lx >= pml - NOP && lx < pml + NOP) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
-    if (lx >= nxpml - pml - NOP && lx < nxpml - pml + NOP)
-        return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
-    return -1;
+struct Band {
+    int x0, x1, z0, z1;  // cell rectangle [x0, x1) x [z0, z1)
+};
+// b = 0 top, 1 bottom, 2 left, 3 right
+__host__ __device__ __forceinline__ Band band_rect(int b, int pml, int nxpml, int nzpml) {
+    Band r;
+    if (b < 2) {
+        r.x0 = pml;
+        r.x1 = nxpml - pml;
+        r.z0 = b == 0 ? pml - NOP : nzpml - pml - NOP;
+        r.z1 = r.z0 + 2 * NOP;
+    } else {
+        r.z0 = pml;
+        r.z1 = nzpml - pml;
+        r.x0 = b == 2 ? pml - NOP : nxpml - pml - NOP;
+        r.x1 = r.x0 + 2 * NOP;
+    }
+    return r;
 }
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }

@@ -72,25 +72,29 @@ struct ShotIn {
     const float *obs_z = nullptr, *obs_x = nullptr;  // host [ntr][nt]
 };
 
-enum RecArr { R_SYNT_Z, R_SYNT_X, R_SYN2T_Z, R_SYN2T_X, R_SYN_Z, R_SYN_X, R_SYN2_Z, R_SYN2_X, R_OBS_Z, R_OBS_X,
-              R_RES_Z, R_RES_X, NREC };
+// trace-major [ntr_tot][nt] record arrays; the first four are in the
+// component order of the receiver-row records (Params::rrow)
+enum RecArr { R_SYN_Z, R_SYN_X, R_SYN2_Z, R_SYN2_X, R_OBS_Z, R_OBS_X, R_RES_Z, R_RES_X, NREC };
 
 struct Batch {
     int nshots = 0, ntiles = 0, X = 0, P = 0, ntr_tot = 0, max_nxpml = 0;
     std::vector<ShotGeo> geo;
     std::vector<Tile> tiles;
-    std::vector<int> csr_start, csr_trace;
+    std::vector<int> trow;      // packed receiver row of each trace, -1 outside the update region
+    std::vector<int> rtr;       // per packed row: the trace whose residual is injected there, or -1
     std::vector<double> sigma;  // OT scale per trace/component
-    long long strip_total = 0;
+    int rsp = 0;                // row length of the residual source (2 nt rounded up to 4)
     // device
     DevBuf<float> grid;      // NGRID * X * P
-    DevBuf<float> strips;
+    DevBuf<float> tb, lr;    // edge strips (sfwi_common.cuh layout)
+    DevBuf<float> rrow;      // receiver-row records [nt][nrc][X]
+    DevBuf<float> rsrc;      // residual source [X][rsp]
     DevBuf<float> recs;      // NREC * ntr_tot * nt
     DevBuf<double> tmis;     // 2 * ntr_tot
     DevBuf<double> dsigma;
     DevBuf<ShotGeo> dgeo;
     DevBuf<Tile> dtiles;
-    DevBuf<int> dcsr_start, dcsr_trace;
+    DevBuf<int> dtrow, drtr;
     size_t cells = 0;        // X * P
     DevBuf<int> derr;        // device-side error flag (bounded waits)
     DevBuf<int> dctr;        // dynamic tile counters of the step kernels (zeroed per run)
@@ -120,7 +124,8 @@ struct sfwi_handle {
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     DevBuf<float> sou, vp_all, vs_all, rho_all, dvp_all, dvs_all;
     bool have_model = false, have_rho = false, have_m = false;
-    DevBuf<double> gpp, gps, gil;
+    DevBuf<double> gpp, gps, gil, grh;
+    bool want_rho = false;       // accumulate the density kernel as well
     // one-shot state written by the reference-shaped calls
     int ngx_min = 0;
     std::vector<float> rec_z, rec_x;
@@ -163,18 +168,36 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // 3-D tiled map over the packed grid: dims (P, X, NGRID) floats, boxes of
-// bz x bx x 1; out-of-range elements of a box load arrive as zeros
-int encode_grid_map(CUtensorMap *m, float *base, int P, int X, int bz, int bx) {
+// bz x bx x depth (depth consecutive arrays); out-of-range elements of a box
+// load arrive as zeros
+int encode_grid_map(CUtensorMap *m, float *base, int P, int X, int bz, int bx, int depth) {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[3] = {(cuuint64_t)P, (cuuint64_t)X, (cuuint64_t)NGRID};
     const cuuint64_t strides[2] = {(cuuint64_t)P * 4, (cuuint64_t)P * X * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, (cuuint32_t)depth};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SFWI_OK;
+}
+
+// 2-D tiled map over a row-major float array of `outer` rows of `inner`
+// floats (row pitch a multiple of 16 bytes), boxes of box_inner x box_outer
+int encode_2d_map(CUtensorMap *m, float *base, unsigned long long inner, unsigned long long outer, int box_inner,
+                  int box_outer) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+    const cuuint64_t strides[1] = {(cuuint64_t)inner * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled (2-D) failed (%d)", (int)r);
     return SFWI_OK;
 }
 
@@ -185,11 +208,10 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     b.P = (nzpml + 3) & ~3;
     b.geo.assign(b.nshots, ShotGeo{});
     b.tiles.clear();
-    b.csr_start.clear();
-    b.csr_trace.clear();
+    b.trow.clear();
+    b.rtr.clear();
     b.sigma.clear();
     int row = 0, tr0 = 0;
-    long long strip0 = 0;
     b.max_nxpml = 0;
     for (int s = 0; s < b.nshots; s++) {
         const ShotIn &in = shots[s];
@@ -212,26 +234,21 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
         g.ntr = in.ntr;
         g.tr0 = tr0;
         g.win0 = in.win0;
-        g.strip0 = strip0;
-        g.rec0 = (long long)tr0 * nt;
-        g.csr0 = (int)b.csr_start.size();
-        // receiver columns, CSR sorted by column then trace
+        // receiver rows: the record of a trace is its cell (rix, igz), which
+        // stays zero outside the update region [NOP, n-NOP); the residual
+        // injected at a cell is the highest-index trace recorded there
         std::vector<int> rix(in.ntr);
-        std::vector<std::vector<int>> bycol(nxpml);
+        b.rtr.resize((size_t)row + nxpml, -1);
+        const bool igz_live = in.igz >= NOP && in.igz < nzpml - NOP;
         for (int t = 0; t < in.ntr; t++) {
             rix[t] = receiver_ix(h->stage, pml, in.gc[t], in.ngx_left, h->dx);
             if (rix[t] < 0 || rix[t] >= nxpml)
                 return fail(SFWI_E_ARG, "shot %d trace %d: receiver column %d outside the %d-wide grid", s, t, rix[t],
                             nxpml);
-            bycol[rix[t]].push_back(tr0 + t);
+            const bool live = igz_live && rix[t] >= NOP && rix[t] < nxpml - NOP;
+            b.trow.push_back(live ? row + rix[t] : -1);
+            b.rtr[(size_t)row + rix[t]] = std::max(b.rtr[(size_t)row + rix[t]], tr0 + t);
         }
-        int acc = (int)b.csr_trace.size();
-        for (int x = 0; x < nxpml; x++) {
-            b.csr_start.push_back(acc);
-            for (int t : bycol[x]) b.csr_trace.push_back(t);
-            acc += (int)bycol[x].size();
-        }
-        b.csr_start.push_back(acc);
         // tiles over the update region [NOP, n-NOP)
         for (int x0 = NOP; x0 < nxpml - NOP; x0 += TX)
             for (int z0 = NOP; z0 < nzpml - NOP; z0 += TZ) {
@@ -276,13 +293,12 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
         }
         row += nxpml;
         tr0 += in.ntr;
-        strip0 += strip_floats(in.nx, nz) * nt;
         b.max_nxpml = std::max(b.max_nxpml, nxpml);
     }
     b.X = row;
     b.ntr_tot = tr0;
     b.ntiles = (int)b.tiles.size();
-    b.strip_total = strip0;
+    b.rsp = (2 * nt + 3) & ~3;
     b.cells = (size_t)b.X * b.P;
     h->last_ntr.clear();
     h->last_tr0.clear();
@@ -317,20 +333,15 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     p.glam = b.g(G_LAM);
     p.gmu = b.g(G_MU);
     p.illum = b.g(G_ILL);
+    p.grho = h->want_rho && !forward_only ? b.g(G_RHO) : nullptr;
     p.geo = b.dgeo.p;
     p.tiles = b.dtiles.p;
     p.sou = h->sou.p;
-    p.strips = forward_only ? nullptr : b.strips.p;  // modelling only: no strips saved
-    const int nt = h->nt;
-    p.syn_z = b.r(R_SYNT_Z, nt);
-    p.syn_x = b.r(R_SYNT_X, nt);
-    p.syn2_z = b.r(R_SYN2T_Z, nt);
-    p.syn2_x = b.r(R_SYN2T_X, nt);
-    p.res_z = b.r(R_RES_Z, nt);
-    p.res_x = b.r(R_RES_X, nt);
-    p.csr_start = b.dcsr_start.p;
-    p.csr_trace = b.dcsr_trace.p;
-    p.ntr_tot = b.ntr_tot;
+    p.tb = forward_only ? nullptr : b.tb.p;  // modelling only: no strips saved
+    p.lr = forward_only ? nullptr : b.lr.p;
+    p.rrow = b.rrow.p;
+    p.nrc = h->stage == 2 ? 4 : 2;
+    p.nshots = b.nshots;
     p.ntiles = b.ntiles;
     p.err = b.derr.p;
     p.counters = b.dctr.p;
@@ -341,32 +352,47 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     Batch &b = h->b;
     const int nt = h->nt;
     const size_t recs = (size_t)NREC * std::max(b.ntr_tot, 1) * nt;
-    float *old_grid = b.grid.p, *old_strips = b.strips.p, *old_recs = b.recs.p;
+    const int nrc = h->stage == 2 ? 4 : 2;
+    // TMA row coordinates of the strip arrays are 32-bit
+    if (!forward_only && ((long long)nt * 4 * b.X >= (1LL << 31) || (long long)nt * 4 * b.nshots * 8 >= (1LL << 31)))
+        return fail(SFWI_E_ARG, "batch too large for one run (nt x packed rows = %lld); split the shots",
+                    (long long)nt * b.X);
     CK(b.grid.ensure((size_t)NGRID * b.cells));
-    CK(b.strips.ensure(forward_only ? 1 : (size_t)std::max<long long>(b.strip_total, 1)));
+    if (!forward_only) {
+        CK(b.tb.ensure((size_t)nt * 4 * b.X * 8));
+        CK(b.lr.ensure((size_t)nt * 4 * b.nshots * 8 * b.P));
+        CK(b.rsrc.ensure((size_t)b.X * b.rsp));
+    }
+    CK(b.rrow.ensure((size_t)nt * nrc * b.X));
     CK(b.recs.ensure(recs));
     CK(b.tmis.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
     CK(b.dsigma.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
     CK(b.dgeo.ensure(b.geo.size()));
     CK(b.dtiles.ensure(b.tiles.size()));
-    CK(b.dcsr_start.ensure(b.csr_start.size()));
-    CK(b.dcsr_trace.ensure(std::max<size_t>(b.csr_trace.size(), 1)));
+    CK(b.dtrow.ensure(std::max<size_t>(b.trow.size(), 1)));
+    CK(b.drtr.ensure(b.rtr.size()));
     CK(b.derr.ensure(1));
     CK(cudaMemsetAsync(b.derr.p, 0, sizeof(int), h->st));
     const size_t nctr = 4 * (size_t)std::max(h->nt, kTimeKernelsMaxReps + 1);
     CK(b.dctr.ensure(nctr));
     CK(cudaMemsetAsync(b.dctr.p, 0, nctr * sizeof(int), h->st));
-    if (int rc = encode_grid_map(&b.tm.box, b.grid.p, b.P, b.X, BZ, BX)) return rc;
-    if (int rc = encode_grid_map(&b.tm.core, b.grid.p, b.P, b.X, TZ, TX)) return rc;
-    if (old_grid != b.grid.p || old_strips != b.strips.p || old_recs != b.recs.p) b.drop_graphs();
+    for (int d = 0; d < 3; d++) {
+        if (int rc = encode_grid_map(&b.tm.box[d], b.grid.p, b.P, b.X, BZ, BX, d + 1)) return rc;
+        if (int rc = encode_grid_map(&b.tm.core[d], b.grid.p, b.P, b.X, TZ, TX, d + 1)) return rc;
+    }
+    if (!forward_only) {
+        // strips: boxes of (BX rows x 8) and (8 rows x BZ); residual source: BX rows x 4
+        if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, BX)) return rc;
+        if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, BZ, 8))
+            return rc;
+        if (int rc = encode_2d_map(&b.tm.rs, b.rsrc.p, b.rsp, b.X, 4, BX)) return rc;
+    }
     cudaStream_t st = h->st;
     CK(cudaMemcpyAsync(b.dgeo.p, b.geo.data(), b.geo.size() * sizeof(ShotGeo), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(b.dcsr_start.p, b.csr_start.data(), b.csr_start.size() * sizeof(int), cudaMemcpyHostToDevice,
-                       st));
-    if (!b.csr_trace.empty())
-        CK(cudaMemcpyAsync(b.dcsr_trace.p, b.csr_trace.data(), b.csr_trace.size() * sizeof(int),
-                           cudaMemcpyHostToDevice, st));
+    if (!b.trow.empty())
+        CK(cudaMemcpyAsync(b.dtrow.p, b.trow.data(), b.trow.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(b.drtr.p, b.rtr.data(), b.rtr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!b.sigma.empty())
         CK(cudaMemcpyAsync(b.dsigma.p, b.sigma.data(), b.sigma.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     // zero the state (fields, memory variables, accumulators) and the records
@@ -416,18 +442,17 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
-    std::vector<long long> s = {h->nt, h->stage, forward_only, b.ntiles, b.X, b.P, b.ntr_tot,
-                                (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.strips.p,
-                                (long long)(uintptr_t)b.recs.p, (long long)(uintptr_t)b.dtiles.p,
-                                (long long)(uintptr_t)b.dgeo.p, (long long)(uintptr_t)b.dcsr_start.p,
-                                (long long)(uintptr_t)b.dcsr_trace.p, (long long)(uintptr_t)h->sou.p};
+    std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, b.nshots, b.ntiles, b.X, b.P,
+                                b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
+                                (long long)(uintptr_t)b.lr.p, (long long)(uintptr_t)b.rrow.p,
+                                (long long)(uintptr_t)b.rsrc.p, (long long)(uintptr_t)b.dtiles.p,
+                                (long long)(uintptr_t)b.dgeo.p, (long long)(uintptr_t)h->sou.p};
     for (auto &t : b.tiles) s.push_back(((long long)t.shot << 40) ^ ((long long)t.x0 << 24) ^ (t.z0 << 8) ^ t.flags);
     for (auto &g : b.geo) {
         s.push_back(g.isx * 100003LL + g.isz);
         s.push_back(g.igz * 1000003LL + g.nx);
-        s.push_back(g.strip0);
+        s.push_back(g.row0);
     }
-    for (int v : b.csr_trace) s.push_back(v);
     return s;
 }
 
@@ -495,14 +520,11 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
     h->launches += 2LL * nt;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[1], st));
-    // records to trace-major
-    launch_transpose(b.r(R_SYNT_Z, nt), b.r(R_SYN_Z, nt), nt, b.ntr_tot, st);
-    launch_transpose(b.r(R_SYNT_X, nt), b.r(R_SYN_X, nt), nt, b.ntr_tot, st);
-    h->launches += 2;
-    if (h->stage == 2) {
-        launch_transpose(b.r(R_SYN2T_Z, nt), b.r(R_SYN2_Z, nt), nt, b.ntr_tot, st);
-        launch_transpose(b.r(R_SYN2T_X, nt), b.r(R_SYN2_X, nt), nt, b.ntr_tot, st);
-        h->launches += 2;
+    // receiver-row records to trace-major records
+    if (b.ntr_tot) {
+        launch_record_gather(b.rrow.p, b.dtrow.p, nt, h->stage == 2 ? 4 : 2, b.X, b.ntr_tot, b.r(R_SYN_Z, nt),
+                             (size_t)b.ntr_tot * nt, st);
+        h->launches++;
     }
     CK(cudaGetLastError());
     if (forward_only) {
@@ -541,6 +563,9 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
         o.trace_misfit = b.tmis.p;
         CK(launch_ot(o, st));
     }
+    // the adjoint sources per packed row, time-major, for the backward sweeps
+    launch_recv_source(b.r(R_RES_Z, nt), b.r(R_RES_X, nt), b.drtr.p, nt, b.X, b.rsp, b.rsrc.p, st);
+    h->launches++;
     h->launches++;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[2], st));
@@ -567,6 +592,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
     fa.gpp = h->gpp.p;
     fa.gps = h->gps.p;
     fa.gil = h->gil.p;
+    fa.grho = h->want_rho ? b.g(G_RHO) : nullptr;
+    fa.grh = h->grh.p;
     launch_finalize(fa, st);
     h->launches++;
     CK(cudaGetLastError());
@@ -610,9 +637,11 @@ int ensure_grads(sfwi_handle *h) {
     CK(h->gpp.ensure(n));
     CK(h->gps.ensure(n));
     CK(h->gil.ensure(n));
+    CK(h->grh.ensure(n));
     CK(cudaMemset(h->gpp.p, 0, n * sizeof(double)));
     CK(cudaMemset(h->gps.p, 0, n * sizeof(double)));
     CK(cudaMemset(h->gil.p, 0, n * sizeof(double)));
+    CK(cudaMemset(h->grh.p, 0, n * sizeof(double)));
     return SFWI_OK;
 }
 
@@ -716,7 +745,7 @@ int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float 
     *out = nullptr;
     if (stage != 1 && stage != 2) return fail(SFWI_E_ARG, "stage must be 1 or 2");
     if (nop != NOP) return fail(SFWI_E_ARG, "nop must be %d (8th-order stencil)", NOP);
-    if (!sou || nt < 1 || dx <= 0 || dz <= 0 || dt <= 0 || pml < NOP + 1 || allnx < 1 || allnz < 1 || ntr < 0)
+    if (!sou || nt < 1 || dx <= 0 || dz <= 0 || dt <= 0 || pml < 2 * NOP || allnx < 1 || allnz < 1 || ntr < 0)
         return fail(SFWI_E_ARG, "bad size or spacing");
     if (nzpml != allnz + 2 * pml) return fail(SFWI_E_ARG, "nzpml must be allnz + 2*pml");
     if (nxpml < 2 * pml + 1) return fail(SFWI_E_ARG, "nxpml must exceed 2*pml");
@@ -771,20 +800,24 @@ int sfwi_destroy(sfwi_handle *h) {
     if (h->st) cudaStreamSynchronize(h->st);
     h->b.drop_graphs();
     h->b.grid.release();
-    h->b.strips.release();
+    h->b.tb.release();
+    h->b.lr.release();
+    h->b.rrow.release();
+    h->b.rsrc.release();
     h->b.recs.release();
     h->b.tmis.release();
     h->b.dsigma.release();
     h->b.dgeo.release();
     h->b.dtiles.release();
-    h->b.dcsr_start.release();
-    h->b.dcsr_trace.release();
+    h->b.dtrow.release();
+    h->b.drtr.release();
     h->b.derr.release();
     h->b.dctr.release();
     for (auto *d : {&h->sou, &h->vp_all, &h->vs_all, &h->rho_all, &h->dvp_all, &h->dvs_all}) d->release();
     h->gpp.release();
     h->gps.release();
     h->gil.release();
+    h->grh.release();
     for (auto &ev : h->ev)
         if (ev) cudaEventDestroy(ev);
     if (h->st) cudaStreamDestroy(h->st);
@@ -863,6 +896,23 @@ int sfwi_set_misfit(sfwi_handle *h, int kind) {
     return SFWI_OK;
 }
 
+int sfwi_set_density_gradient(sfwi_handle *h, int on) {
+    if (int rc = check(h)) return rc;
+    h->want_rho = on != 0;
+    return SFWI_OK;
+}
+
+int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho) {
+    if (int rc = check(h)) return rc;
+    if (!grad_rho) return fail(SFWI_E_ARG, "null output");
+    const size_t n = (size_t)h->allnx * h->allnz;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->st));
+    if (int rc = ensure_grads(h)) return rc;
+    CK(cudaMemcpy(grad_rho, h->grh.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return SFWI_OK;
+}
+
 int sfwi_image_singleshot(sfwi_handle *h, double *misfit) {
     if (int rc = check(h)) return rc;
     if (!h->have_geom || !h->have_rec) return fail(SFWI_E_STATE, "shot geometry and records must be set first");
@@ -904,6 +954,7 @@ int sfwi_imagebuffer_resettozero(sfwi_handle *h, float *grad_pp, float *grad_ps,
         }
         CK(cudaMemset(src[k]->p, 0, n * sizeof(double)));
     }
+    if (h->grh.p) CK(cudaMemset(h->grh.p, 0, n * sizeof(double)));
     for (float *bb : {b1, b2, b3, b4})
         if (bb) std::memset(bb, 0, n * sizeof(float));
     return SFWI_OK;

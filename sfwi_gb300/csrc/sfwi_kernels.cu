@@ -116,6 +116,15 @@ __device__ __forceinline__ void tma_load(float *dst, const CUtensorMap *map, int
         : "memory");
 }
 
+// 2-D tiled bulk tensor load global -> shared (x = innermost coordinate)
+__device__ __forceinline__ void tma_load_2d(float *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // ----------------------------------------------------------------------------
 // stencils on staged boxes (row pitch BZ)
 // ----------------------------------------------------------------------------
@@ -220,13 +229,12 @@ struct CellMap {
     size_t gi;    // packed index of the first cell
     bool live;    // the row is updated and the first cell's column < nzpml-NOP
     bool ok[4];   // cell inside the update region
-    bool frame[4];
     bool image[4];  // inside the imaging interior [pml, n-pml)
 };
 
 __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, const ShotGeo &g) {
     CellMap m;
-    const int tz = threadIdx.x & 7, tr = threadIdx.x >> 3;
+    const int tz = threadIdx.x % (TZ / 4), tr = threadIdx.x / (TZ / 4);
     m.r = tr + HALO;
     m.c = 4 * tz + HALO;
     m.ci = tr * TZ + 4 * tz;
@@ -236,13 +244,11 @@ __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, cons
     const bool row_ok = m.lx >= NOP && m.lx < g.nxpml - NOP;
     m.live = row_ok && m.lz < p.nzpml - NOP;  // lz, P are multiples of 4, so lz+3 < P
     const int pml = p.pml, nzpml = p.nzpml, nxpml = g.nxpml;
-    const bool xf = m.lx < pml || m.lx > nxpml - pml;
     const bool xi = m.lx >= pml && m.lx < nxpml - pml;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         const int z = m.lz + j;
         m.ok[j] = row_ok && z >= NOP && z < nzpml - NOP;
-        m.frame[j] = xf || z < pml || z > nzpml - pml;
         m.image[j] = m.ok[j] && xi && z >= pml && z < nzpml - pml;
     }
     return m;
@@ -284,6 +290,11 @@ __device__ __forceinline__ void S2(float v[4], int h, float2 x) {
     v[2 * h + 1] = x.y;
 }
 __device__ __forceinline__ float2 B2(float x) { return make_float2(x, x); }
+// store a packed pair into cells 2h, 2h+1 of v where the cell is updated
+__device__ __forceinline__ void sel2(float v[4], int h, float2 x, const bool ok[4]) {
+    if (ok[2 * h]) v[2 * h] = x.x;
+    if (ok[2 * h + 1]) v[2 * h + 1] = x.y;
+}
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
@@ -309,22 +320,26 @@ __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const
         st4(f.vz + m.gi, to_f4(s.vz));
         return;
     }
+    // tile with PML cells: the split update of the reference for every cell,
+    //   v_x = (d1 v_x + c_x D_x) r2,  v_z = (d3 v_z + c_z D_z) r4,  v = v_x + v_z,
+    // with the x-part kept in mx and the z-part = v - mx (damping factors are
+    // 1 away from the PML); cells outside the update region keep their values
+    {
+        const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        if (!m.ok[j]) continue;
-        const float cx = dir * ib[j] * p.dtdx, cz_ = dir * ib[j] * p.dtdz;
-        if (FRAME && m.frame[j]) {
-            const float xx = (d.d1[j] * s.mx[j] + cx * ax.v[j]) * d.r2[j];
-            const float xz = (d.d3[j] * (s.vx[j] - s.mx[j]) + cz_ * bz.v[j]) * d.r4[j];
-            const float zx = (d.d1[j] * s.mz[j] + cx * dx_.v[j]) * d.r2[j];
-            const float zz = (d.d3[j] * (s.vz[j] - s.mz[j]) + cz_ * cz.v[j]) * d.r4[j];
-            s.mx[j] = xx;
-            s.mz[j] = zx;
-            s.vx[j] = xx + xz;
-            s.vz[j] = zx + zz;
-        } else {
-            s.vx[j] = s.vx[j] + (cx * ax.v[j] + cz_ * bz.v[j]);
-            s.vz[j] = s.vz[j] + (cx * dx_.v[j] + cz_ * cz.v[j]);
+        for (int h = 0; h < 2; h++) {
+            const float2 i2 = P2(ib, h);
+            const float2 cx = mul2(i2, tx), cz2 = mul2(i2, tz);
+            const float2 d1 = P2(d.d1, h), r2 = P2(d.r2, h), d3 = P2(d.d3, h), r4 = P2(d.r4, h);
+            const float2 mx = P2(s.mx, h), mz = P2(s.mz, h);
+            const float2 xx = mul2(fma2(d1, mx, mul2(cx, P2(ax.v, h))), r2);
+            const float2 xz = mul2(fma2(d3, fma2(mx, neg, P2(s.vx, h)), mul2(cz2, P2(bz.v, h))), r4);
+            const float2 zx = mul2(fma2(d1, mz, mul2(cx, P2(dx_.v, h))), r2);
+            const float2 zz = mul2(fma2(d3, fma2(mz, neg, P2(s.vz, h)), mul2(cz2, P2(cz.v, h))), r4);
+            sel2(s.mx, h, xx, m.ok);
+            sel2(s.mz, h, zx, m.ok);
+            sel2(s.vx, h, add2(xx, xz), m.ok);
+            sel2(s.vz, h, add2(zx, zz), m.ok);
         }
     }
     st4(f.vx + m.gi, to_f4(s.vx));
@@ -366,40 +381,41 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
         st4(f.txz + m.gi, to_f4(s.xz));
         return;
     }
+    // tile with PML cells: the split updates of the reference for every cell
+    // (x-parts in mxx, mzz, mxz; z-part = total - x-part), Born increments
+    // added to the split parts before the damping
+    {
+        const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        if (!m.ok[j]) continue;
-        const float l2m = lam[j] + 2 * mu[j];
-        const float ax = dir * p.dtdx * a.v[j], bz = dir * p.dtdz * b.v[j];
-        const float cz = dir * p.dtdz * c.v[j], dx_ = dir * p.dtdx * d.v[j];
-        // Born increments of the six split parts (xx_x, xx_z, zz_x, zz_z, xz_x, xz_z)
-        float bxx_x = 0.f, bxx_z = 0.f, bzz_x = 0.f, bzz_z = 0.f, bxz_x = 0.f, bxz_z = 0.f;
-        if (born) {
-            bxx_x = born[0][j];
-            bxx_z = born[1][j];
-            bzz_x = born[2][j];
-            bzz_z = born[3][j];
-            bxz_x = born[4][j];
-            bxz_z = born[5][j];
-        }
-        if (FRAME && m.frame[j]) {
-            const float d1 = dm.d1[j], r2 = dm.r2[j], d3 = dm.d3[j], r4 = dm.r4[j];
-            const float nxx_x = (d1 * (s.mxx[j] + bxx_x) + l2m * ax) * r2;
-            const float nxx_z = (d3 * ((s.xx[j] - s.mxx[j]) + bxx_z) + lam[j] * bz) * r4;
-            const float nzz_x = (d1 * (s.mzz[j] + bzz_x) + lam[j] * ax) * r2;
-            const float nzz_z = (d3 * ((s.zz[j] - s.mzz[j]) + bzz_z) + l2m * bz) * r4;
-            const float nxz_x = (d1 * (s.mxz[j] + bxz_x) + mu[j] * dx_) * r2;
-            const float nxz_z = (d3 * ((s.xz[j] - s.mxz[j]) + bxz_z) + mu[j] * cz) * r4;
-            s.mxx[j] = nxx_x;
-            s.mzz[j] = nzz_x;
-            s.mxz[j] = nxz_x;
-            s.xx[j] = nxx_x + nxx_z;
-            s.zz[j] = nzz_x + nzz_z;
-            s.xz[j] = nxz_x + nxz_z;
-        } else {
-            s.xx[j] = s.xx[j] + (bxx_x + bxx_z) + (l2m * ax + lam[j] * bz);
-            s.zz[j] = s.zz[j] + (bzz_x + bzz_z) + (lam[j] * ax + l2m * bz);
-            s.xz[j] = s.xz[j] + (bxz_x + bxz_z) + mu[j] * (dx_ + cz);
+        for (int h = 0; h < 2; h++) {
+            const float2 l = P2(lam, h), u = P2(mu, h);
+            const float2 l2m = fma2(u, B2(2.f), l);
+            const float2 ax = mul2(tx, P2(a.v, h)), bz = mul2(tz, P2(b.v, h));
+            const float2 cz = mul2(tz, P2(c.v, h)), dx_ = mul2(tx, P2(d.v, h));
+            const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
+            float2 mxx = P2(s.mxx, h), mzz = P2(s.mzz, h), mxz = P2(s.mxz, h);
+            float2 zxx = fma2(mxx, neg, P2(s.xx, h)), zzz = fma2(mzz, neg, P2(s.zz, h));
+            float2 zxz = fma2(mxz, neg, P2(s.xz, h));
+            if (born) {
+                mxx = add2(mxx, P2(born[0], h));
+                zxx = add2(zxx, P2(born[1], h));
+                mzz = add2(mzz, P2(born[2], h));
+                zzz = add2(zzz, P2(born[3], h));
+                mxz = add2(mxz, P2(born[4], h));
+                zxz = add2(zxz, P2(born[5], h));
+            }
+            const float2 nxx_x = mul2(fma2(d1, mxx, mul2(l2m, ax)), r2);
+            const float2 nxx_z = mul2(fma2(d3, zxx, mul2(l, bz)), r4);
+            const float2 nzz_x = mul2(fma2(d1, mzz, mul2(l, ax)), r2);
+            const float2 nzz_z = mul2(fma2(d3, zzz, mul2(l2m, bz)), r4);
+            const float2 nxz_x = mul2(fma2(d1, mxz, mul2(u, dx_)), r2);
+            const float2 nxz_z = mul2(fma2(d3, zxz, mul2(u, cz)), r4);
+            sel2(s.mxx, h, nxx_x, m.ok);
+            sel2(s.mzz, h, nzz_x, m.ok);
+            sel2(s.mxz, h, nxz_x, m.ok);
+            sel2(s.xx, h, add2(nxx_x, nxx_z), m.ok);
+            sel2(s.zz, h, add2(nzz_x, nzz_z), m.ok);
+            sel2(s.xz, h, add2(nxz_x, nxz_z), m.ok);
         }
     }
     st4(f.txx + m.gi, to_f4(s.xx));
@@ -438,6 +454,17 @@ __device__ __forceinline__ TileCtx tile_ctx(const Params &p, int ti) {
     return c;
 }
 
+// n (1..3) consecutive grid arrays from `arr` in one instruction: the halo
+// boxes (or core tiles) of the tile land in n consecutive shared-memory slots
+__device__ __forceinline__ void load_boxes(float *dst, const TmaMaps &tm, const TileCtx &c, int arr, int n,
+                                           uint64_t *bar) {
+    tma_load(dst, &tm.box[n - 1], c.bcol, c.brow, arr, bar);
+}
+__device__ __forceinline__ void load_cores(float *dst, const TmaMaps &tm, const TileCtx &c, int arr, int n,
+                                           uint64_t *bar) {
+    tma_load(dst, &tm.core[n - 1], c.ccol, c.crow, arr, bar);
+}
+
 // Warp-specialised tile pipeline.  Warp NTHREADS/32 is the producer: its lane
 // 0 takes the next tile index from this launch's counter (atomicAdd; SMs that
 // drew cheap tiles take more of them), stores the tile's context in shared
@@ -446,10 +473,29 @@ __device__ __forceinline__ TileCtx tile_ctx(const Params &p, int ti) {
 // wait on full[stage], run body(ctx, stage_ptr), and release the stage one
 // arrival per warp.  Every wait is bounded; a wait that gives up sets the
 // error flag and the CTA winds down without leaving a copy in flight.
-//   issue(ctx, stage_ptr, bar): producer lane 0, arms `bar` with expect_tx first
-//   body(ctx, stage_ptr):       consumers; may use consumer_sync()
+//   issue(ctx, stage_ptr, bar):    producer lane 0, arms `bar` with expect_tx first
+//   body(ctx, stage_ptr, release): consumers; may use consumer_sync(); calls
+//                                  release() once its reads of the stage are
+//                                  done, so the refill overlaps its arithmetic
+//                                  and stores (run_tiles releases after the
+//                                  body for a thread that did not)
 constexpr int PRODUCER_WARP = NTHREADS / 32;
 constexpr int BLOCK_THREADS = NTHREADS + 32;
+
+// one consumer thread's release of a stage (idempotent)
+struct StageRelease {
+    uint64_t *bar;
+    bool done;
+    __device__ __forceinline__ void operator()() {
+        if (!done) {
+            // this thread's generic-proxy reads of the stage come before the
+            // asynchronous-proxy writes that refill it
+            fence_proxy_async();
+            mbar_arrive(bar);
+            done = true;
+        }
+    }
+};
 
 template <int STAGE_FLOATS, class Issue, class Body>
 __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body) {
@@ -461,27 +507,33 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
     if (threadIdx.x == 0) {
         for (int s = 0; s < NSTAGE; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], NTHREADS / 32);
+            mbar_init(&empty[s], NTHREADS);
         }
         fence_mbar_init();
     }
     __syncthreads();
     if (warp == PRODUCER_WARP) {
         if (lane != 0) return;
+        // the next tile's index and table entries are fetched before the wait
+        // for a free stage, so their global round trips overlap that wait
+        int t = atomicAdd(counter, 1);
+        TileCtx ctx;
+        if (t < p.ntiles) ctx = tile_ctx(p, t);
         for (int k = 0;; k++) {
             const int s = k % NSTAGE;
             if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1))) {
                 atomicExch(p.err, 2);
                 return;  // consumers give up on full[s] the same way
             }
-            const int t = atomicAdd(counter, 1);
             s_tile[s] = t;
             if (t >= p.ntiles) {
                 mbar_arrive(&full[s]);  // no tile: complete the phase with no bytes
                 return;
             }
-            s_ctx[s] = tile_ctx(p, t);
-            issue(s_ctx[s], sm + s * STAGE_FLOATS, &full[s]);
+            s_ctx[s] = ctx;
+            issue(ctx, sm + s * STAGE_FLOATS, &full[s]);
+            t = atomicAdd(counter, 1);
+            if (t < p.ntiles) ctx = tile_ctx(p, t);
         }
     }
     for (int k = 0;; k++) {
@@ -496,11 +548,10 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
             return;
         }
         if (s_tile[s] >= p.ntiles) return;
-        body(s_ctx[s], sm + s * STAGE_FLOATS);
-        // this stage is refilled by the asynchronous proxy after the release
-        fence_proxy_async();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[s]);
+        const TileCtx ctx = s_ctx[s];  // the producer rewrites s_ctx[s] after the release
+        StageRelease release{&empty[s], false};
+        body(ctx, sm + s * STAGE_FLOATS, release);
+        release();
     }
 }
 
@@ -517,8 +568,7 @@ struct FwdV {
 
 template <bool BORN>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
-    k_fwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
-            int it) {
+    k_fwd_v(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdV<BORN>;
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME;
@@ -526,31 +576,20 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (frame) bytes += (BORN ? 6 : 4) * CORE_BYTES;
         mbar_expect_tx(bar, bytes);
         float *core = s + S::NB * BOX;
-        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_TXX, bar);
-        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_TZZ, bar);
-        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, BG_TXZ, bar);
-        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_IB, bar);
-        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, BG_VX, bar);
-        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_VZ, bar);
+        load_boxes(s, tm, c, BG_TXX, 3, bar);  // txx, tzz, txz
+        load_cores(core + 0 * CORE, tm, c, C_IB, 1, bar);
+        load_cores(core + 1 * CORE, tm, c, BG_VX, 2, bar);  // vx, vz
         if (frame) {
-            tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
-            tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
-            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, BG_MVX, bar);
-            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, BG_MVZ, bar);
+            load_cores(core + 3 * CORE, tm, c, C_DX, 2, bar);    // dampx, dampz
+            load_cores(core + 5 * CORE, tm, c, BG_MVX, 2, bar);  // x-parts of vx, vz
         }
         if (BORN) {
-            tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, SC_TXX, bar);
-            tma_load(s + 4 * BOX, &tbox, c.bcol, c.brow, SC_TZZ, bar);
-            tma_load(s + 5 * BOX, &tbox, c.bcol, c.brow, SC_TXZ, bar);
-            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, SC_VX, bar);
-            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, SC_VZ, bar);
-            if (frame) {
-                tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, SC_MVX, bar);
-                tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, SC_MVZ, bar);
-            }
+            load_boxes(s + 3 * BOX, tm, c, SC_TXX, 3, bar);
+            load_cores(core + 7 * CORE, tm, c, SC_VX, 2, bar);
+            if (frame) load_cores(core + 9 * CORE, tm, c, SC_MVX, 2, bar);
         }
     };
-    auto body = [&](const TileCtx &c, float *s) {
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
         const float *core = s + S::NB * BOX;
         if ((c.t.flags & TILE_SOURCE) && threadIdx.x == 0) {
@@ -564,47 +603,47 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
-        float ib[4];
+        // everything this thread needs from the stage, then release it
+        float ib[4], ex[4], ez[4];
         core4(core, 0, m.ci, ib);
-        Damp d;
         if (frame) {
-            float x[4], z[4];
-            core4(core, 3, m.ci, x);
-            core4(core, 4, m.ci, z);
-            d = make_damp(p, x, z);
+            core4(core, 3, m.ci, ex);
+            core4(core, 4, m.ci, ez);
         }
-        {
-            VState st;
-            core4(core, 1, m.ci, st.vx);
-            core4(core, 2, m.ci, st.vz);
-            const V4 ax = dxp(s_xx, m.r, m.c);
-            const V4 bz = dzm(loadw(s_xz, m.r, m.c));
-            const V4 dx_ = dxm(s_xz, m.r, m.c);
-            const V4 cz = dzp(loadw(s_zz, m.r, m.c));
-            if (frame) {
-                core4(core, 5, m.ci, st.mx);
-                core4(core, 6, m.ci, st.mz);
-                v_apply<true>(p, m, p.bg, st, ib, d, 1.f, ax, bz, dx_, cz);
-            } else {
-                v_apply<false>(p, m, p.bg, st, ib, d, 1.f, ax, bz, dx_, cz);
-            }
+        VState bg, sc;
+        core4(core, 1, m.ci, bg.vx);
+        core4(core, 2, m.ci, bg.vz);
+        if (frame) {
+            core4(core, 5, m.ci, bg.mx);
+            core4(core, 6, m.ci, bg.mz);
         }
+        const V4 ax = dxp(s_xx, m.r, m.c);
+        const V4 bz = dzm(loadw(s_xz, m.r, m.c));
+        const V4 dx_ = dxm(s_xz, m.r, m.c);
+        const V4 cz = dzp(loadw(s_zz, m.r, m.c));
+        V4 sax, sbz, sdx, scz;
         if (BORN) {
             const float *b_xx = s + 3 * BOX, *b_zz = s + 4 * BOX, *b_xz = s + 5 * BOX;
-            VState st;
-            core4(core, 7, m.ci, st.vx);
-            core4(core, 8, m.ci, st.vz);
-            const V4 ax = dxp(b_xx, m.r, m.c);
-            const V4 bz = dzm(loadw(b_xz, m.r, m.c));
-            const V4 dx_ = dxm(b_xz, m.r, m.c);
-            const V4 cz = dzp(loadw(b_zz, m.r, m.c));
+            core4(core, 7, m.ci, sc.vx);
+            core4(core, 8, m.ci, sc.vz);
             if (frame) {
-                core4(core, 9, m.ci, st.mx);
-                core4(core, 10, m.ci, st.mz);
-                v_apply<true>(p, m, p.sc, st, ib, d, 1.f, ax, bz, dx_, cz);
-            } else {
-                v_apply<false>(p, m, p.sc, st, ib, d, 1.f, ax, bz, dx_, cz);
+                core4(core, 9, m.ci, sc.mx);
+                core4(core, 10, m.ci, sc.mz);
             }
+            sax = dxp(b_xx, m.r, m.c);
+            sbz = dzm(loadw(b_xz, m.r, m.c));
+            sdx = dxm(b_xz, m.r, m.c);
+            scz = dzp(loadw(b_zz, m.r, m.c));
+        }
+        release();
+        if (frame) {
+            const Damp d = make_damp(p, ex, ez);
+            v_apply<true>(p, m, p.bg, bg, ib, d, 1.f, ax, bz, dx_, cz);
+            if (BORN) v_apply<true>(p, m, p.sc, sc, ib, d, 1.f, sax, sbz, sdx, scz);
+        } else {
+            const Damp d{};
+            v_apply<false>(p, m, p.bg, bg, ib, d, 1.f, ax, bz, dx_, cz);
+            if (BORN) v_apply<false>(p, m, p.sc, sc, ib, d, 1.f, sax, sbz, sdx, scz);
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body);
@@ -622,37 +661,9 @@ struct FwdS {
     static constexpr int STAGE = NB * BOX + NC * CORE;
 };
 
-// the cells of one edge-strip band (0 top, 1 bottom, 2 left, 3 right) and the
-// slot of a cell inside one step's component block (sfwi_common.cuh layout)
-struct Band {
-    int x0, x1, z0, z1;
-};
-__device__ __forceinline__ Band band_rect(int band, int pml, int nxpml, int nzpml) {
-    Band b;
-    if (band < 2) {
-        b.x0 = pml;
-        b.x1 = nxpml - pml;
-        b.z0 = band == 0 ? pml - NOP : nzpml - pml - NOP;
-        b.z1 = b.z0 + 2 * NOP;
-    } else {
-        b.z0 = pml;
-        b.z1 = nzpml - pml;
-        b.x0 = band == 2 ? pml - NOP : nxpml - pml - NOP;
-        b.x1 = b.x0 + 2 * NOP;
-    }
-    return b;
-}
-__device__ __forceinline__ int band_slot(int band, int lx, int lz, int pml, int nxpml, int nzpml, int nx, int nz) {
-    if (band == 0) return (lx - pml) * 8 + (lz - (pml - NOP));
-    if (band == 1) return 8 * nx + (lx - pml) * 8 + (lz - (nzpml - pml - NOP));
-    if (band == 2) return 16 * nx + (lx - (pml - NOP)) * nz + (lz - pml);
-    return 16 * nx + 8 * nz + (lx - (nxpml - pml - NOP)) * nz + (lz - pml);
-}
-
 template <bool BORN>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
-    k_fwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
-            int it) {
+    k_fwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdS<BORN>;
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME;
@@ -660,151 +671,150 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (frame) bytes += (BORN ? 8 : 5) * CORE_BYTES;
         mbar_expect_tx(bar, bytes);
         float *core = s + S::NB * BOX;
-        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_VX, bar);
-        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_VZ, bar);
-        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_LAM, bar);
-        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, C_MU, bar);
-        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_TXX, bar);
-        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, BG_TZZ, bar);
-        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, BG_TXZ, bar);
+        load_boxes(s, tm, c, BG_VX, 2, bar);  // vx, vz
+        load_cores(core + 0 * CORE, tm, c, C_LAM, 2, bar);   // lam, mu
+        load_cores(core + 2 * CORE, tm, c, BG_TXX, 3, bar);  // txx, tzz, txz
         if (frame) {
-            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
-            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
-            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, BG_MTXX, bar);
-            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, BG_MTZZ, bar);
-            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, BG_MTXZ, bar);
+            load_cores(core + 5 * CORE, tm, c, C_DX, 2, bar);
+            load_cores(core + 7 * CORE, tm, c, BG_MTXX, 3, bar);
         }
         if (BORN) {
-            tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, SC_VX, bar);
-            tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, SC_VZ, bar);
-            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, C_BP, bar);
-            tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, C_BS, bar);
-            tma_load(core + 12 * CORE, &tcore, c.ccol, c.crow, SC_TXX, bar);
-            tma_load(core + 13 * CORE, &tcore, c.ccol, c.crow, SC_TZZ, bar);
-            tma_load(core + 14 * CORE, &tcore, c.ccol, c.crow, SC_TXZ, bar);
-            if (frame) {
-                tma_load(core + 15 * CORE, &tcore, c.ccol, c.crow, SC_MTXX, bar);
-                tma_load(core + 16 * CORE, &tcore, c.ccol, c.crow, SC_MTZZ, bar);
-                tma_load(core + 17 * CORE, &tcore, c.ccol, c.crow, SC_MTXZ, bar);
-            }
+            load_boxes(s + 2 * BOX, tm, c, SC_VX, 2, bar);
+            load_cores(core + 10 * CORE, tm, c, C_BP, 2, bar);  // bp, bs
+            load_cores(core + 12 * CORE, tm, c, SC_TXX, 3, bar);
+            if (frame) load_cores(core + 15 * CORE, tm, c, SC_MTXX, 3, bar);
         }
     };
-    auto body = [&](const TileCtx &c, float *s) {
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         const float *s_vx = s, *s_vz = s + BOX;
         const float *b_vx = s + 2 * BOX, *b_vz = s + 3 * BOX;
         const float *core = s + S::NB * BOX;
         const CellMap m = cell_map(p, c.t, c.g);
         const bool frame = c.t.flags & TILE_FRAME;
-        if (m.live) {
-            float lam[4], mu[4];
-            core4(core, 0, m.ci, lam);
-            core4(core, 1, m.ci, mu);
-            Damp dm;
-            if (frame) {
-                float x[4], z[4];
-                core4(core, 5, m.ci, x);
-                core4(core, 6, m.ci, z);
-                dm = make_damp(p, x, z);
-            }
-            const V4 a = dxm(s_vx, m.r, m.c);
-            const V4 cc = dzp(loadw(s_vx, m.r, m.c));
-            const V4 b = dzm(loadw(s_vz, m.r, m.c));
-            const V4 d = dxp(s_vz, m.r, m.c);
-            {
-                SState st;
-                core4(core, 2, m.ci, st.xx);
-                core4(core, 3, m.ci, st.zz);
-                core4(core, 4, m.ci, st.xz);
-                if (frame) {
-                    core4(core, 7, m.ci, st.mxx);
-                    core4(core, 8, m.ci, st.mzz);
-                    core4(core, 9, m.ci, st.mxz);
-                    s_apply<true>(p, m, p.bg, st, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
-                } else {
-                    s_apply<false>(p, m, p.bg, st, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
-                }
-            }
-            if (BORN) {
-                // Born virtual source from the updated background velocity
-                // (add_born_source_components, sfwi-stage2/born.cu:788-798); bp/bs
-                // are zero outside the Born region
-                float bp[4], bs[4], born[6][4];
-                core4(core, 10, m.ci, bp);
-                core4(core, 11, m.ci, bs);
-#pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const float2 bp2 = P2(bp, h), bs2 = P2(bs, h);
-                    const float2 mix = fma2(bs2, B2(-2.f), bp2);
-                    const float2 ax = mul2(P2(a.v, h), B2(p.idx)), bz = mul2(P2(b.v, h), B2(p.idz));
-                    const float2 dx_ = mul2(P2(d.v, h), B2(p.idx)), cz = mul2(P2(cc.v, h), B2(p.idz));
-                    const float2 dt2 = B2(p.dt);
-                    S2(born[0], h, mul2(dt2, mul2(bp2, ax)));
-                    S2(born[1], h, mul2(dt2, mul2(mix, bz)));
-                    S2(born[2], h, mul2(dt2, mul2(mix, ax)));
-                    S2(born[3], h, mul2(dt2, mul2(bp2, bz)));
-                    S2(born[4], h, mul2(dt2, mul2(bs2, dx_)));
-                    S2(born[5], h, mul2(dt2, mul2(bs2, cz)));
-                }
-                const V4 as = dxm(b_vx, m.r, m.c);
-                const V4 cs = dzp(loadw(b_vx, m.r, m.c));
-                const V4 bs_ = dzm(loadw(b_vz, m.r, m.c));
-                const V4 ds = dxp(b_vz, m.r, m.c);
-                SState st;
-                core4(core, 12, m.ci, st.xx);
-                core4(core, 13, m.ci, st.zz);
-                core4(core, 14, m.ci, st.xz);
-                if (frame) {
-                    core4(core, 15, m.ci, st.mxx);
-                    core4(core, 16, m.ci, st.mzz);
-                    core4(core, 17, m.ci, st.mxz);
-                    s_apply<true>(p, m, p.sc, st, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
-                } else {
-                    s_apply<false>(p, m, p.sc, st, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
-                }
-            }
-        }
-        // receivers on this tile's core: syn[it][trace] (time-major)
+        // receiver row: the velocities at column igz of this tile's core rows,
+        // time-major per packed row (gathered into trace order after the loop)
         if ((c.t.flags & TILE_RECV) && threadIdx.x < TX) {
             const int lx = c.t.x0 + threadIdx.x;
             const int zc = c.g.igz - c.t.z0;
-            if (lx < c.g.nxpml && zc >= 0 && zc < TZ) {
-                const int r = threadIdx.x + HALO, col = zc + HALO;
-                const int b0 = p.csr_start[c.g.csr0 + lx], b1 = p.csr_start[c.g.csr0 + lx + 1];
-                for (int k = b0; k < b1; k++) {
-                    const int tr = p.csr_trace[k];
-                    const size_t o = (size_t)it * p.ntr_tot + tr;
-                    if (BORN) {
-                        p.syn_z[o] = b_vz[r * BZ + col];
-                        p.syn_x[o] = b_vx[r * BZ + col];
-                        p.syn2_z[o] = s_vz[r * BZ + col];
-                        p.syn2_x[o] = s_vx[r * BZ + col];
-                    } else {
-                        p.syn_z[o] = s_vz[r * BZ + col];
-                        p.syn_x[o] = s_vx[r * BZ + col];
-                    }
+            if (lx >= NOP && lx < c.g.nxpml - NOP && zc >= 0 && zc < TZ) {
+                const int bi = (threadIdx.x + HALO) * BZ + zc + HALO;
+                float *rr = p.rrow + (size_t)it * p.nrc * p.X + c.g.row0 + lx;
+                if (BORN) {
+                    rr[0] = b_vz[bi];
+                    rr[(size_t)p.X] = b_vx[bi];
+                    rr[2 * (size_t)p.X] = s_vz[bi];
+                    rr[3 * (size_t)p.X] = s_vx[bi];
+                } else {
+                    rr[0] = s_vz[bi];
+                    rr[(size_t)p.X] = s_vx[bi];
                 }
             }
         }
         // edge strips of the background velocity after this step: the core
         // cells of this tile inside each of the four bands
-        if ((c.t.flags & TILE_STRIP) && p.strips) {
-            const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml, nz = nzpml - 2 * pml;
-            float *sb = p.strips + c.g.strip0 + (long long)it * strip_floats(c.g.nx, nz);
-            const long long cb = strip_comp_floats(c.g.nx, nz);
+        if ((c.t.flags & TILE_STRIP) && p.tb) {
+            const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml;
             for (int band = 0; band < 4; band++) {
                 const Band bb = band_rect(band, pml, nxpml, nzpml);
-                const int rx0 = max(bb.x0, c.t.x0), rx1 = min(bb.x1, c.t.x0 + TX);
-                const int rz0 = max(bb.z0, c.t.z0), rz1 = min(bb.z1, c.t.z0 + TZ);
-                if (rx0 >= rx1 || rz0 >= rz1) continue;
-                const int w = rz1 - rz0, n = (rx1 - rx0) * w;
+                if (max(bb.x0, c.t.x0) >= min(bb.x1, c.t.x0 + TX) || max(bb.z0, c.t.z0) >= min(bb.z1, c.t.z0 + TZ))
+                    continue;
+                // top/bottom: core rows x the band's 8 columns; left/right: the
+                // band's 8 rows x core columns
+                const int n = band < 2 ? TX * 2 * NOP : 2 * NOP * TZ;
                 for (int i = threadIdx.x; i < n; i += NTHREADS) {
-                    const int lx = rx0 + i / w, lz = rz0 + i % w;
+                    int lx, lz;
+                    if (band < 2) {
+                        lx = c.t.x0 + i / (2 * NOP);
+                        lz = bb.z0 + i % (2 * NOP);
+                    } else {
+                        lx = bb.x0 + i / TZ;
+                        lz = c.t.z0 + i % TZ;
+                    }
+                    if (lx < bb.x0 || lx >= bb.x1 || lz < bb.z0 || lz >= bb.z1) continue;
+                    if (lx < c.t.x0 || lx >= c.t.x0 + TX || lz < c.t.z0 || lz >= c.t.z0 + TZ) continue;
                     const int bi = (lx - c.t.x0 + HALO) * BZ + (lz - c.t.z0 + HALO);
-                    const int slot = band_slot(band, lx, lz, pml, nxpml, nzpml, c.g.nx, nz);
-                    sb[slot] = s_vx[bi];
-                    sb[cb + slot] = s_vz[bi];
+                    if (band < 2) {
+                        const long long o = c.g.row0 + lx;
+                        p.tb[tb_row(it, 0, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vx[bi];
+                        p.tb[tb_row(it, 1, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vz[bi];
+                    } else {
+                        const int r = lx - bb.x0;
+                        p.lr[lr_row(it, 0, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vx[bi];
+                        p.lr[lr_row(it, 1, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vz[bi];
+                    }
                 }
             }
+        }
+        if (!m.live) return;
+        // everything this thread needs from the stage, then release it
+        float lam[4], mu[4], ex[4], ez[4];
+        core4(core, 0, m.ci, lam);
+        core4(core, 1, m.ci, mu);
+        if (frame) {
+            core4(core, 5, m.ci, ex);
+            core4(core, 6, m.ci, ez);
+        }
+        const V4 a = dxm(s_vx, m.r, m.c);
+        const V4 cc = dzp(loadw(s_vx, m.r, m.c));
+        const V4 b = dzm(loadw(s_vz, m.r, m.c));
+        const V4 d = dxp(s_vz, m.r, m.c);
+        SState bg, sc;
+        core4(core, 2, m.ci, bg.xx);
+        core4(core, 3, m.ci, bg.zz);
+        core4(core, 4, m.ci, bg.xz);
+        if (frame) {
+            core4(core, 7, m.ci, bg.mxx);
+            core4(core, 8, m.ci, bg.mzz);
+            core4(core, 9, m.ci, bg.mxz);
+        }
+        float bp[4], bs[4];
+        V4 as, cs, bs_, ds;
+        if (BORN) {
+            core4(core, 10, m.ci, bp);
+            core4(core, 11, m.ci, bs);
+            as = dxm(b_vx, m.r, m.c);
+            cs = dzp(loadw(b_vx, m.r, m.c));
+            bs_ = dzm(loadw(b_vz, m.r, m.c));
+            ds = dxp(b_vz, m.r, m.c);
+            core4(core, 12, m.ci, sc.xx);
+            core4(core, 13, m.ci, sc.zz);
+            core4(core, 14, m.ci, sc.xz);
+            if (frame) {
+                core4(core, 15, m.ci, sc.mxx);
+                core4(core, 16, m.ci, sc.mzz);
+                core4(core, 17, m.ci, sc.mxz);
+            }
+        }
+        release();
+        Damp dm{};
+        if (frame) dm = make_damp(p, ex, ez);
+        if (frame)
+            s_apply<true>(p, m, p.bg, bg, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
+        else
+            s_apply<false>(p, m, p.bg, bg, lam, mu, dm, 1.f, a, b, cc, d, nullptr);
+        if (BORN) {
+            // Born virtual source from the updated background velocity
+            // (add_born_source_components, sfwi-stage2/born.cu:788-798); bp/bs
+            // are zero outside the Born region
+            float born[6][4];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float2 bp2 = P2(bp, h), bs2 = P2(bs, h);
+                const float2 mix = fma2(bs2, B2(-2.f), bp2);
+                const float2 ax = mul2(P2(a.v, h), B2(p.idx)), bz = mul2(P2(b.v, h), B2(p.idz));
+                const float2 dx_ = mul2(P2(d.v, h), B2(p.idx)), cz = mul2(P2(cc.v, h), B2(p.idz));
+                const float2 dt2 = B2(p.dt);
+                S2(born[0], h, mul2(dt2, mul2(bp2, ax)));
+                S2(born[1], h, mul2(dt2, mul2(mix, bz)));
+                S2(born[2], h, mul2(dt2, mul2(mix, ax)));
+                S2(born[3], h, mul2(dt2, mul2(bp2, bz)));
+                S2(born[4], h, mul2(dt2, mul2(bs2, dx_)));
+                S2(born[5], h, mul2(dt2, mul2(bs2, cz)));
+            }
+            if (frame)
+                s_apply<true>(p, m, p.sc, sc, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
+            else
+                s_apply<false>(p, m, p.sc, sc, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body);
@@ -818,118 +828,169 @@ struct BwdS {
     // core: 0 lam, 1 mu, 2 txx, 3 tzz, 4 txz, 5 atxx, 6 atzz, 7 atxz,
     //       8 dampx, 9 dampz, 10 mtxx, 11 mtzz, 12 mtxz, 13 amtxz, 14 glam, 15 gmu
     static constexpr int NC = 16;
-    static constexpr int STAGE = NB * BOX + NC * CORE;
+    // edge strips of step `it` inside the box: one top/bottom band (vx, vz:
+    // BX rows x 8) and one left/right band (vx, vz: 8 rows x BZ); the
+    // residual source of step `it` for the box rows (BX rows x 4 columns)
+    static constexpr int TBF = BX * 2 * NOP, LRF = 2 * NOP * BZ, RSF = BX * 4;
+    static constexpr int STRIPS = NB * BOX + NC * CORE;
+    static constexpr int RS = STRIPS + 2 * TBF + 2 * LRF;
+    static constexpr int STAGE = RS + RSF;
 };
+// every TMA destination of a stage starts on a 128-byte boundary
+static_assert((BOX * 4) % 128 == 0 && (CORE * 4) % 128 == 0, "box/core alignment");
+static_assert((BwdS::TBF * 4) % 128 == 0 && (BwdS::LRF * 4) % 128 == 0 && (BwdS::RSF * 4) % 128 == 0,
+              "strip/residual slot alignment");
+
+// the top/bottom and the left/right band whose part inside the tile's box the
+// producer stages by TMA (-1: none); a second band of the same kind (only on
+// grids a box spans from edge to edge) is read from global memory instead
+struct StripPick {
+    int tb, lr;
+};
+__device__ __forceinline__ bool band_hits_box(const Band &b, int bx, int bz) {
+    return max(b.x0, bx) < min(b.x1, bx + BX) && max(b.z0, bz) < min(b.z1, bz + BZ);
+}
+__device__ __forceinline__ StripPick strip_pick(const TileCtx &c, int pml, int nzpml) {
+    StripPick sp{-1, -1};
+    const int bx = c.t.x0 - HALO, bz = c.bcol, nxpml = c.g.nxpml;
+    for (int b = 0; b < 2 && sp.tb < 0; b++)
+        if (band_hits_box(band_rect(b, pml, nxpml, nzpml), bx, bz)) sp.tb = b;
+    for (int b = 0; b < 2 && sp.lr < 0; b++)
+        if (band_hits_box(band_rect(b + 2, pml, nxpml, nzpml), bx, bz)) sp.lr = b;
+    return sp;
+}
+// bit pattern marking a packed row without a receiver in the residual source
+constexpr uint32_t NO_RECEIVER = 0xFFFFFFFFu;
 
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
-    k_bwd_s(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
-            int it, float adj_dir) {
+    k_bwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
     using S = BwdS;
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
-        const uint32_t bytes =
-            S::NB * BOX_BYTES + (8 + (frame ? 6 : 0) + (image ? 2 : 0)) * CORE_BYTES;
+        const bool strip = c.t.flags & TILE_STRIP, recv = c.t.flags & TILE_RECV;
+        const StripPick sp = strip ? strip_pick(c, p.pml, p.nzpml) : StripPick{-1, -1};
+        const uint32_t bytes = S::NB * BOX_BYTES + (8 + (frame ? 6 : 0) + (image ? 2 : 0)) * CORE_BYTES +
+                               (sp.tb >= 0 ? 2 * S::TBF * 4 : 0) + (sp.lr >= 0 ? 2 * S::LRF * 4 : 0) +
+                               (recv ? S::RSF * 4 : 0);
         mbar_expect_tx(bar, bytes);
         float *core = s + S::NB * BOX;
-        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_VX, bar);
-        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_VZ, bar);
-        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, AD_VX, bar);
-        tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, AD_VZ, bar);
-        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_LAM, bar);
-        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, C_MU, bar);
-        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_TXX, bar);
-        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, BG_TZZ, bar);
-        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, BG_TXZ, bar);
-        tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, AD_TXX, bar);
-        tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, AD_TZZ, bar);
-        tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, AD_TXZ, bar);
+        load_boxes(s, tm, c, BG_VX, 2, bar);            // vx, vz
+        load_boxes(s + 2 * BOX, tm, c, AD_VX, 2, bar);  // adjoint vx, vz
+        load_cores(core + 0 * CORE, tm, c, C_LAM, 2, bar);
+        load_cores(core + 2 * CORE, tm, c, BG_TXX, 3, bar);
+        load_cores(core + 5 * CORE, tm, c, AD_TXX, 3, bar);
         if (frame) {
-            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
-            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
-            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, BG_MTXX, bar);
-            tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, BG_MTZZ, bar);
-            tma_load(core + 12 * CORE, &tcore, c.ccol, c.crow, BG_MTXZ, bar);
-            tma_load(core + 13 * CORE, &tcore, c.ccol, c.crow, AD_MTXZ, bar);
+            load_cores(core + 8 * CORE, tm, c, C_DX, 2, bar);
+            load_cores(core + 10 * CORE, tm, c, BG_MTXX, 3, bar);
+            load_cores(core + 13 * CORE, tm, c, AD_MTXZ, 1, bar);
         }
-        if (image) {
-            tma_load(core + 14 * CORE, &tcore, c.ccol, c.crow, G_LAM, bar);
-            tma_load(core + 15 * CORE, &tcore, c.ccol, c.crow, G_MU, bar);
+        if (image) load_cores(core + 14 * CORE, tm, c, G_LAM, 2, bar);  // G_lam, G_mu
+        // rows of the strip arrays are addressed by (step, component, band,
+        // row); a box row before a shot's first row reads either the fill
+        // (negative coordinate) or rows no band cell maps to
+        for (int comp = 0; comp < 2; comp++) {
+            if (sp.tb >= 0)
+                tma_load_2d(s + S::STRIPS + comp * S::TBF, &tm.tb, 0, (int)tb_row(it, comp, sp.tb, p.X, c.brow), bar);
+            if (sp.lr >= 0)
+                tma_load_2d(s + S::STRIPS + 2 * S::TBF + comp * S::LRF, &tm.lr, c.bcol,
+                            (int)lr_row(it, comp, sp.lr, p.nshots, c.t.shot, 0), bar);
         }
+        if (recv) tma_load_2d(s + S::RS, &tm.rs, (2 * it) & ~3, c.brow, bar);
     };
-    auto body = [&](const TileCtx &c, float *s) {
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         float *s_vx = s, *s_vz = s + BOX, *a_vx = s + 2 * BOX, *a_vz = s + 3 * BOX;
         const float *core = s + S::NB * BOX;
-        const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml, nz = nzpml - 2 * pml;
+        const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml;
         if (c.t.flags & TILE_STRIP) {
             // the saved strips of step `it` replace vx, vz in this sweep's view:
             // the box cells inside each band (a cell in two bands holds the
-            // same value in both)
-            const float *sb = p.strips + c.g.strip0 + (long long)it * strip_floats(c.g.nx, nz);
-            const long long cb = strip_comp_floats(c.g.nx, nz);
+            // same value in both), from the staged slots or, for a second band
+            // of one kind, from global memory
+            const StripPick sp = strip_pick(c, pml, nzpml);
+            const float *tbs = s + S::STRIPS, *lrs = s + S::STRIPS + 2 * S::TBF;
             const int bx = c.t.x0 - HALO, bz = c.bcol;
             for (int band = 0; band < 4; band++) {
                 const Band bb = band_rect(band, pml, nxpml, nzpml);
-                const int rx0 = max(bb.x0, bx), rx1 = min(bb.x1, bx + BX);
-                const int rz0 = max(bb.z0, bz), rz1 = min(bb.z1, bz + BZ);
-                if (rx0 >= rx1 || rz0 >= rz1) continue;
-                const int w = rz1 - rz0, n = (rx1 - rx0) * w;
+                if (!band_hits_box(bb, bx, bz)) continue;
+                const bool staged = band < 2 ? band == sp.tb : band - 2 == sp.lr;
+                // top/bottom: box rows x the band's 8 columns; left/right: the
+                // band's 8 rows x box columns (fixed shapes, no division)
+                const int n = band < 2 ? BX * 2 * NOP : 2 * NOP * BZ;
                 for (int i = threadIdx.x; i < n; i += NTHREADS) {
-                    const int lx = rx0 + i / w, lz = rz0 + i % w;
+                    int lx, lz;
+                    if (band < 2) {
+                        lx = bx + i / (2 * NOP);
+                        lz = bb.z0 + i % (2 * NOP);
+                    } else {
+                        lx = bb.x0 + i / BZ;
+                        lz = bz + i % BZ;
+                    }
+                    if (lx < bb.x0 || lx >= bb.x1 || lz < bb.z0 || lz >= bb.z1) continue;
+                    if (lx < bx || lx >= bx + BX || lz < bz || lz >= bz + BZ) continue;
+                    float vx, vz;
+                    if (band < 2) {
+                        if (staged) {
+                            vx = tbs[i];  // slot (lx - bx) * 8 + (lz - z0)
+                            vz = tbs[S::TBF + i];
+                        } else {
+                            const int prow = c.g.row0 + lx;
+                            vx = p.tb[tb_row(it, 0, band, p.X, prow) * 8 + (lz - bb.z0)];
+                            vz = p.tb[tb_row(it, 1, band, p.X, prow) * 8 + (lz - bb.z0)];
+                        }
+                    } else {
+                        if (staged) {
+                            vx = lrs[i];  // slot (lx - x0) * BZ + (lz - bz)
+                            vz = lrs[S::LRF + i];
+                        } else {
+                            vx = p.lr[lr_row(it, 0, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
+                            vz = p.lr[lr_row(it, 1, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
+                        }
+                    }
                     const int bi = (lx - bx) * BZ + (lz - bz);
-                    const int slot = band_slot(band, lx, lz, pml, nxpml, nzpml, c.g.nx, nz);
-                    s_vx[bi] = sb[slot];
-                    s_vz[bi] = sb[cb + slot];
+                    s_vx[bi] = vx;
+                    s_vz[bi] = vz;
                 }
             }
         }
         if ((c.t.flags & TILE_RECV) && threadIdx.x < BX) {
             // the residual of step `it` replaces the adjoint velocity at the
-            // receivers in this sweep's view (the highest trace index wins
-            // where several traces share a cell)
+            // receivers in this sweep's view (rows without a receiver carry
+            // the NO_RECEIVER pattern)
             const int lx = c.t.x0 - HALO + threadIdx.x;
             const int zc = c.g.igz - c.bcol;
             if (lx >= 0 && lx < nxpml && zc >= 0 && zc < BZ) {
-                const int b0 = p.csr_start[c.g.csr0 + lx], b1 = p.csr_start[c.g.csr0 + lx + 1];
-                if (b1 > b0) {
-                    const int tr = p.csr_trace[b1 - 1];
-                    const size_t o = (size_t)tr * p.nt + it;
-                    a_vz[threadIdx.x * BZ + zc] = p.res_z[o];
-                    a_vx[threadIdx.x * BZ + zc] = p.res_x[o];
+                const float *rs = s + S::RS + threadIdx.x * 4 + (2 * it - ((2 * it) & ~3));
+                if (__float_as_uint(rs[0]) != NO_RECEIVER) {
+                    a_vz[threadIdx.x * BZ + zc] = rs[0];
+                    a_vx[threadIdx.x * BZ + zc] = rs[1];
                 }
             }
         }
         consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
-        const bool frame = c.t.flags & TILE_FRAME;
-        float lam[4], mu[4];
+        const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
+        // everything this thread needs from the stage, then release it
+        float lam[4], mu[4], ex[4], ez[4];
         core4(core, 0, m.ci, lam);
         core4(core, 1, m.ci, mu);
-        Damp dm;
         if (frame) {
-            float x[4], z[4];
-            core4(core, 8, m.ci, x);
-            core4(core, 9, m.ci, z);
-            dm = make_damp(p, x, z);
+            core4(core, 8, m.ci, ex);
+            core4(core, 9, m.ci, ez);
         }
         // reconstruction (direction -1) with strains
         const V4 a = dxm(s_vx, m.r, m.c);
         const V4 cc = dzp(loadw(s_vx, m.r, m.c));
         const V4 b = dzm(loadw(s_vz, m.r, m.c));
         const V4 d = dxp(s_vz, m.r, m.c);
-        {
-            SState st;
-            core4(core, 2, m.ci, st.xx);
-            core4(core, 3, m.ci, st.zz);
-            core4(core, 4, m.ci, st.xz);
-            if (frame) {
-                core4(core, 10, m.ci, st.mxx);
-                core4(core, 11, m.ci, st.mzz);
-                core4(core, 12, m.ci, st.mxz);
-                s_apply<true>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
-            } else {
-                s_apply<false>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
-            }
+        SState st;
+        core4(core, 2, m.ci, st.xx);
+        core4(core, 3, m.ci, st.zz);
+        core4(core, 4, m.ci, st.xz);
+        if (frame) {
+            core4(core, 10, m.ci, st.mxx);
+            core4(core, 11, m.ci, st.mzz);
+            core4(core, 12, m.ci, st.mxz);
         }
         // adjoint stresses: txx' = x-part only, tzz' = z-part only, txz split
         float axx[4], azz[4], axz[4], amxz[4];
@@ -941,6 +1002,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         const V4 ca = dzp(loadw(a_vx, m.r, m.c));
         const V4 ba = dzm(loadw(a_vz, m.r, m.c));
         const V4 da = dxp(a_vz, m.r, m.c);
+        float gl[4], gm[4];
+        if (image) {
+            core4(core, 14, m.ci, gl);
+            core4(core, 15, m.ci, gm);
+        }
+        release();
+        Damp dm{};
+        if (frame) dm = make_damp(p, ex, ez);
+        if (frame)
+            s_apply<true>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
+        else
+            s_apply<false>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
         if (!frame) {
             const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz);
 #pragma unroll
@@ -949,24 +1022,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
                 S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
             }
-        } else
+        } else {
+            // PML tile: txx' keeps only an x-part and tzz' only a z-part, txz'
+            // is split (x-part in amxz); damping factors are 1 away from the PML
+            const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (!m.ok[j]) continue;
-            const float ax = adj_dir * p.dtdx * aa.v[j], bz = adj_dir * p.dtdz * ba.v[j];
-            const float cz = adj_dir * p.dtdz * ca.v[j], dx_ = adj_dir * p.dtdx * da.v[j];
-            if (m.frame[j]) {
-                const float d1 = dm.d1[j], r2 = dm.r2[j], d3 = dm.d3[j], r4 = dm.r4[j];
-                axx[j] = (d1 * axx[j] + ax) * r2;
-                azz[j] = (d3 * azz[j] + bz) * r4;
-                const float nx_ = (d1 * amxz[j] + dx_) * r2;
-                const float nz_ = (d3 * (axz[j] - amxz[j]) + cz) * r4;
-                amxz[j] = nx_;
-                axz[j] = nx_ + nz_;
-            } else {
-                axx[j] = axx[j] + ax;
-                azz[j] = azz[j] + bz;
-                axz[j] = axz[j] + (dx_ + cz);
+            for (int h = 0; h < 2; h++) {
+                const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
+                const float2 nxx = mul2(fma2(d1, P2(axx, h), mul2(tx, P2(aa.v, h))), r2);
+                const float2 nzz = mul2(fma2(d3, P2(azz, h), mul2(tz, P2(ba.v, h))), r4);
+                const float2 nx_ = mul2(fma2(d1, P2(amxz, h), mul2(tx, P2(da.v, h))), r2);
+                const float2 nz_ = mul2(fma2(d3, fma2(P2(amxz, h), neg, P2(axz, h)), mul2(tz, P2(ca.v, h))), r4);
+                sel2(axx, h, nxx, m.ok);
+                sel2(azz, h, nzz, m.ok);
+                sel2(amxz, h, nx_, m.ok);
+                sel2(axz, h, add2(nx_, nz_), m.ok);
             }
         }
         st4(p.ad.txx + m.gi, to_f4(axx));
@@ -974,10 +1044,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         st4(p.ad.txz + m.gi, to_f4(axz));
         if (frame) st4(p.ad.mtxz + m.gi, to_f4(amxz));
         // zero-lag imaging of the lambda and mu kernels (interior cells)
-        if (c.t.flags & TILE_IMAGE) {
-            float gl[4], gm[4];
-            core4(core, 14, m.ci, gl);
-            core4(core, 15, m.ci, gm);
+        if (image) {
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
@@ -1014,38 +1081,27 @@ struct BwdV {
 };
 
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
-    k_bwd_v(const Params p, const __grid_constant__ CUtensorMap tbox, const __grid_constant__ CUtensorMap tcore,
-            int it, float adj_dir) {
+    k_bwd_v(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
     using S = BwdV;
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
         const uint32_t bytes = S::NB * BOX_BYTES + (5 + (frame ? 6 : 0) + (image ? 1 : 0)) * CORE_BYTES;
         mbar_expect_tx(bar, bytes);
         float *core = s + S::NB * BOX;
-        tma_load(s + 0 * BOX, &tbox, c.bcol, c.brow, BG_TXX, bar);
-        tma_load(s + 1 * BOX, &tbox, c.bcol, c.brow, BG_TZZ, bar);
-        tma_load(s + 2 * BOX, &tbox, c.bcol, c.brow, BG_TXZ, bar);
-        tma_load(s + 3 * BOX, &tbox, c.bcol, c.brow, AD_TXX, bar);
-        tma_load(s + 4 * BOX, &tbox, c.bcol, c.brow, AD_TZZ, bar);
-        tma_load(s + 5 * BOX, &tbox, c.bcol, c.brow, AD_TXZ, bar);
-        tma_load(s + 6 * BOX, &tbox, c.bcol, c.brow, C_LAM, bar);
-        tma_load(s + 7 * BOX, &tbox, c.bcol, c.brow, C_MU, bar);
-        tma_load(core + 0 * CORE, &tcore, c.ccol, c.crow, C_IB, bar);
-        tma_load(core + 1 * CORE, &tcore, c.ccol, c.crow, BG_VX, bar);
-        tma_load(core + 2 * CORE, &tcore, c.ccol, c.crow, BG_VZ, bar);
-        tma_load(core + 3 * CORE, &tcore, c.ccol, c.crow, AD_VX, bar);
-        tma_load(core + 4 * CORE, &tcore, c.ccol, c.crow, AD_VZ, bar);
+        load_boxes(s, tm, c, BG_TXX, 3, bar);            // txx, tzz, txz
+        load_boxes(s + 3 * BOX, tm, c, AD_TXX, 3, bar);  // adjoint txx, tzz, txz
+        load_boxes(s + 6 * BOX, tm, c, C_LAM, 2, bar);   // lam, mu
+        load_cores(core + 0 * CORE, tm, c, C_IB, 1, bar);
+        load_cores(core + 1 * CORE, tm, c, BG_VX, 2, bar);
+        load_cores(core + 3 * CORE, tm, c, AD_VX, 2, bar);
         if (frame) {
-            tma_load(core + 5 * CORE, &tcore, c.ccol, c.crow, C_DX, bar);
-            tma_load(core + 6 * CORE, &tcore, c.ccol, c.crow, C_DZ, bar);
-            tma_load(core + 7 * CORE, &tcore, c.ccol, c.crow, BG_MVX, bar);
-            tma_load(core + 8 * CORE, &tcore, c.ccol, c.crow, BG_MVZ, bar);
-            tma_load(core + 9 * CORE, &tcore, c.ccol, c.crow, AD_MVX, bar);
-            tma_load(core + 10 * CORE, &tcore, c.ccol, c.crow, AD_MVZ, bar);
+            load_cores(core + 5 * CORE, tm, c, C_DX, 2, bar);
+            load_cores(core + 7 * CORE, tm, c, BG_MVX, 2, bar);
+            load_cores(core + 9 * CORE, tm, c, AD_MVX, 2, bar);
         }
-        if (image) tma_load(core + 11 * CORE, &tcore, c.ccol, c.crow, G_ILL, bar);
+        if (image) load_cores(core + 11 * CORE, tm, c, G_ILL, 1, bar);
     };
-    auto body = [&](const TileCtx &c, float *s) {
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         const float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
         float *s_P = s + 3 * BOX, *s_Q = s + 4 * BOX, *s_R = s + 5 * BOX;
         const float *s_l = s + 6 * BOX, *s_u = s + 7 * BOX;
@@ -1073,55 +1129,75 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
-        const bool frame = c.t.flags & TILE_FRAME;
-        float ib[4];
+        const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
+        // everything this thread needs from the stage, then release it
+        float ib[4], ex[4], ez[4], il[4];
         core4(core, 0, m.ci, ib);
-        Damp dm;
         if (frame) {
-            float x[4], z[4];
-            core4(core, 5, m.ci, x);
-            core4(core, 6, m.ci, z);
-            dm = make_damp(p, x, z);
+            core4(core, 5, m.ci, ex);
+            core4(core, 6, m.ci, ez);
         }
-        {
-            VState st;
-            core4(core, 1, m.ci, st.vx);
-            core4(core, 2, m.ci, st.vz);
-            const V4 ax = dxp(s_xx, m.r, m.c);
-            const V4 bz = dzm(loadw(s_xz, m.r, m.c));
-            const V4 dx_ = dxm(s_xz, m.r, m.c);
-            const V4 cz = dzp(loadw(s_zz, m.r, m.c));
-            if (frame) {
-                core4(core, 7, m.ci, st.mx);
-                core4(core, 8, m.ci, st.mz);
-                v_apply<true>(p, m, p.bg, st, ib, dm, -1.f, ax, bz, dx_, cz);
-            } else {
-                v_apply<false>(p, m, p.bg, st, ib, dm, -1.f, ax, bz, dx_, cz);
-            }
-            if (c.t.flags & TILE_IMAGE) {
-                float il[4];
-                core4(core, 11, m.ci, il);
+        VState bg, ad;
+        core4(core, 1, m.ci, bg.vx);
+        core4(core, 2, m.ci, bg.vz);
+        if (frame) {
+            core4(core, 7, m.ci, bg.mx);
+            core4(core, 8, m.ci, bg.mz);
+        }
+        const V4 ax = dxp(s_xx, m.r, m.c);
+        const V4 bz = dzm(loadw(s_xz, m.r, m.c));
+        const V4 dx_ = dxm(s_xz, m.r, m.c);
+        const V4 cz = dzp(loadw(s_zz, m.r, m.c));
+        if (image) core4(core, 11, m.ci, il);
+        core4(core, 3, m.ci, ad.vx);
+        core4(core, 4, m.ci, ad.vz);
+        if (frame) {
+            core4(core, 9, m.ci, ad.mx);
+            core4(core, 10, m.ci, ad.mz);
+        }
+        const V4 aax = dxp(s_P, m.r, m.c);
+        const V4 abz = dzm(loadw(s_R, m.r, m.c));
+        const V4 adx = dxm(s_R, m.r, m.c);
+        const V4 acz = dzp(loadw(s_Q, m.r, m.c));
+        release();
+        Damp dm{};
+        if (frame) dm = make_damp(p, ex, ez);
+        // density kernel (when requested) needs the velocity step of this
+        // sweep, (v(it) - v(it-1)) / dt.  Imaging cells lie outside the PML,
+        // where the reconstruction (direction -1) subtracts dt (1/rho) D sigma,
+        // so the step is formed from that increment directly rather than as a
+        // difference of two nearly equal velocities.
+        const bool rho_img = p.grho != nullptr && image;
+        float gvx[4], gvz[4];
+        if (rho_img) {
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (m.image[j]) il[j] += st.vx[j] * st.vx[j] + st.vz[j] * st.vz[j];
-                st4(p.illum + m.gi, to_f4(il));
+            for (int j = 0; j < 4; j++) {
+                gvx[j] = ib[j] * (ax.v[j] * p.idx + bz.v[j] * p.idz);
+                gvz[j] = ib[j] * (dx_.v[j] * p.idx + cz.v[j] * p.idz);
             }
         }
-        {
-            VState st;
-            core4(core, 3, m.ci, st.vx);
-            core4(core, 4, m.ci, st.vz);
-            const V4 ax = dxp(s_P, m.r, m.c);
-            const V4 bz = dzm(loadw(s_R, m.r, m.c));
-            const V4 dx_ = dxm(s_R, m.r, m.c);
-            const V4 cz = dzp(loadw(s_Q, m.r, m.c));
-            if (frame) {
-                core4(core, 9, m.ci, st.mx);
-                core4(core, 10, m.ci, st.mz);
-                v_apply<true>(p, m, p.ad, st, ib, dm, adj_dir, ax, bz, dx_, cz);
-            } else {
-                v_apply<false>(p, m, p.ad, st, ib, dm, adj_dir, ax, bz, dx_, cz);
-            }
+        if (frame)
+            v_apply<true>(p, m, p.bg, bg, ib, dm, -1.f, ax, bz, dx_, cz);
+        else
+            v_apply<false>(p, m, p.bg, bg, ib, dm, -1.f, ax, bz, dx_, cz);
+        if (image) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (m.image[j]) il[j] += bg.vx[j] * bg.vx[j] + bg.vz[j] * bg.vz[j];
+            st4(p.illum + m.gi, to_f4(il));
+        }
+        if (frame)
+            v_apply<true>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
+        else
+            v_apply<false>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
+        if (rho_img) {
+            // G_rho -= v_adj . (v(it) - v(it-1)) / dt
+            float gr[4];
+            f4_to(ld4(p.grho + m.gi), gr);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (m.image[j]) gr[j] -= ad.vx[j] * gvx[j] + ad.vz[j] * gvz[j];
+            st4(p.grho + m.gi, to_f4(gr));
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
@@ -1163,21 +1239,21 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
     switch (which) {
         case 0:
             if (born)
-                k_fwd_v<true><<<grid, BLOCK_THREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_v<true><<<grid, BLOCK_THREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm, it);
             else
-                k_fwd_v<false><<<grid, BLOCK_THREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_v<false><<<grid, BLOCK_THREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm, it);
             break;
         case 1:
             if (born)
-                k_fwd_s<true><<<grid, BLOCK_THREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_s<true><<<grid, BLOCK_THREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm, it);
             else
-                k_fwd_s<false><<<grid, BLOCK_THREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm.box, tm.core, it);
+                k_fwd_s<false><<<grid, BLOCK_THREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm, it);
             break;
         case 2:
-            k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm, it, adj_dir);
             break;
         default:
-            k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm.box, tm.core, it, adj_dir);
+            k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm, it, adj_dir);
             break;
     }
 }

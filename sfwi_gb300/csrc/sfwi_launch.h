@@ -8,10 +8,15 @@
 namespace sfwi {
 
 // sfwi_kernels.cu
-// TMA descriptors of the packed grid: 3-D [array][row][column], boxes of
-// (TX+2*HALO) x (TZ+2*HALO) and TX x TZ floats
+// TMA descriptors of the packed grid, 3-D [array][row][column]: box[k] and
+// core[k] fetch k+1 consecutive arrays per instruction as (TX+2*HALO) x
+// (TZ+2*HALO) halo boxes or TX x TZ core tiles (one TMA instruction costs the
+// issuing warp about the same whatever its size, so arrays read together are
+// fetched together)
 struct TmaMaps {
-    CUtensorMap box, core;
+    CUtensorMap box[3], core[3];
+    CUtensorMap tb, lr;  // edge strips (top/bottom, left/right layouts)
+    CUtensorMap rs;      // residual source per packed row [X][2 nt]
 };
 cudaError_t configure_step_kernels();
 void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st);
@@ -29,7 +34,10 @@ struct SetupArgs {
     const ShotGeo *geo;
 };
 void launch_setup(const SetupArgs &a, int nshots, int max_nxpml, cudaStream_t st);
-void launch_transpose(const float *in, float *out, int nt, int ntr, cudaStream_t st);
+void launch_record_gather(const float *rrow, const int *trow, int nt, int nrc, int X, int ntr, float *out,
+                          size_t cstride, cudaStream_t st);
+void launch_recv_source(const float *res_z, const float *res_x, const int *rtr, int nt, int X, int rsp, float *rs,
+                        cudaStream_t st);
 void launch_residual_l2(int stage, int nt, int ntr_tot, const float *syn_z, const float *syn_x, const float *syn2_z,
                         const float *syn2_x, const float *obs_z, const float *obs_x, float *res_z, float *res_x,
                         double *trace_misfit, cudaStream_t st);
@@ -38,6 +46,8 @@ struct FinalArgs {
     const ShotGeo *geo;
     const float *glam, *gmu, *illum, *vp, *vs, *rho;
     double *gpp, *gps, *gil;
+    const float *grho;  // density kernel per cell, or null
+    double *grh;
 };
 void launch_finalize(const FinalArgs &a, cudaStream_t st);
 

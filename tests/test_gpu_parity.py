@@ -167,3 +167,21 @@ def test_deterministic_repeat():
     for k in KEYS:
         assert np.array_equal(a[k], b[k]), k
     assert a["misfit"] == b["misfit"]
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_density_gradient_matches_fp64_oracle(case):
+    """The density kernel (no reference counterpart, parity with the oracle
+    only) next to the Vp/Vs gradients of the same run."""
+    from tests.helpers import make_engine
+    shot, inputs, _ = load_case(case)
+    ref = po.run_shot("f64", shot, inputs, want_rho=True)
+    fd = make_engine(shot, inputs)
+    fd.set_density_gradient(True)
+    out = run_ref_api(shot, inputs, fd=fd)
+    grho = fd.read_density_gradient_f64()
+    fd.close()
+    assert np.linalg.norm(ref["grad_rho"]) > 0
+    assert rel(grho, ref["grad_rho"]) < TOL, rel(grho, ref["grad_rho"])
+    for k in ("grad_pp", "grad_ps", "illum"):
+        assert rel(out[k], ref[k]) < TOL, (k, rel(out[k], ref[k]))

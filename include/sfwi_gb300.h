@@ -128,6 +128,29 @@ int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit);
  * sfwi_read_records; clears the queue */
 int sfwi_run_forward(sfwi_handle *h);
 
+/* ---- line searches ----
+ * CALCULATE_ALPHA_parabola_mb (sfwi-stage1/FD2DGPU.cu:4819-5036, stage 1):
+ * the L2 misfit of the current shot at the trial models vp - s grad_pp,
+ * vs - s grad_ps for s = 0, step1, step2 (background forward only; rho
+ * unchanged), added to *misfit_step0..2.  grad_* are [allnx][allnz] host
+ * arrays; the uploaded model is left as it was. */
+int sfwi_calculate_alpha_parabola_mb(sfwi_handle *h, const float *grad_pp, const float *grad_ps, float step1,
+                                     float step2, double *misfit_step0, double *misfit_step1, double *misfit_step2);
+/* CALCULATE_ALPHA (sfwi-stage2/FD2DGPU.cu:4576-4722, stage 2): Born runs of
+ * the current shot with the model perturbation image_pp/ps (giving the
+ * residual r = (du - d) + u0) and with the search direction cg_pp/ps (giving
+ * its scattered records q); *fenzi += sum q.r, *fenmu += sum q.q. */
+int sfwi_calculate_alpha(sfwi_handle *h, const float *image_pp, const float *image_ps, const float *cg_pp,
+                         const float *cg_ps, double *fenzi, double *fenmu);
+/* The same two searches over every queued shot at once: all shots and all
+ * trial models advance in the same forward launches.  misfit3[k] += the
+ * misfit at step k; per_shot3 (may be NULL) receives [shot][3];
+ * per_shot2 (may be NULL) receives [shot][fenzi, fenmu].  Clear the queue. */
+int sfwi_line_search_parabola(sfwi_handle *h, const float *grad_pp, const float *grad_ps, float step1, float step2,
+                              double *misfit3, double *per_shot3);
+int sfwi_line_search_exact(sfwi_handle *h, const float *image_pp, const float *image_ps, const float *cg_pp,
+                           const float *cg_ps, double *fenzi, double *fenmu, double *per_shot2);
+
 /* ---- optimal-transport misfit (declared, not implemented, in the reference:
  *      OT / OT_power / OT_alltrace, sfwi-stage1/FD2DGPU.cuh:21-25) ----
  * obs/cal/res are host [tracenum][length]; misfit += W2 over traces and both

@@ -181,6 +181,50 @@ class FD2DGPU_ELASTIC:
             self._keep = []
         return m.value, per[:n]
 
+    # -- line searches --
+    def CALCULATE_ALPHA_parabola_mb(self, grad_pp, grad_ps, step1, step2):
+        """Misfits (m0, m1, m2) of the current shot at the trial models
+        m - s*grad, s = 0, step1, step2 (stage 1)."""
+        g1, g2 = _f32(grad_pp), _f32(grad_ps)
+        m = [C.c_double(0.0) for _ in range(3)]
+        _lib.check(_lib.load().sfwi_calculate_alpha_parabola_mb(self._h, _fp(g1), _fp(g2), float(step1), float(step2),
+                                                               *[C.byref(x) for x in m]))
+        return tuple(x.value for x in m)
+
+    def CALCULATE_ALPHA(self, image_pp, image_ps, cg_pp, cg_ps):
+        """(fenzi, fenmu) of the current shot (stage 2)."""
+        arrs = [_f32(a) for a in (image_pp, image_ps, cg_pp, cg_ps)]
+        zi, mu = C.c_double(0.0), C.c_double(0.0)
+        _lib.check(_lib.load().sfwi_calculate_alpha(self._h, *[_fp(a) for a in arrs], C.byref(zi), C.byref(mu)))
+        return zi.value, mu.value
+
+    def line_search_parabola(self, grad_pp, grad_ps, step1, step2, nshots=None):
+        """Queued shots at three trial models: (misfit[3], per_shot[nshots, 3])."""
+        n = nshots if nshots is not None else len(self._keep) // 3
+        g1, g2 = _f32(grad_pp), _f32(grad_ps)
+        m = np.zeros(3, np.float64)
+        per = np.zeros((max(n, 1), 3), np.float64)
+        dp = C.POINTER(C.c_double)
+        try:
+            _lib.check(_lib.load().sfwi_line_search_parabola(self._h, _fp(g1), _fp(g2), float(step1), float(step2),
+                                                             m.ctypes.data_as(dp), per.ctypes.data_as(dp)))
+        finally:
+            self._keep = []
+        return m, per[:n]
+
+    def line_search_exact(self, image_pp, image_ps, cg_pp, cg_ps, nshots=None):
+        """Queued shots: (fenzi, fenmu, per_shot[nshots, 2])."""
+        n = nshots if nshots is not None else len(self._keep) // 3
+        arrs = [_f32(a) for a in (image_pp, image_ps, cg_pp, cg_ps)]
+        zi, mu = C.c_double(0.0), C.c_double(0.0)
+        per = np.zeros((max(n, 1), 2), np.float64)
+        try:
+            _lib.check(_lib.load().sfwi_line_search_exact(self._h, *[_fp(a) for a in arrs], C.byref(zi), C.byref(mu),
+                                                          per.ctypes.data_as(C.POINTER(C.c_double))))
+        finally:
+            self._keep = []
+        return zi.value, mu.value, per[:n]
+
     def run_forward(self):
         try:
             _lib.check(_lib.load().sfwi_run_forward(self._h))

@@ -40,6 +40,10 @@ SIGNATURES = {
     "sfwi_enqueue_shot": (C.c_int, [_h, C.POINTER(ShotDesc)]),
     "sfwi_run": (C.c_int, [_h, _dp, _dp]),
     "sfwi_run_forward": (C.c_int, [_h]),
+    "sfwi_calculate_alpha_parabola_mb": (C.c_int, [_h, _fp, _fp, C.c_float, C.c_float, _dp, _dp, _dp]),
+    "sfwi_calculate_alpha": (C.c_int, [_h, _fp, _fp, _fp, _fp, _dp, _dp]),
+    "sfwi_line_search_parabola": (C.c_int, [_h, _fp, _fp, C.c_float, C.c_float, _dp, _dp]),
+    "sfwi_line_search_exact": (C.c_int, [_h, _fp, _fp, _fp, _fp, _dp, _dp, _dp]),
     "sfwi_ot": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),
     "sfwi_ot_power": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),
     "sfwi_ot_alltrace": (C.c_int, [_fp, _fp, _fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_float, _dp]),

@@ -26,11 +26,12 @@ __global__ void k_setup(SetupArgs a) {
             const int cx = min(max(lx, a.pml), g.nxpml - a.pml - 1) - a.pml;
             const int cz = min(max(lz, a.pml), a.nzpml - a.pml - 1) - a.pml;
             const size_t go = (size_t)(g.win0 + cx) * a.allnz + cz;
-            vp = a.vp_all[go];
-            vs = a.vs_all[go];
+            const size_t gv = go + (size_t)g.model * a.vslot, gm = go + (size_t)g.model * a.mslot;
+            vp = a.vp_all[gv];
+            vs = a.vs_all[gv];
             rho = a.stage == 2 ? 2000.f : a.rho_all[go];
-            if (a.dvp_all) dmp = a.dvp_all[go];
-            if (a.dvs_all) dms = a.dvs_all[go];
+            if (a.dvp_all) dmp = a.dvp_all[gm];
+            if (a.dvs_all) dms = a.dvs_all[gm];
             const int pml = a.pml;
             if (lx < pml) dx = (float)(l10 * (5.0 * vp / (2.0 * pml)) * powf((float)(1.0 * (pml - lx) / pml), 4.0f));
             if (lx > g.nxpml - pml)
@@ -145,7 +146,7 @@ __global__ void k_residual_l2(int stage, int nt, const float *syn_z, const float
         }
         res_z[o + t] = rz;
         res_x[o + t] = rx;
-        acc += (double)(rz * rz + rx * rx);
+        acc += (double)__fadd_rn(__fmul_rn(rz, rz), __fmul_rn(rx, rx));
     }
     const double s = block_sum(acc, red);
     if (threadIdx.x == 0) trace_misfit[blockIdx.x] = s;
@@ -196,6 +197,46 @@ __global__ void k_finalize(FinalArgs a) {
             if (a.grho) a.grh[i] = rh;
         }
     }
+}
+
+__global__ void k_trial_models(const float *__restrict__ base, const float *__restrict__ g,
+                               const float *__restrict__ steps, int nslot, size_t n, float *__restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float b = base[i], gi = g[i];
+        for (int k = 0; k < nslot; k++) out[(size_t)k * n + i] = __fsub_rn(b, __fmul_rn(steps[k], gi));
+    }
+}
+
+void launch_trial_models(const float *base, const float *g, const float *steps, int nslot, size_t n, float *out,
+                         cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_trial_models<<<blocks, 256, 0, st>>>(base, g, steps, nslot, n, out);
+}
+
+// the sums of CALCULATE_ALPHA (sfwi-stage2/FD2DGPU.cu:4705-4710): per sample
+// (a_z b_z + a_x b_x) and (a_z a_z + a_x a_x) in float, summed in double
+__global__ void k_trace_dots(const float *az, const float *ax, const float *bz, const float *bx, int nt, double *ab,
+                             double *aa) {
+    __shared__ double red[32];
+    const size_t o = (size_t)blockIdx.x * nt;
+    double sab = 0.0, saa = 0.0;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        const float z = az[o + t], x = ax[o + t];
+        sab += (double)__fadd_rn(__fmul_rn(z, bz[o + t]), __fmul_rn(x, bx[o + t]));
+        saa += (double)__fadd_rn(__fmul_rn(z, z), __fmul_rn(x, x));
+    }
+    const double tab = block_sum(sab, red);
+    const double taa = block_sum(saa, red);
+    if (threadIdx.x == 0) {
+        ab[blockIdx.x] = tab;
+        aa[blockIdx.x] = taa;
+    }
+}
+
+void launch_trace_dots(const float *az, const float *ax, const float *bz, const float *bx, int nt, int ntr,
+                       double *ab, double *aa, cudaStream_t st) {
+    if (ntr > 0) k_trace_dots<<<ntr, 256, 0, st>>>(az, ax, bz, bx, nt, ab, aa);
 }
 
 void launch_finalize(const FinalArgs &a, cudaStream_t st) {

@@ -48,7 +48,7 @@ struct ShotGeo {
     int ntr;       // traces of this shot
     int tr0;       // first trace in the packed trace arrays
     int win0;      // global-model column of interior column 0 (delta_left + record_left_in_v)
-    int pad_;
+    int model;     // model slot the shot's window is cut from (line searches run several models)
 };
 
 // tile table entry: shot, first local row, first column, flags

@@ -68,6 +68,7 @@ struct DevBuf {
 
 struct ShotIn {
     int nx, win0, isx, isz, igz, ngx_left, ntr;
+    int model = 0;  // model slot (line searches)
     std::vector<int> gc;
     const float *obs_z = nullptr, *obs_x = nullptr;  // host [ntr][nt]
 };
@@ -140,6 +141,11 @@ struct sfwi_handle {
     float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
     bool use_graphs = true;
     bool last_forward_only = false;
+    // trial models of a line search: while set, shots cut their windows from
+    // these slot arrays instead of the uploaded model
+    const float *slot_vp = nullptr, *slot_vs = nullptr, *slot_dvp = nullptr, *slot_dvs = nullptr;
+    bool force_l2 = false;  // the exact step length is defined on the L2 residual
+    DevBuf<float> ls_buf;   // trial models and search directions
 };
 
 namespace {
@@ -234,6 +240,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
         g.ntr = in.ntr;
         g.tr0 = tr0;
         g.win0 = in.win0;
+        g.model = in.model;
         // receiver rows: the record of a trace is its cell (rix, igz), which
         // stays zero outside the update region [NOP, n-NOP); the residual
         // injected at a cell is the highest-index trace recorded there
@@ -348,7 +355,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     return p;
 }
 
-int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_only) {
+int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_only, bool with_obs) {
     Batch &b = h->b;
     const int nt = h->nt;
     const size_t recs = (size_t)NREC * std::max(b.ntr_tot, 1) * nt;
@@ -399,7 +406,7 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(cudaMemsetAsync(b.grid.p, 0, (size_t)NSTATE * b.cells * sizeof(float), st));
     CK(cudaMemsetAsync(b.recs.p, 0, recs * sizeof(float), st));
     // observed records, trace-major
-    if (!forward_only) {
+    if (with_obs) {
         for (size_t s = 0; s < shots.size(); s++) {
             const ShotIn &in = shots[s];
             const size_t off = (size_t)b.geo[s].tr0 * nt, n = (size_t)in.ntr * nt;
@@ -417,11 +424,14 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     a.stage = h->stage;
     a.born_lo = h->stage == 2 ? NOP : h->pml;
     a.dt = h->dt;
-    a.vp_all = h->vp_all.p;
-    a.vs_all = h->vs_all.p;
+    const size_t nmodel = (size_t)h->allnx * h->allnz;
+    a.vp_all = h->slot_vp ? h->slot_vp : h->vp_all.p;
+    a.vs_all = h->slot_vs ? h->slot_vs : h->vs_all.p;
+    a.vslot = h->slot_vp ? nmodel : 0;
     a.rho_all = h->have_rho ? h->rho_all.p : h->vp_all.p;
-    a.dvp_all = h->stage == 2 && h->have_m ? h->dvp_all.p : nullptr;
-    a.dvs_all = h->stage == 2 && h->have_m ? h->dvs_all.p : nullptr;
+    a.dvp_all = h->slot_dvp ? h->slot_dvp : (h->stage == 2 && h->have_m ? h->dvp_all.p : nullptr);
+    a.dvs_all = h->slot_dvs ? h->slot_dvs : (h->stage == 2 && h->have_m ? h->dvs_all.p : nullptr);
+    a.mslot = h->slot_dvp ? nmodel : 0;
     a.ib = b.g(C_IB);
     a.lam = b.g(C_LAM);
     a.mu = b.g(C_MU);
@@ -485,17 +495,67 @@ int capture(sfwi_handle *h, cudaGraphExec_t *out, bool fwd, const Params &p, boo
     return SFWI_OK;
 }
 
-int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_only, double *misfit,
-              double *per_shot) {
+// Wait for the run, check the device error flag, read the per-trace misfits
+// back and sum them per shot (in shot and trace order) into per_shot[] and
+// *misfit (added).
+int collect_misfit(sfwi_handle *h, int misfit_kind, double *misfit, double *per_shot, bool backward) {
+    Batch &b = h->b;
+    cudaStream_t st = h->st;
+    std::vector<double> tm(2 * (size_t)b.ntr_tot);
+    const size_t nm = misfit_kind == SFWI_MISFIT_L2 ? b.ntr_tot : 2 * (size_t)b.ntr_tot;
+    if (nm) CK(cudaMemcpyAsync(tm.data(), b.tmis.p, nm * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
+    cudaEventElapsedTime(&h->fwd_ms, h->ev[0], h->ev[1]);
+    if (backward) {
+        cudaEventElapsedTime(&h->other_ms, h->ev[1], h->ev[2]);
+        cudaEventElapsedTime(&h->bwd_ms, h->ev[2], h->ev[3]);
+    } else {
+        h->other_ms = h->bwd_ms = 0.f;
+    }
+    cudaEventElapsedTime(&h->total_ms, h->ev[4], h->ev[5]);
+    double total = 0.0;
+    for (int s = 0; s < b.nshots; s++) {
+        double ms = 0.0;
+        const ShotGeo &g = b.geo[s];
+        for (int t = 0; t < g.ntr; t++) {
+            if (misfit_kind == SFWI_MISFIT_L2)
+                ms += tm[g.tr0 + t];
+            else
+                ms += tm[2 * (size_t)(g.tr0 + t)] + tm[2 * (size_t)(g.tr0 + t) + 1];
+        }
+        if (per_shot) per_shot[s] = ms;
+        total += ms;
+    }
+    if (misfit) *misfit += total;
+    return SFWI_OK;
+}
+
+int finish_misfit(sfwi_handle *h, int misfit_kind, double *misfit, double *per_shot) {
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[5], h->st));
+    return collect_misfit(h, misfit_kind, misfit, per_shot, false);
+}
+
+// what a run computes: a shot-gradient pass, the forward records only, or
+// the forward records with the residual and misfit (line searches)
+enum RunMode { RUN_GRADIENT, RUN_FORWARD, RUN_MISFIT };
+
+int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double *misfit, double *per_shot) {
     if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
     if (shots.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    const bool forward_only = mode != RUN_GRADIENT;
+    const int misfit_kind = h->force_l2 ? SFWI_MISFIT_L2 : h->misfit_kind;
     h->last_forward_only = forward_only;
     CK(cudaSetDevice(h->device));
     int rc = build_batch(h, shots);
     if (rc) return rc;
-    if (!forward_only && h->misfit_kind != SFWI_MISFIT_L2 && ot_smem_bytes(h->nt) > 227 * 1024)
+    if (mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2 && ot_smem_bytes(h->nt) > 227 * 1024)
         return fail(SFWI_E_ARG, "OT misfit supports nt <= %d", (int)(227 * 1024 / 32));
-    rc = upload_batch(h, shots, forward_only);
+    rc = upload_batch(h, shots, forward_only, mode != RUN_FORWARD);
     if (rc) return rc;
     Batch &b = h->b;
     const Params p = make_params(h, forward_only);
@@ -527,7 +587,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
         h->launches++;
     }
     CK(cudaGetLastError());
-    if (forward_only) {
+    if (mode == RUN_FORWARD) {
         CK(cudaEventRecord(h->ev[5], st));
         int derr = 0;
         CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -540,13 +600,13 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
         return SFWI_OK;
     }
     // adjoint source and misfit
-    if (h->misfit_kind == SFWI_MISFIT_L2) {
+    if (misfit_kind == SFWI_MISFIT_L2) {
         launch_residual_l2(h->stage, nt, b.ntr_tot, b.r(R_SYN_Z, nt), b.r(R_SYN_X, nt), b.r(R_SYN2_Z, nt),
                            b.r(R_SYN2_X, nt), b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), b.r(R_RES_Z, nt), b.r(R_RES_X, nt),
                            b.tmis.p, st);
     } else {
         OtArgs o{};
-        o.kind = h->misfit_kind;
+        o.kind = misfit_kind;
         o.nt = nt;
         o.ntr = b.ntr_tot;
         o.stage = h->stage;
@@ -563,6 +623,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
         o.trace_misfit = b.tmis.p;
         CK(launch_ot(o, st));
     }
+    if (mode == RUN_MISFIT) return finish_misfit(h, misfit_kind, misfit, per_shot);
     // the adjoint sources per packed row, time-major, for the backward sweeps
     launch_recv_source(b.r(R_RES_Z, nt), b.r(R_RES_X, nt), b.drtr.p, nt, b.X, b.rsp, b.rsrc.p, st);
     h->launches++;
@@ -598,36 +659,132 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_onl
     h->launches++;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[5], st));
-    std::vector<double> tm(2 * (size_t)b.ntr_tot);
-    const size_t nm = h->misfit_kind == SFWI_MISFIT_L2 ? b.ntr_tot : 2 * (size_t)b.ntr_tot;
-    if (nm) CK(cudaMemcpyAsync(tm.data(), b.tmis.p, nm * sizeof(double), cudaMemcpyDeviceToHost, st));
-    int derr = 0;
-    CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
-    cudaEventElapsedTime(&h->fwd_ms, h->ev[0], h->ev[1]);
-    cudaEventElapsedTime(&h->other_ms, h->ev[1], h->ev[2]);
-    cudaEventElapsedTime(&h->bwd_ms, h->ev[2], h->ev[3]);
-    cudaEventElapsedTime(&h->total_ms, h->ev[4], h->ev[5]);
-    double total = 0.0;
-    for (int s = 0; s < b.nshots; s++) {
-        double ms = 0.0;
-        const ShotGeo &g = b.geo[s];
-        for (int t = 0; t < g.ntr; t++) {
-            if (h->misfit_kind == SFWI_MISFIT_L2)
-                ms += tm[g.tr0 + t];
-            else
-                ms += tm[2 * (size_t)(g.tr0 + t)] + tm[2 * (size_t)(g.tr0 + t) + 1];
-        }
-        if (per_shot) per_shot[s] = ms;
-        total += ms;
-    }
-    if (misfit) *misfit += total;
-    return SFWI_OK;
+    return collect_misfit(h, misfit_kind, misfit, per_shot, true);
 }
 
 int check(sfwi_handle *h) {
     if (!h) return fail(SFWI_E_ARG, "null handle");
+    return SFWI_OK;
+}
+
+// the shot described by the reference-shaped per-shot calls
+int current_shot(sfwi_handle *h, ShotIn &s) {
+    if (!h->have_geom || !h->have_rec) return fail(SFWI_E_STATE, "shot geometry and records must be set first");
+    s.nx = h->nxpml - 2 * h->pml;
+    // the window is the one bufferVpVsHtoD cut; the gradient lands at delta_left + record_left_in_v
+    s.win0 = h->delta_left + h->record_left_in_v;
+    if (s.win0 != h->ngx_min)
+        return fail(SFWI_E_ARG, "bufferVpVsHtoD(%d) and delta_left+record_left_in_v=%d differ", h->ngx_min, s.win0);
+    s.isx = h->isx;
+    s.isz = h->isz;
+    s.igz = h->igz;
+    s.ngx_left = h->ngx_left;
+    s.ntr = h->ntr;
+    s.gc = h->gc;
+    s.obs_z = h->rec_z.data();
+    s.obs_x = h->rec_x.data();
+    return SFWI_OK;
+}
+
+// Stage-1 parabola line search over shots q: the misfit of every shot at the
+// trial models m - step_k g, k = 0, 1, 2 (steps 0, step1, step2), all shots and
+// all three models advancing in the same forward launches.
+int line_search_parabola(sfwi_handle *h, const std::vector<ShotIn> &q, const float *grad_pp, const float *grad_ps,
+                         float step1, float step2, double m[3], double *per_shot) {
+    if (h->stage != 1) return fail(SFWI_E_STATE, "the parabola line search belongs to stage 1");
+    if (!grad_pp || !grad_ps) return fail(SFWI_E_ARG, "null search direction");
+    if (q.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
+    const size_t n = (size_t)h->allnx * h->allnz;
+    const int ns = (int)q.size();
+    CK(cudaSetDevice(h->device));
+    CK(h->ls_buf.ensure(8 * n + 4));
+    float *gpp = h->ls_buf.p, *gps = gpp + n, *vps = gps + n, *vss = vps + 3 * n, *steps = vss + 3 * n;
+    const float st3[3] = {0.f, step1, step2};
+    CK(cudaMemcpyAsync(gpp, grad_pp, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(gps, grad_ps, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(steps, st3, sizeof st3, cudaMemcpyHostToDevice, h->st));
+    launch_trial_models(h->vp_all.p, gpp, steps, 3, n, vps, h->st);
+    launch_trial_models(h->vs_all.p, gps, steps, 3, n, vss, h->st);
+    h->launches += 2;
+    CK(cudaGetLastError());
+    std::vector<ShotIn> all;
+    for (int k = 0; k < 3; k++)
+        for (const ShotIn &s : q) {
+            all.push_back(s);
+            all.back().model = k;
+        }
+    std::vector<double> per(3 * (size_t)ns);
+    h->slot_vp = vps;
+    h->slot_vs = vss;
+    const int rc = run_batch(h, all, RUN_MISFIT, nullptr, per.data());
+    h->slot_vp = h->slot_vs = nullptr;
+    if (rc) return rc;
+    for (int k = 0; k < 3; k++)
+        for (int s = 0; s < ns; s++) {
+            m[k] += per[(size_t)k * ns + s];
+            if (per_shot) per_shot[(size_t)s * 3 + k] = per[(size_t)k * ns + s];
+        }
+    return SFWI_OK;
+}
+
+// Stage-2 exact step length over shots q: a Born run with the model
+// perturbation `image` gives the residual r = (du - d) + u0, a Born run with
+// the search direction `cg` gives its scattered records q; fenzi += sum q.r,
+// fenmu += sum q.q (alpha = fenzi / fenmu).  Both runs of every shot advance
+// in the same forward launches.
+int line_search_exact(sfwi_handle *h, const std::vector<ShotIn> &q, const float *image_pp, const float *image_ps,
+                      const float *cg_pp, const float *cg_ps, double *fenzi, double *fenmu, double *per_shot) {
+    if (h->stage != 2) return fail(SFWI_E_STATE, "the exact line search belongs to stage 2");
+    if (!image_pp || !image_ps || !cg_pp || !cg_ps) return fail(SFWI_E_ARG, "null model perturbation");
+    if (q.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
+    const size_t n = (size_t)h->allnx * h->allnz;
+    const int ns = (int)q.size();
+    CK(cudaSetDevice(h->device));
+    CK(h->ls_buf.ensure(4 * n));
+    float *dvp = h->ls_buf.p, *dvs = dvp + 2 * n;
+    CK(cudaMemcpyAsync(dvp, image_pp, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(dvp + n, cg_pp, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(dvs, image_ps, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(dvs + n, cg_ps, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    std::vector<ShotIn> all;
+    for (int k = 0; k < 2; k++)
+        for (const ShotIn &s : q) {
+            all.push_back(s);
+            all.back().model = k;
+        }
+    h->slot_dvp = dvp;
+    h->slot_dvs = dvs;
+    h->force_l2 = true;
+    int rc = run_batch(h, all, RUN_MISFIT, nullptr, nullptr);
+    h->slot_dvp = h->slot_dvs = nullptr;
+    h->force_l2 = false;
+    if (rc) return rc;
+    Batch &b = h->b;
+    const int nt = h->nt, T = b.ntr_tot / 2;
+    const size_t off = (size_t)T * nt;
+    launch_trace_dots(b.r(R_SYN_Z, nt) + off, b.r(R_SYN_X, nt) + off, b.r(R_RES_Z, nt), b.r(R_RES_X, nt), nt, T,
+                      b.tmis.p, b.tmis.p + T, h->st);
+    h->launches++;
+    CK(cudaGetLastError());
+    std::vector<double> d(2 * (size_t)T);
+    if (T) CK(cudaMemcpyAsync(d.data(), b.tmis.p, 2 * (size_t)T * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int s = 0; s < ns; s++) {
+        const ShotGeo &g = b.geo[s];
+        double zi = 0.0, mu = 0.0;
+        for (int t = 0; t < g.ntr; t++) {
+            zi += d[g.tr0 + t];
+            mu += d[T + g.tr0 + t];
+        }
+        *fenzi += zi;
+        *fenmu += mu;
+        if (per_shot) {
+            per_shot[2 * (size_t)s] = zi;
+            per_shot[2 * (size_t)s + 1] = mu;
+        }
+    }
     return SFWI_OK;
 }
 
@@ -818,6 +975,7 @@ int sfwi_destroy(sfwi_handle *h) {
     h->gps.release();
     h->gil.release();
     h->grh.release();
+    h->ls_buf.release();
     for (auto &ev : h->ev)
         if (ev) cudaEventDestroy(ev);
     if (h->st) cudaStreamDestroy(h->st);
@@ -915,24 +1073,10 @@ int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho) {
 
 int sfwi_image_singleshot(sfwi_handle *h, double *misfit) {
     if (int rc = check(h)) return rc;
-    if (!h->have_geom || !h->have_rec) return fail(SFWI_E_STATE, "shot geometry and records must be set first");
-    ShotIn s;
-    s.nx = h->nxpml - 2 * h->pml;
-    // the window is the one bufferVpVsHtoD cut; the gradient lands at delta_left + record_left_in_v
-    s.win0 = h->delta_left + h->record_left_in_v;
-    if (s.win0 != h->ngx_min)
-        return fail(SFWI_E_ARG, "bufferVpVsHtoD(%d) and delta_left+record_left_in_v=%d differ", h->ngx_min, s.win0);
-    s.isx = h->isx;
-    s.isz = h->isz;
-    s.igz = h->igz;
-    s.ngx_left = h->ngx_left;
-    s.ntr = h->ntr;
-    s.gc = h->gc;
-    s.obs_z = h->rec_z.data();
-    s.obs_x = h->rec_x.data();
-    std::vector<ShotIn> v{std::move(s)};
+    std::vector<ShotIn> v(1);
+    if (int rc = current_shot(h, v[0])) return rc;
     double m = 0.0;
-    int rc = run_batch(h, v, false, &m, nullptr);
+    int rc = run_batch(h, v, RUN_GRADIENT, &m, nullptr);
     if (rc) return rc;
     if (misfit) *misfit += m;
     return SFWI_OK;
@@ -1015,17 +1159,58 @@ int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit) {
     std::vector<ShotIn> q;
     q.swap(h->queue);
     double m = 0.0;
-    int rc = run_batch(h, q, false, &m, per_shot_misfit);
+    int rc = run_batch(h, q, RUN_GRADIENT, &m, per_shot_misfit);
     if (rc) return rc;
     if (misfit) *misfit += m;
     return SFWI_OK;
+}
+
+int sfwi_calculate_alpha_parabola_mb(sfwi_handle *h, const float *grad_pp, const float *grad_ps, float step1,
+                                     float step2, double *misfit_step0, double *misfit_step1, double *misfit_step2) {
+    if (int rc = check(h)) return rc;
+    if (!misfit_step0 || !misfit_step1 || !misfit_step2) return fail(SFWI_E_ARG, "null output");
+    std::vector<ShotIn> v(1);
+    if (int rc = current_shot(h, v[0])) return rc;
+    double m[3] = {0.0, 0.0, 0.0};
+    if (int rc = line_search_parabola(h, v, grad_pp, grad_ps, step1, step2, m, nullptr)) return rc;
+    *misfit_step0 += m[0];
+    *misfit_step1 += m[1];
+    *misfit_step2 += m[2];
+    return SFWI_OK;
+}
+
+int sfwi_calculate_alpha(sfwi_handle *h, const float *image_pp, const float *image_ps, const float *cg_pp,
+                         const float *cg_ps, double *fenzi, double *fenmu) {
+    if (int rc = check(h)) return rc;
+    if (!fenzi || !fenmu) return fail(SFWI_E_ARG, "null output");
+    std::vector<ShotIn> v(1);
+    if (int rc = current_shot(h, v[0])) return rc;
+    return line_search_exact(h, v, image_pp, image_ps, cg_pp, cg_ps, fenzi, fenmu, nullptr);
+}
+
+int sfwi_line_search_parabola(sfwi_handle *h, const float *grad_pp, const float *grad_ps, float step1, float step2,
+                              double *misfit3, double *per_shot3) {
+    if (int rc = check(h)) return rc;
+    if (!misfit3) return fail(SFWI_E_ARG, "null output");
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    return line_search_parabola(h, q, grad_pp, grad_ps, step1, step2, misfit3, per_shot3);
+}
+
+int sfwi_line_search_exact(sfwi_handle *h, const float *image_pp, const float *image_ps, const float *cg_pp,
+                           const float *cg_ps, double *fenzi, double *fenmu, double *per_shot2) {
+    if (int rc = check(h)) return rc;
+    if (!fenzi || !fenmu) return fail(SFWI_E_ARG, "null output");
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    return line_search_exact(h, q, image_pp, image_ps, cg_pp, cg_ps, fenzi, fenmu, per_shot2);
 }
 
 int sfwi_run_forward(sfwi_handle *h) {
     if (int rc = check(h)) return rc;
     std::vector<ShotIn> q;
     q.swap(h->queue);
-    return run_batch(h, q, true, nullptr, nullptr);
+    return run_batch(h, q, RUN_FORWARD, nullptr, nullptr);
 }
 
 int sfwi_ot(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x, float *res_z,

@@ -30,6 +30,7 @@ struct SetupArgs {
     int X, P, nzpml, pml, allnz, stage, born_lo;
     float dt;
     const float *vp_all, *vs_all, *rho_all, *dvp_all, *dvs_all;
+    size_t vslot, mslot;  // floats between model slots of vp/vs and of dvp/dvs (0: one model)
     float *ib, *lam, *mu, *dampx, *dampz, *bp, *bs, *vp, *vs, *rho;
     const ShotGeo *geo;
 };
@@ -50,6 +51,14 @@ struct FinalArgs {
     double *grh;
 };
 void launch_finalize(const FinalArgs &a, cudaStream_t st);
+// out[k] = base[k] - step[k] * g (k < nslot; no fused multiply-add, as the
+// reference forms its trial models on the host)
+void launch_trial_models(const float *base, const float *g, const float *steps, int nslot, size_t n, float *out,
+                         cudaStream_t st);
+// per trace tr < ntr: sum_t (a.b) and sum_t (a.a) over the z and x components
+// of trace-major records, each term formed in float and summed in double
+void launch_trace_dots(const float *az, const float *ax, const float *bz, const float *bx, int nt, int ntr,
+                       double *ab, double *aa, cudaStream_t st);
 
 // sfwi_ot.cu
 struct OtArgs {

@@ -281,6 +281,12 @@ static int receiver_ix(int stage, int pml, int gc, int ngx_left, float dx) {
     return pml + (int)((float)(gc - ngx_left) / dx);
 }
 
+/* column where the residual of a trace is injected,
+ * GPUapplysource_backward_from_record: dx stays a float in both stages
+ * (sfwi-stage1/FD2DGPU.cu:3425-3441, sfwi-stage2/FD2DGPU.cu:3357-3370), so in
+ * stage 2 it differs from the recording column when dx is not a whole number */
+static int injection_ix(int pml, int gc, int ngx_left, float dx) { return pml + (int)((float)(gc - ngx_left) / dx); }
+
 /* edge strips of vx/vz: record_edge_wavefield / load_edge_wavefield
  * (sfwi-stage1/FD2DGPU.cu:3842-3899).  save=1 copies field -> strip. */
 static void edge_strips(const grid_t *g, real *vx, real *vz, real *up_x, real *up_z, real *dn_x, real *dn_z,
@@ -499,8 +505,12 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
         F_(MU)[i] = r * q * q;
     }
 
-    int *rix = (int *)malloc(sizeof(int) * (ntr > 0 ? ntr : 1));
-    for (int tr = 0; tr < ntr; tr++) rix[tr] = receiver_ix(s.stage, pml, io->gc[tr], s.ngx_left, s.dx);
+    int *rix = (int *)malloc(sizeof(int) * 2 * (ntr > 0 ? ntr : 1));
+    int *iix = rix + (ntr > 0 ? ntr : 1);
+    for (int tr = 0; tr < ntr; tr++) {
+        rix[tr] = receiver_ix(s.stage, pml, io->gc[tr], s.ngx_left, s.dx);
+        iix[tr] = injection_ix(pml, io->gc[tr], s.ngx_left, s.dx);
+    }
     const int isx = s.isx, isz = s.isz, igz = s.igz;
     const int born_lo = s.stage == 2 ? g->nop : pml;
     const int adj_dir = s.stage == 1 ? 1 : -1;
@@ -620,7 +630,8 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
                  F_(DZ_), -1);
         /* elastic_rotation_addS_bac: assign (stack=false), FD2DGPU.cu:3425-3441 */
         for (int tr = 0; tr < ntr; tr++) {
-            size_t c = IDX(rix[tr], igz);
+            if (iix[tr] < 0 || iix[tr] >= g->nxpml) continue; /* outside the grid: nothing to inject */
+            size_t c = IDX(iix[tr], igz);
             F_(AVZ)[c] = res_z[(size_t)tr * nt + it];
             F_(AVX)[c] = res_x[(size_t)tr * nt + it];
         }

@@ -156,6 +156,11 @@ int receiver_ix(int stage, int pml, int gc, int ngx_left, float dx) {
     return pml + (int)((float)(gc - ngx_left) / dx);
 }
 
+// column where a trace's residual is injected, GPUapplysource_backward_from_record
+// (sfwi-stage1/FD2DGPU.cu:3425-3441, sfwi-stage2/FD2DGPU.cu:3357-3370): dx is a
+// float in both stages, so in stage 2 it can differ from the recording column
+int injection_ix(int pml, int gc, int ngx_left, float dx) { return pml + (int)((float)(gc - ngx_left) / dx); }
+
 bool box_hits(int bx0, int bx1, int bz0, int bz1, int x0, int x1, int z0, int z1) {
     return bx0 < x1 && x0 < bx1 && bz0 < z1 && z0 < bz1;
 }
@@ -243,18 +248,19 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
         g.model = in.model;
         // receiver rows: the record of a trace is its cell (rix, igz), which
         // stays zero outside the update region [NOP, n-NOP); the residual
-        // injected at a cell is the highest-index trace recorded there
-        std::vector<int> rix(in.ntr);
+        // injected at a cell (iix, igz) is the highest-index trace injected there
+        std::vector<int> rix(in.ntr), iix(in.ntr);
         b.rtr.resize((size_t)row + nxpml, -1);
         const bool igz_live = in.igz >= NOP && in.igz < nzpml - NOP;
         for (int t = 0; t < in.ntr; t++) {
             rix[t] = receiver_ix(h->stage, pml, in.gc[t], in.ngx_left, h->dx);
-            if (rix[t] < 0 || rix[t] >= nxpml)
-                return fail(SFWI_E_ARG, "shot %d trace %d: receiver column %d outside the %d-wide grid", s, t, rix[t],
-                            nxpml);
+            iix[t] = injection_ix(pml, in.gc[t], in.ngx_left, h->dx);
+            if (rix[t] < 0 || rix[t] >= nxpml || iix[t] < 0 || iix[t] >= nxpml)
+                return fail(SFWI_E_ARG, "shot %d trace %d: receiver column %d (%d) outside the %d-wide grid", s, t,
+                            rix[t], iix[t], nxpml);
             const bool live = igz_live && rix[t] >= NOP && rix[t] < nxpml - NOP;
             b.trow.push_back(live ? row + rix[t] : -1);
-            b.rtr[(size_t)row + rix[t]] = std::max(b.rtr[(size_t)row + rix[t]], tr0 + t);
+            b.rtr[(size_t)row + iix[t]] = std::max(b.rtr[(size_t)row + iix[t]], tr0 + t);
         }
         // tiles over the update region [NOP, n-NOP)
         for (int x0 = NOP; x0 < nxpml - NOP; x0 += TX)
@@ -273,7 +279,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
                     f |= TILE_STRIP;
                 if (in.igz >= bz0 && in.igz < bz1)
                     for (int t = 0; t < in.ntr; t++)
-                        if (rix[t] >= bx0 && rix[t] < bx1) {
+                        if ((rix[t] >= bx0 && rix[t] < bx1) || (iix[t] >= bx0 && iix[t] < bx1)) {
                             f |= TILE_RECV;
                             break;
                         }

@@ -4,7 +4,7 @@ Run here, where the reference sources are mounted, after
 `python oracle/ref_build.py` has built oracle/_ref (the reference's own
 kernels compiled for the CPU):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 Each case stores its float32 inputs and the reference's outputs (records,
 residuals, misfit, Vp/Vs gradients, illumination).  Observed data are the
@@ -25,17 +25,22 @@ from oracle import pyoracle as po  # noqa: E402
 from sfwi_gb300 import synth  # noqa: E402
 
 CASES = {
-    # name: (stage, allnx, allnz, pml, nt, f0, window (g0, g1) in nodes or None, source node)
+    # name: (stage, allnx, allnz, pml, nt, f0, window (g0, g1) in nodes or None, source node[, dx])
     "s1_full": (1, 48, 32, 10, 300, 25.0, None, 21),
     "s1_window": (1, 56, 28, 8, 260, 25.0, (10, 45), 30),
     "s2_full": (2, 48, 32, 10, 300, 25.0, None, 21),
     "s2_window": (2, 56, 28, 8, 260, 25.0, (6, 41), 20),
+    # 12.5 m spacing: receiver coordinates in whole metres, and stage 2 divides
+    # them by (int)dx = 12 (sfwi-stage2/FD2DGPU.cu:3109), stage 1 by 12.5
+    "s1_dx12p5": (1, 60, 30, 8, 240, 20.0, (4, 52), 27, 12.5),
+    "s2_dx12p5": (2, 60, 30, 8, 240, 20.0, (4, 52), 27, 12.5),
 }
 
 
 def make_case(name):
-    stage, allnx, allnz, pml, nt, f0, win, sxn = CASES[name]
-    dx, dt = 10.0, 1e-3
+    stage, allnx, allnz, pml, nt, f0, win, sxn = CASES[name][:8]
+    dx = CASES[name][8] if len(CASES[name]) > 8 else 10.0
+    dt = 1e-3
     vp, vs, rho = synth.layered_model(allnx, allnz, dx, vmin=1800, vmax=3000)
     vp0 = synth.smooth_z(vp, 4)
     vs0 = (vp0 / 1.73).astype(np.float32)
@@ -84,6 +89,6 @@ def load_case(name):
 if __name__ == "__main__":
     if not po.available("ref1"):
         sys.exit("oracle/_ref not built: run python oracle/ref_build.py first")
-    for n in CASES:
+    for n in sys.argv[1:] or CASES:
         make_case(n)
         print("wrote", n)

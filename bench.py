@@ -35,8 +35,17 @@ if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
 
 import numpy as np  # noqa: E402
 
-WORKLOAD = dict(name="fwi-iteration-376x201-38shots-born-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
-                dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0)
+WORKLOADS = {
+    # one FWI iteration at 376x201 (the headline line)
+    "fwi376": dict(name="fwi-iteration-376x201-38shots-born-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
+                   dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0, model="layered", aperture=None, misfit="OT"),
+    # stage-2 batch at 401x301, 12.5 m: salt body, 80 shots with seeded
+    # window widths of 150-401 nodes
+    "salt401": dict(name="stage2-salt-401x301-80shots-uneven-apertures", allnx=401, allnz=301, dx=12.5, pml=20,
+                    nt=4000, dt=1e-3, f0=15.0, nshots=80, spacing=5, sy=2, gy=0, model="salt", aperture=(150, 401),
+                    misfit="L2"),
+}
+WORKLOAD = WORKLOADS["fwi376"]
 METRIC = "shot-gradients/s"
 
 # algorithmic bytes per padded cell per time step of each kernel (FP32; each
@@ -65,11 +74,14 @@ def dist_info():
 
 def build_workload(w):
     from sfwi_gb300 import synth
-    vp, vs, rho = synth.layered_model(w["allnx"], w["allnz"], w["dx"])
+    if w.get("model") == "salt":
+        vp, vs, rho = synth.salt_model(w["allnx"], w["allnz"], w["dx"])
+    else:
+        vp, vs, rho = synth.layered_model(w["allnx"], w["allnz"], w["dx"])
     vp0 = synth.smooth_z(vp, 10)
     vs0 = (vp0 / 1.73).astype(np.float32)
     rho0 = (310.0 * vp0.astype(np.float64) ** 0.25).astype(np.float32)
-    shots = synth.config_shots(w["allnx"], w["dx"], w["pml"], w["nshots"], w["spacing"])
+    shots = synth.config_shots(w["allnx"], w["dx"], w["pml"], w["nshots"], w["spacing"], aperture=w.get("aperture"))
     sou = ricker(w["nt"], w["dt"], w["f0"])
     return dict(vp=vp, vs=vs, rho=rho, vp0=vp0, vs0=vs0, rho0=rho0, dvp=(vp - vp0).astype(np.float32),
                 dvs=(vs - vs0).astype(np.float32), shots=shots, sou=sou)
@@ -77,12 +89,8 @@ def build_workload(w):
 
 def ricker(nt, dt, fm):
     """Ricker wavelet as the reference computes it (sfwi-stage1/main.cpp:251-260)."""
-    PI = np.float32(3.14159265358979)
-    fm, dt = np.float32(fm), np.float32(dt)
-    Nk = np.float32(PI * PI * fm * fm * dt * dt)
-    t0 = int(np.ceil(1.0 / float(np.float32(fm * dt))))
-    t = np.arange(nt, dtype=np.float64) - t0
-    return ((1.0 - 2.0 * float(Nk) * t * t) * np.exp(-float(Nk) * t * t)).astype(np.float32)
+    from sfwi_gb300 import synth
+    return synth.ricker(nt, dt, fm)
 
 
 class Clocks:
@@ -173,6 +181,25 @@ def cpu_baseline_sample(w, data, nthreads, nt_sample, kind="port"):
     return 1.0 / per_shot, el
 
 
+def run_serving(n, budget_gb=64.0, slots=4):
+    """Serving loop on a seeded Poisson stream (50 requests/s; grids, nt and
+    shots drawn from the serving configuration's ranges, then scaled by 0.3 in
+    each grid dimension and 0.1 in nt so the stream is served in seconds):
+    continuous admission against an HBM budget vs the plain FIFO loop."""
+    from sfwi_gb300 import serve
+    reqs = serve.poisson_requests(n, 50.0, seed=4, grid_scale=0.3, nt_scale=0.1)
+    serve.run_request(reqs[0])  # warm the kernels and the allocator
+    out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
+           "scale": "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
+    for name, srv in (("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
+                      ("fifo", serve.Server(budget_gb * 2 ** 30, max_active=1))):
+        res = srv.run(reqs)
+        st = serve.latency_stats(res)
+        st["shot_gradients_per_s"] = sum(r.shot_gradients for r in reqs) / st["span_s"]
+        out[name] = {k: round(v, 3) if isinstance(v, float) else v for k, v in st.items()}
+    return out
+
+
 def run_reference_arm(args, w):
     ws, rank = dist_info()
     if rank != 0:
@@ -214,13 +241,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fwi376", choices=sorted(WORKLOADS))
     ap.add_argument("--nt", type=int, default=None, help="override the number of time steps (testing)")
     ap.add_argument("--shots", type=int, default=None, help="override the number of shots (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=4, help="shots timed one at a time for the plain form")
+    ap.add_argument("--serving-requests", type=int, default=24, help="requests of the serving-loop measurement")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     args = ap.parse_args()
-    w = dict(WORKLOAD)
+    w = dict(WORKLOADS[args.workload])
     if args.nt:
         w["nt"] = args.nt
     if args.shots:
@@ -263,7 +292,8 @@ def main():
                             4, shots[0]["ntr"], stage=2)
     fd.GPUbufferVPVS(data["vp0"], data["vs0"])
     fd.GPUbufferM(data["dvp"], data["dvs"])
-    fd.set_misfit(sg.MISFIT_OT)
+    if w["misfit"] == "OT":
+        fd.set_misfit(sg.MISFIT_OT)
 
     def step():
         for d, (pz, px) in zip(shots, obs):
@@ -353,19 +383,20 @@ def main():
     for pz, px in obs:
         pz.free()
         px.free()
+    serving = run_serving(args.serving_requests) if args.serving_requests > 0 and rank == 0 else None
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": round(value, 3), "unit": "shot-gradients/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
-                       "nt": nt, "misfit": "OT", "born": True, "parallelism": "shots-per-gpu",
+                       "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"], "parallelism": "shots-per-gpu",
                        "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),
                        "alg_bytes_per_step_GB": round(alg_bytes_step / 1e9, 2),
                        "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving,
             "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2)}}
     print(json.dumps(line), flush=True)
     return 0

@@ -60,9 +60,11 @@ typedef struct {
 
 /* Ricker wavelet, sfwi-stage1/main.cpp:251-260 */
 void FN(ricker)(float *w, int nt, float dt, float fm) {
-    const float PI_ = 3.14159265358979f;
-    float Nk = PI_ * PI_ * fm * fm * dt * dt;
-    int t0 = (int)ceil(1.0 / (fm * dt));
+    /* ricker_wave, sfwi-stage1/main.cpp:251-260: PI is a double literal
+     * (main.cpp:8), Nk is stored as float, the exponent is a float product */
+    const double PI_ = 3.14159265358979;
+    const float Nk = (float)(PI_ * PI_ * fm * fm * dt * dt);
+    const int t0 = (int)ceil(1.0 / (fm * dt));
     for (int t = 0; t < nt; t++)
         w[t] = (float)((1.0 - 2.0 * Nk * (t - t0) * (t - t0)) * exp(-Nk * (t - t0) * (t - t0)));
 }

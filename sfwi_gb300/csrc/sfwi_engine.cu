@@ -46,21 +46,34 @@ int fail(int code, const char *fmt, ...) {
                         #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
     } while (0)
 
+// Device buffer that grows on demand.  With a stream attached, allocation
+// and release are stream-ordered (cudaMallocAsync / cudaFreeAsync on the
+// owning handle's stream), so a handle that grows or frees its buffers never
+// waits for work other handles have in flight on the same device.
 template <class T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t st = nullptr;
     cudaError_t ensure(size_t m) {
         if (m <= n && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(m, 1) * sizeof(T));
-        if (e == cudaSuccess) n = m;
+        release();
+        const size_t bytes = std::max<size_t>(m, 1) * sizeof(T);
+        cudaError_t e = st ? cudaMallocAsync(reinterpret_cast<void **>(&p), bytes, st)
+                           : cudaMalloc(reinterpret_cast<void **>(&p), bytes);
+        if (e == cudaSuccess)
+            n = m;
+        else
+            p = nullptr;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (st)
+                cudaFreeAsync(p, st);
+            else
+                cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }
@@ -668,6 +681,16 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     return collect_misfit(h, misfit_kind, misfit, per_shot, true);
 }
 
+// every device buffer of a handle
+template <class F>
+void for_each_buf(sfwi_handle *h, F f) {
+    Batch &b = h->b;
+    f(b.grid), f(b.tb), f(b.lr), f(b.rrow), f(b.rsrc), f(b.recs), f(b.tmis), f(b.dsigma), f(b.dgeo), f(b.dtiles);
+    f(b.dtrow), f(b.drtr), f(b.derr), f(b.dctr);
+    f(h->sou), f(h->vp_all), f(h->vs_all), f(h->rho_all), f(h->dvp_all), f(h->dvs_all);
+    f(h->gpp), f(h->gps), f(h->gil), f(h->grh), f(h->ls_buf);
+}
+
 int check(sfwi_handle *h) {
     if (!h) return fail(SFWI_E_ARG, "null handle");
     return SFWI_OK;
@@ -801,16 +824,17 @@ int ensure_grads(sfwi_handle *h) {
     CK(h->gps.ensure(n));
     CK(h->gil.ensure(n));
     CK(h->grh.ensure(n));
-    CK(cudaMemset(h->gpp.p, 0, n * sizeof(double)));
-    CK(cudaMemset(h->gps.p, 0, n * sizeof(double)));
-    CK(cudaMemset(h->gil.p, 0, n * sizeof(double)));
-    CK(cudaMemset(h->grh.p, 0, n * sizeof(double)));
+    CK(cudaMemsetAsync(h->gpp.p, 0, n * sizeof(double), h->st));
+    CK(cudaMemsetAsync(h->gps.p, 0, n * sizeof(double), h->st));
+    CK(cudaMemsetAsync(h->gil.p, 0, n * sizeof(double), h->st));
+    CK(cudaMemsetAsync(h->grh.p, 0, n * sizeof(double), h->st));
     return SFWI_OK;
 }
 
 int upload_model(DevBuf<float> &d, const float *src, size_t n) {
     CK(d.ensure(n));
-    CK(cudaMemcpy(d.p, src, n * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(d.p, src, n * sizeof(float), cudaMemcpyHostToDevice, d.st));
+    CK(cudaStreamSynchronize(d.st));
     return SFWI_OK;
 }
 
@@ -940,6 +964,7 @@ int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float 
             rc = fail(SFWI_E_CUDA, "stream: %s", cudaGetErrorString(e));
             break;
         }
+        for_each_buf(h, [h](auto &d) { d.st = h->st; });
         for (auto &ev : h->ev)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
                 rc = fail(SFWI_E_CUDA, "event: %s", cudaGetErrorString(e));
@@ -962,26 +987,8 @@ int sfwi_destroy(sfwi_handle *h) {
     cudaSetDevice(h->device);
     if (h->st) cudaStreamSynchronize(h->st);
     h->b.drop_graphs();
-    h->b.grid.release();
-    h->b.tb.release();
-    h->b.lr.release();
-    h->b.rrow.release();
-    h->b.rsrc.release();
-    h->b.recs.release();
-    h->b.tmis.release();
-    h->b.dsigma.release();
-    h->b.dgeo.release();
-    h->b.dtiles.release();
-    h->b.dtrow.release();
-    h->b.drtr.release();
-    h->b.derr.release();
-    h->b.dctr.release();
-    for (auto *d : {&h->sou, &h->vp_all, &h->vs_all, &h->rho_all, &h->dvp_all, &h->dvs_all}) d->release();
-    h->gpp.release();
-    h->gps.release();
-    h->gil.release();
-    h->grh.release();
-    h->ls_buf.release();
+    for_each_buf(h, [](auto &d) { d.release(); });
+    if (h->st) cudaStreamSynchronize(h->st);  // the stream-ordered frees
     for (auto &ev : h->ev)
         if (ev) cudaEventDestroy(ev);
     if (h->st) cudaStreamDestroy(h->st);
@@ -1073,7 +1080,8 @@ int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho) {
     CK(cudaSetDevice(h->device));
     CK(cudaStreamSynchronize(h->st));
     if (int rc = ensure_grads(h)) return rc;
-    CK(cudaMemcpy(grad_rho, h->grh.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(grad_rho, h->grh.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return SFWI_OK;
 }
 
@@ -1099,12 +1107,14 @@ int sfwi_imagebuffer_resettozero(sfwi_handle *h, float *grad_pp, float *grad_ps,
     DevBuf<double> *src[3] = {&h->gpp, &h->gps, &h->gil};
     for (int k = 0; k < 3; k++) {
         if (outs[k]) {
-            CK(cudaMemcpy(tmp.data(), src[k]->p, n * sizeof(double), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(tmp.data(), src[k]->p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
             for (size_t i = 0; i < n; i++) outs[k][i] = (float)tmp[i];
         }
-        CK(cudaMemset(src[k]->p, 0, n * sizeof(double)));
+        CK(cudaMemsetAsync(src[k]->p, 0, n * sizeof(double), h->st));
     }
-    if (h->grh.p) CK(cudaMemset(h->grh.p, 0, n * sizeof(double)));
+    if (h->grh.p) CK(cudaMemsetAsync(h->grh.p, 0, n * sizeof(double), h->st));
+    CK(cudaStreamSynchronize(h->st));
     for (float *bb : {b1, b2, b3, b4})
         if (bb) std::memset(bb, 0, n * sizeof(float));
     return SFWI_OK;
@@ -1115,9 +1125,10 @@ int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, do
     const size_t n = (size_t)h->allnx * h->allnz;
     CK(cudaSetDevice(h->device));
     CK(cudaStreamSynchronize(h->st));
-    if (grad_pp) CK(cudaMemcpy(grad_pp, h->gpp.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-    if (grad_ps) CK(cudaMemcpy(grad_ps, h->gps.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-    if (illum) CK(cudaMemcpy(illum, h->gil.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad_pp) CK(cudaMemcpyAsync(grad_pp, h->gpp.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    if (grad_ps) CK(cudaMemcpyAsync(grad_ps, h->gps.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    if (illum) CK(cudaMemcpyAsync(illum, h->gil.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return SFWI_OK;
 }
 
@@ -1136,7 +1147,9 @@ int sfwi_read_records(sfwi_handle *h, int i, float *syn_z, float *syn_x, float *
     } items[6] = {{syn_z, R_SYN_Z}, {syn_x, R_SYN_X}, {syn2_z, R_SYN2_Z}, {syn2_x, R_SYN2_X}, {res_z, R_RES_Z},
                   {res_x, R_RES_X}};
     for (auto &it : items)
-        if (it.dst && n) CK(cudaMemcpy(it.dst, b.r(it.k, nt) + off, n * sizeof(float), cudaMemcpyDeviceToHost));
+        if (it.dst && n)
+            CK(cudaMemcpyAsync(it.dst, b.r(it.k, nt) + off, n * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return SFWI_OK;
 }
 

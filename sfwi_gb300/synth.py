@@ -68,6 +68,21 @@ def salt_model(allnx, allnz, dx, vmin=1500.0, vmax=3500.0, vsalt=4500.0, seed=SE
     return vp, vs, rho
 
 
+def ricker(nt, dt, fm):
+    """Ricker wavelet as the reference computes it (sfwi-stage1/main.cpp:251-260):
+    Nk = pi^2 f^2 dt^2 formed in double and stored as float, t0 = ceil(1/(f dt)),
+    w = (1 - 2 Nk t^2) exp(-Nk t^2) with the exponent a float product."""
+    PI = 3.14159265358979
+    fm, dt = np.float32(fm), np.float32(dt)
+    Nk = np.float32(PI * PI * float(fm) * float(fm) * float(dt) * float(dt))
+    t0 = int(math.ceil(1.0 / float(np.float32(fm * dt))))
+    t = np.arange(nt, dtype=np.int64) - t0
+    a = 1.0 - 2.0 * float(Nk) * t * t
+    tf = t.astype(np.float32)
+    e = (-Nk * tf) * tf
+    return (a * np.exp(e.astype(np.float64))).astype(np.float32)
+
+
 def smooth_z(a, half_width):
     """Box-smooth a model along z (the starting model of an inversion)."""
     if half_width <= 0:

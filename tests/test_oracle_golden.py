@@ -50,3 +50,11 @@ def test_receiver_and_source_indices():
     d = synth.shot_descriptor(1000, [600, 610, 1200], 10.0, pml=20, all_left=0, sy=2, gy=0)
     assert d["ngx_left"] == 600 and d["nx"] == 61 and d["isx"] == 20 + 40 and d["isz"] == 22 and d["igz"] == 20
     assert d["delta_left"] == 60
+
+
+def test_ricker_restatements_agree():
+    """The package's wavelet (used by the benchmarks and the serving loop) and
+    the oracle's both restate ricker_wave (sfwi-stage1/main.cpp:251-260)."""
+    from sfwi_gb300 import synth
+    for nt, dt, f in ((3000, 1e-3, 15.0), (6000, 5e-4, 25.0), (257, 1e-3, 20.0)):
+        assert np.array_equal(synth.ricker(nt, dt, f), po.ricker(nt, dt, f))

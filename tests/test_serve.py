@@ -1,0 +1,91 @@
+"""The serving loop (sfwi_gb300/serve.py): admission against the HBM budget,
+FIFO order for the one-job loop, latency statistics (host logic, stand-in
+runner), and on the GPU the same result for a request alone and in the mix."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from sfwi_gb300 import serve
+
+
+def _fake_requests(sizes, arrivals):
+    out = []
+    for rid, (size, t) in enumerate(zip(sizes, arrivals)):
+        r = serve.Request(rid, t, 0, 0, 10.0, 1e-3, 0, 0, None, None, None, None, [dict(gc=[0])])
+        r.size = size
+        out.append(r)
+    return out
+
+
+class Recorder:
+    """Runner that sleeps and records what ran concurrently."""
+
+    def __init__(self, dur=0.05):
+        self.lock = threading.Lock()
+        self.active, self.bytes, self.max_active, self.max_bytes = 0, 0, 0, 0
+        self.order = []
+        self.dur = dur
+
+    def __call__(self, r):
+        with self.lock:
+            self.active += 1
+            self.bytes += r.size
+            self.max_active = max(self.max_active, self.active)
+            self.max_bytes = max(self.max_bytes, self.bytes)
+            self.order.append(r.rid)
+        time.sleep(self.dur)
+        with self.lock:
+            self.active -= 1
+            self.bytes -= r.size
+        z = np.zeros((1, 1))
+        return (float(r.rid), z, z, z)
+
+
+def test_admission_respects_budget_and_slots():
+    reqs = _fake_requests([40, 30, 50, 20, 60, 10], [0.0, 0.0, 0.01, 0.01, 0.02, 0.02])
+    rec = Recorder()
+    res = serve.Server(100, max_active=3, runner=rec, sizer=lambda r: r.size).run(reqs)
+    assert [r.rid for r in res] == list(range(6))
+    assert rec.max_bytes <= 100 and rec.max_active <= 3
+    assert rec.max_active >= 2  # work overlapped
+    assert all(r.done >= r.admitted >= r.arrival - 1e-9 for r in res)
+
+
+def test_fifo_runs_one_job_at_a_time_in_arrival_order():
+    reqs = _fake_requests([40, 30, 50, 20], [0.03, 0.0, 0.02, 0.01])
+    rec = Recorder(0.02)
+    serve.Server(100, max_active=1, runner=rec, sizer=lambda r: r.size).run(reqs)
+    assert rec.max_active == 1
+    assert rec.order == [1, 3, 2, 0]
+
+
+def test_oversized_request_is_refused():
+    reqs = _fake_requests([200], [0.0])
+    with pytest.raises(ValueError):
+        serve.Server(100, runner=Recorder(), sizer=lambda r: r.size).run(reqs)
+
+
+def test_latency_stats():
+    z = np.zeros(1)
+    res = [serve.Result(i, 0.0, z, z, z, 0.0, 0.0, 0.1 * (i + 1)) for i in range(100)]
+    st = serve.latency_stats(res)
+    assert st["p50_ms"] == pytest.approx(5050.0) and st["p99_ms"] == pytest.approx(9901.0)
+
+
+def test_request_bytes_grows_with_the_request():
+    a, b = serve.poisson_requests(2, 10.0, grid=((60, 30), (60, 30)), nt=(100, 100), shots=(1, 1))
+    b.shots = b.shots + b.shots
+    assert serve.request_bytes(b) > serve.request_bytes(a) > 0
+
+
+@pytest.mark.gpu
+def test_request_gives_the_same_result_alone_and_in_the_mix():
+    reqs = serve.poisson_requests(4, 1000.0, seed=7, grid=((64, 32), (110, 48)), nt=(180, 260), shots=(1, 3))
+    alone = [serve.run_request(r) for r in reqs]
+    res = serve.Server(8 << 30, max_active=4).run(reqs)
+    for a, r in zip(alone, res):
+        assert a[0] == r.misfit
+        for x, y in zip(a[1:], (r.grad_pp, r.grad_ps, r.illum)):
+            assert np.array_equal(x, y)

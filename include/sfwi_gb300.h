@@ -98,6 +98,22 @@ int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, do
  * [allnx][allnz] buffer.  sfwi_read_density_gradient_f64 copies it out (no
  * reset); sfwi_imagebuffer_resettozero zeroes it with the others. */
 int sfwi_set_density_gradient(sfwi_handle *h, int on);
+
+/* Snapshot imaging.  No reference counterpart: the reference reconstructs
+ * the forward wavefield backwards in time from saved edge strips.  With
+ * every = k > 0, later gradient runs instead keep the background vx, vz after
+ * every k-th forward step (format SFWI_SNAP_F32, or SFWI_SNAP_F16 /
+ * SFWI_SNAP_BF16 as 16-bit values scaled by the snapshot's max |v| over the
+ * shot) and the backward pass runs the adjoint only, imaging at the snapshot
+ * steps with weight k (strains of the snapshot by the reconstruction's
+ * stencils; illumination k |v|^2).  every = 0 restores the reconstruction.
+ * Device memory: ceil(nt/k) x 2 x packed cells x 4 (FP32) or 2 bytes, in
+ * place of the edge strips; at most 512 shots per run; excludes the density
+ * kernel. */
+#define SFWI_SNAP_F32 1
+#define SFWI_SNAP_F16 2
+#define SFWI_SNAP_BF16 3
+int sfwi_set_snapshots(sfwi_handle *h, int every, int format);
 int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho);
 
 /* Records of the last shot-gradient call(s): forward records (stage 1:

@@ -22,7 +22,12 @@
  *     adjoint source (orc*_ot_trace below);
  *   - grad_rho: a density kernel -sum_t v_adj . dv/dt, with dv the velocity
  *     step of the reconstruction (the reference computes no density
- *     gradient).
+ *     gradient);
+ *   - snap_every = k > 0: no reconstruction and no edge strips; the forward
+ *     vx, vz are kept (exactly) after every k-th step, and the backward pass
+ *     images at those steps only, with strains taken from the kept velocities
+ *     by the reconstruction's own stencils (update_s) and weight k; the
+ *     illumination is k * |v|^2 of the kept velocities.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -174,6 +179,28 @@ static void update_s(const grid_t *g, real *txx, real *tzz, real *txx_x, real *t
                 vx_gz[i] = c / dz;
                 vz_gx[i] = d / dx;
             }
+        }
+}
+
+/* the strains update_s forms (vx_x, vz_z, vx_z, vz_x), from given velocities */
+static void strains(const grid_t *g, const real *vx, const real *vz, real *gxx, real *gzz, real *gxz, real *gzx) {
+    const int nop = g->nop, nz = g->nzpml;
+    const real dx = g->dx, dz = g->dz;
+    OMP_FOR
+    for (int ix = nop; ix < g->nxpml - nop; ix++)
+        for (int iz = nop; iz < g->nzpml - nop; iz++) {
+            size_t i = (size_t)ix * nz + iz;
+            real a = 0, b = 0, c = 0, d = 0;
+            for (int k = 1; k <= nop; k++) {
+                a += C8[k] * (vx[(size_t)(ix + k - 1) * nz + iz] - vx[(size_t)(ix - k) * nz + iz]);
+                b += C8[k] * (vz[(size_t)ix * nz + iz + k - 1] - vz[(size_t)ix * nz + iz - k]);
+                c += C8[k] * (vx[(size_t)ix * nz + iz + k] - vx[(size_t)ix * nz + iz - k + 1]);
+                d += C8[k] * (vz[(size_t)(ix + k) * nz + iz] - vz[(size_t)(ix - k + 1) * nz + iz]);
+            }
+            gxx[i] = a / dx;
+            gzz[i] = b / dz;
+            gxz[i] = c / dz;
+            gzx[i] = d / dx;
         }
 }
 
@@ -478,11 +505,15 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
 #define F_(k) (mem + (size_t)(k) * nD)
     real *rec = (real *)calloc(nrec * 4, sizeof(real));
     const size_t nud = (size_t)2 * g->nop * g->nx * nt, nlr = (size_t)2 * g->nz * g->nop * nt;
-    real *strips = s.forward_only ? NULL : (real *)calloc(4 * nud + 4 * nlr, sizeof(real));
-    if (!rec || (!s.forward_only && !strips)) {
+    const int snap = s.snap_every > 0 && !s.forward_only;
+    const int nsnap = snap ? (nt + s.snap_every - 1) / s.snap_every : 0;
+    real *strips = s.forward_only || snap ? NULL : (real *)calloc(4 * nud + 4 * nlr, sizeof(real));
+    real *snaps = snap ? (real *)malloc(sizeof(real) * 2 * nD * (size_t)nsnap) : NULL;
+    if (!rec || (!s.forward_only && !snap && !strips) || (snap && !snaps)) {
         free(mem);
         free(rec);
         free(strips);
+        free(snaps);
         return -3;
     }
     real *syn_z = rec, *syn_x = rec + nrec, *syn2_z = rec + 2 * nrec, *syn2_x = rec + 3 * nrec;
@@ -552,8 +583,14 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
                 syn_x[(size_t)tr * nt + it] = F_(VX)[c];
             }
         }
-        if (!s.forward_only)
+        if (snap) {
+            if (it % s.snap_every == 0) {
+                memcpy(snaps + (size_t)(it / s.snap_every) * 2 * nD, F_(VX), nD * sizeof(real));
+                memcpy(snaps + (size_t)(it / s.snap_every) * 2 * nD + nD, F_(VZ), nD * sizeof(real));
+            }
+        } else if (!s.forward_only) {
             edge_strips(g, F_(VX), F_(VZ), up_x, up_z, dn_x, dn_z, lf_x, lf_z, rt_x, rt_z, it, 1);
+        }
     }
     for (size_t i = 0; i < nrec; i++) {
         if (io->syn_z) io->syn_z[i] = syn_z[i];
@@ -565,6 +602,7 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
         free(mem);
         free(rec);
         free(strips);
+        free(snaps);
         free(rix);
         return 0;
     }
@@ -620,16 +658,29 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
          * taken before the edge strips are restored into the totals (the
          * restore is not part of the step: update_v rebuilds the totals from
          * the split parts) */
-        if (io->grad_rho) {
+        if (io->grad_rho && !snap) {
             memcpy(F_(VPREV_X), F_(VX), nD * sizeof(real));
             memcpy(F_(VPREV_Z), F_(VZ), nD * sizeof(real));
         }
-        edge_strips(g, F_(VX), F_(VZ), up_x, up_z, dn_x, dn_z, lf_x, lf_z, rt_x, rt_z, it, 0);
-        /* born_modeling(-1, 6): reconstruct sigma (with strains) then v */
-        update_s(g, F_(TXX), F_(TZZ), F_(TXXX), F_(TXXZ), F_(TZZX), F_(TZZZ), F_(TXZ), F_(TXZX), F_(TXZZ), F_(VX),
-                 F_(VZ), F_(LAM), F_(MU), F_(DX_), F_(DZ_), -1, F_(GXX), F_(GZZ), F_(GXZ), F_(GZX));
-        update_v(g, F_(TXX), F_(TZZ), F_(TXZ), F_(VX), F_(VXX), F_(VXZ), F_(VZ), F_(VZX), F_(VZZ), F_(RHO), F_(DX_),
-                 F_(DZ_), -1);
+        real w = 1; /* imaging weight of this step */
+        if (snap) {
+            if (it % s.snap_every == 0) {
+                const real *sv = snaps + (size_t)(it / s.snap_every) * 2 * nD;
+                memcpy(F_(VX), sv, nD * sizeof(real));
+                memcpy(F_(VZ), sv + nD, nD * sizeof(real));
+                strains(g, F_(VX), F_(VZ), F_(GXX), F_(GZZ), F_(GXZ), F_(GZX));
+                w = (real)s.snap_every;
+            } else {
+                w = 0;
+            }
+        } else {
+            edge_strips(g, F_(VX), F_(VZ), up_x, up_z, dn_x, dn_z, lf_x, lf_z, rt_x, rt_z, it, 0);
+            /* born_modeling(-1, 6): reconstruct sigma (with strains) then v */
+            update_s(g, F_(TXX), F_(TZZ), F_(TXXX), F_(TXXZ), F_(TZZX), F_(TZZZ), F_(TXZ), F_(TXZX), F_(TXZZ), F_(VX),
+                     F_(VZ), F_(LAM), F_(MU), F_(DX_), F_(DZ_), -1, F_(GXX), F_(GZZ), F_(GXZ), F_(GZX));
+            update_v(g, F_(TXX), F_(TZZ), F_(TXZ), F_(VX), F_(VXX), F_(VXZ), F_(VZ), F_(VZX), F_(VZZ), F_(RHO),
+                     F_(DX_), F_(DZ_), -1);
+        }
         /* elastic_rotation_addS_bac: assign (stack=false), FD2DGPU.cu:3425-3441 */
         for (int tr = 0; tr < ntr; tr++) {
             if (iix[tr] < 0 || iix[tr] >= g->nxpml) continue; /* outside the grid: nothing to inject */
@@ -643,6 +694,7 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
         back_v(g, F_(ATXX), F_(ATZZ), F_(ATXZ), F_(AVX), F_(AVXX), F_(AVXZ), F_(AVZ), F_(AVZX), F_(AVZZ), F_(LAM),
                F_(MU), F_(RHO), F_(DX_), F_(DZ_), adj_dir);
         /* image_gradient: doimage_gradient + doimage_illum, FD2DGPU.cu:3324-3382 */
+        if (w != 0)
         for (int ix = 0; ix < nx; ix++)
             for (int iz = 0; iz < nz; iz++) {
                 size_t c = IDX(ix + pml, iz + pml);
@@ -652,10 +704,10 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
                           (F_(GXZ)[c] + F_(GZX)[c]) * F_(ATXZ)[c];
                 real cpp = 2 * F_(VP)[c] * F_(RHO)[c] * lg;
                 real cps = -4 * F_(VS)[c] * F_(RHO)[c] * lg + 2 * F_(VS)[c] * F_(RHO)[c] * mg;
-                gpp[o] += cpp;
-                gps[o] += cps;
-                gil[o] += F_(VX)[c] * F_(VX)[c] + F_(VZ)[c] * F_(VZ)[c];
-                if (io->grad_rho) {
+                gpp[o] += w * cpp;
+                gps[o] += w * cps;
+                gil[o] += w * (F_(VX)[c] * F_(VX)[c] + F_(VZ)[c] * F_(VZ)[c]);
+                if (io->grad_rho && !snap) {
                     /* v_adj . dv/dt with the reconstructed step v(it) -> v(it-1) */
                     real dvx = (F_(VPREV_X)[c] - F_(VX)[c]) / g->dt, dvz = (F_(VPREV_Z)[c] - F_(VZ)[c]) / g->dt;
                     grh[o] += -(F_(AVX)[c] * dvx + F_(AVZ)[c] * dvz);
@@ -672,6 +724,7 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
     free(mem);
     free(rec);
     free(strips);
+    free(snaps);
     free(rix);
 #undef F_
     return 0;

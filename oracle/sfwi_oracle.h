@@ -34,6 +34,8 @@ typedef struct {
     int forward_only;     /* 1: stop after the forward loop (records only) */
     int misfit_kind;      /* 0: L2 as the reference; 1: 1D optimal transport (oracle only) */
     int nthreads;         /* OpenMP threads for the emulated launches / loops (<=0: all) */
+    int snap_every;       /* oracle only: 0 = reconstruction (as the reference); k > 0 = image
+                             from exact forward snapshots of vx, vz every k-th step, weight k */
 } sfwi_oracle_shot;
 
 typedef struct {

@@ -145,6 +145,12 @@ class FD2DGPU_ELASTIC:
         reference counterpart) in later gradient runs."""
         _lib.check(_lib.load().sfwi_set_density_gradient(self._h, 1 if on else 0))
 
+    def set_snapshots(self, every, fmt="f16"):
+        """Image from forward snapshots every `every` steps ("f32", "f16",
+        "bf16"; every=0: reconstruction, as the reference)."""
+        code = {"f32": SNAP_F32, "f16": SNAP_F16, "bf16": SNAP_BF16}[fmt] if every else 0
+        _lib.check(_lib.load().sfwi_set_snapshots(self._h, int(every), code))
+
     def read_density_gradient_f64(self):
         out = np.zeros((self.allnx, self.allnz), np.float64)
         _lib.check(_lib.load().sfwi_read_density_gradient_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
@@ -280,6 +286,9 @@ def OT_power(obs_x, obs_z, cal_x, cal_z, dt):
 
 def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
     return _ot("sfwi_ot_alltrace", obs_x, obs_z, cal_x, cal_z, dt)
+
+
+SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
 
 
 class PinnedArray:

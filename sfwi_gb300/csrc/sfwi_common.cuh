@@ -38,6 +38,10 @@ enum GridArr {
     NGRID
 };
 
+// snapshot storage formats
+enum SnapFmt : int { SNAP_OFF = 0, SNAP_F32 = 1, SNAP_F16 = 2, SNAP_BF16 = 3 };
+constexpr int SNAP_MAX_SHOTS = 512;  // shots of one batch in snapshot mode (per-shot scales in shared memory)
+
 // per-shot geometry (device-resident table)
 struct ShotGeo {
     int row0;      // first packed row
@@ -95,6 +99,13 @@ struct Params {
     float *tb, *lr;             // edge strips (layout below); null in modelling-only runs
     float *rrow;                // receiver-row records [nt][nrc][X]
     int nrc;                    // record components: vz, vx (+ background vz, vx in stage 2)
+    // forward snapshots (snap_every = k > 0, no reconstruction): the
+    // background vx, vz after every k-th step, [snapshot][vx|vz][X][PS], FP32
+    // or 16-bit values in units of sscale[(shot * nsnap + snapshot) * 2 + comp]
+    // (the snapshot's max |v| over the shot)
+    void *snap;
+    float *sscale;
+    int snap_every, snap_fmt, nsnap, PS;
     int nshots;
     int ntiles;
     int *err;                   // set to a nonzero code when a bounded device wait gives up

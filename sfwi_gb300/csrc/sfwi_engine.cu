@@ -103,6 +103,9 @@ struct Batch {
     DevBuf<float> tb, lr;    // edge strips (sfwi_common.cuh layout)
     DevBuf<float> rrow;      // receiver-row records [nt][nrc][X]
     DevBuf<float> rsrc;      // residual source [X][rsp]
+    DevBuf<float> snap;      // forward snapshots (FP32 or 16-bit elements)
+    DevBuf<float> sscale;    // snapshot scales [shot][snapshot][vx|vz]
+    int nsnap = 0, PS = 0;   // snapshots of a run, their row pitch in elements
     DevBuf<float> recs;      // NREC * ntr_tot * nt
     DevBuf<double> tmis;     // 2 * ntr_tot
     DevBuf<double> dsigma;
@@ -140,6 +143,8 @@ struct sfwi_handle {
     bool have_model = false, have_rho = false, have_m = false;
     DevBuf<double> gpp, gps, gil, grh;
     bool want_rho = false;       // accumulate the density kernel as well
+    int snap_every = 0;          // > 0: image from forward snapshots every k steps (no reconstruction)
+    int snap_fmt = SNAP_OFF;     // storage format of the snapshots
     // one-shot state written by the reference-shaped calls
     int ngx_min = 0;
     std::vector<float> rec_z, rec_x;
@@ -222,6 +227,23 @@ int encode_2d_map(CUtensorMap *m, float *base, unsigned long long inner, unsigne
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled (2-D) failed (%d)", (int)r);
+    return SFWI_OK;
+}
+
+// 3-D map over the snapshots [depth][X][PS] (FP32 or raw 16-bit elements),
+// boxes of BZ x BX x 2 (vx and vz of one snapshot)
+int encode_snap_map(CUtensorMap *m, void *base, int fmt, int PS, int X, int depth) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const size_t es = fmt == SNAP_F32 ? 4 : 2;
+    const cuuint64_t dims[3] = {(cuuint64_t)PS, (cuuint64_t)X, (cuuint64_t)depth};
+    const cuuint64_t strides[2] = {(cuuint64_t)PS * es, (cuuint64_t)PS * X * es};
+    const cuuint32_t box[3] = {(cuuint32_t)BZ, (cuuint32_t)BX, 2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(m, fmt == SNAP_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, base,
+                     dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled (snapshots) failed (%d)", (int)r);
     return SFWI_OK;
 }
 
@@ -363,8 +385,15 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     p.geo = b.dgeo.p;
     p.tiles = b.dtiles.p;
     p.sou = h->sou.p;
-    p.tb = forward_only ? nullptr : b.tb.p;  // modelling only: no strips saved
-    p.lr = forward_only ? nullptr : b.lr.p;
+    const bool snap = !forward_only && h->snap_every > 0;
+    p.tb = forward_only || snap ? nullptr : b.tb.p;  // modelling only / snapshots: no strips
+    p.lr = forward_only || snap ? nullptr : b.lr.p;
+    p.snap = snap ? b.snap.p : nullptr;
+    p.sscale = snap ? b.sscale.p : nullptr;
+    p.snap_every = snap ? h->snap_every : 0;
+    p.snap_fmt = snap ? h->snap_fmt : SNAP_OFF;
+    p.nsnap = snap ? b.nsnap : 0;
+    p.PS = b.PS;
     p.rrow = b.rrow.p;
     p.nrc = h->stage == 2 ? 4 : 2;
     p.nshots = b.nshots;
@@ -379,14 +408,27 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     const int nt = h->nt;
     const size_t recs = (size_t)NREC * std::max(b.ntr_tot, 1) * nt;
     const int nrc = h->stage == 2 ? 4 : 2;
+    const bool snap = !forward_only && h->snap_every > 0;
+    b.PS = (b.P + 7) & ~7;
+    b.nsnap = snap ? (nt + h->snap_every - 1) / h->snap_every : 0;
     // TMA row coordinates of the strip arrays are 32-bit
-    if (!forward_only && ((long long)nt * 4 * b.X >= (1LL << 31) || (long long)nt * 4 * b.nshots * 8 >= (1LL << 31)))
+    if (!forward_only && !snap &&
+        ((long long)nt * 4 * b.X >= (1LL << 31) || (long long)nt * 4 * b.nshots * 8 >= (1LL << 31)))
         return fail(SFWI_E_ARG, "batch too large for one run (nt x packed rows = %lld); split the shots",
                     (long long)nt * b.X);
+    if (snap && b.nshots > SNAP_MAX_SHOTS)
+        return fail(SFWI_E_ARG, "snapshot runs take at most %d shots at a time", SNAP_MAX_SHOTS);
     CK(b.grid.ensure((size_t)NGRID * b.cells));
     if (!forward_only) {
-        CK(b.tb.ensure((size_t)nt * 4 * b.X * 8));
-        CK(b.lr.ensure((size_t)nt * 4 * b.nshots * 8 * b.P));
+        if (snap) {
+            const size_t elems = (size_t)b.nsnap * 2 * b.X * b.PS;
+            CK(b.snap.ensure(h->snap_fmt == SNAP_F32 ? elems : (elems + 1) / 2));
+            CK(b.sscale.ensure((size_t)b.nshots * b.nsnap * 2));
+            CK(cudaMemsetAsync(b.sscale.p, 0, (size_t)b.nshots * b.nsnap * 2 * sizeof(float), h->st));
+        } else {
+            CK(b.tb.ensure((size_t)nt * 4 * b.X * 8));
+            CK(b.lr.ensure((size_t)nt * 4 * b.nshots * 8 * b.P));
+        }
         CK(b.rsrc.ensure((size_t)b.X * b.rsp));
     }
     CK(b.rrow.ensure((size_t)nt * nrc * b.X));
@@ -407,10 +449,16 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
         if (int rc = encode_grid_map(&b.tm.core[d], b.grid.p, b.P, b.X, TZ, TX, d + 1)) return rc;
     }
     if (!forward_only) {
-        // strips: boxes of (BX rows x 8) and (8 rows x BZ); residual source: BX rows x 4
-        if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, BX)) return rc;
-        if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, BZ, 8))
-            return rc;
+        if (snap) {
+            // snapshots: [snapshot * 2 + comp][X][PS], vx and vz in one box
+            if (int rc = encode_snap_map(&b.tm.snap, b.snap.p, h->snap_fmt, b.PS, b.X, 2 * b.nsnap)) return rc;
+        } else {
+            // strips: boxes of (BX rows x 8) and (8 rows x BZ)
+            if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, BX)) return rc;
+            if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, BZ, 8))
+                return rc;
+        }
+        // residual source: BX rows x 4
         if (int rc = encode_2d_map(&b.tm.rs, b.rsrc.p, b.rsp, b.X, 4, BX)) return rc;
     }
     cudaStream_t st = h->st;
@@ -471,7 +519,9 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
-    std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, b.nshots, b.ntiles, b.X, b.P,
+    std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, h->snap_every, h->snap_fmt,
+                                (long long)(uintptr_t)b.snap.p, (long long)(uintptr_t)b.sscale.p, b.nshots, b.ntiles,
+                                b.X, b.P,
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
                                 (long long)(uintptr_t)b.lr.p, (long long)(uintptr_t)b.rrow.p,
                                 (long long)(uintptr_t)b.rsrc.p, (long long)(uintptr_t)b.dtiles.p,
@@ -686,7 +736,7 @@ template <class F>
 void for_each_buf(sfwi_handle *h, F f) {
     Batch &b = h->b;
     f(b.grid), f(b.tb), f(b.lr), f(b.rrow), f(b.rsrc), f(b.recs), f(b.tmis), f(b.dsigma), f(b.dgeo), f(b.dtiles);
-    f(b.dtrow), f(b.drtr), f(b.derr), f(b.dctr);
+    f(b.dtrow), f(b.drtr), f(b.derr), f(b.dctr), f(b.snap), f(b.sscale);
     f(h->sou), f(h->vp_all), f(h->vs_all), f(h->rho_all), f(h->dvp_all), f(h->dvs_all);
     f(h->gpp), f(h->gps), f(h->gil), f(h->grh), f(h->ls_buf);
 }
@@ -1069,7 +1119,18 @@ int sfwi_set_misfit(sfwi_handle *h, int kind) {
 
 int sfwi_set_density_gradient(sfwi_handle *h, int on) {
     if (int rc = check(h)) return rc;
+    if (on && h->snap_every > 0) return fail(SFWI_E_STATE, "the density kernel needs the reconstruction (snapshots on)");
     h->want_rho = on != 0;
+    return SFWI_OK;
+}
+
+int sfwi_set_snapshots(sfwi_handle *h, int every, int format) {
+    if (int rc = check(h)) return rc;
+    if (every < 0 || (every > 0 && (format < SFWI_SNAP_F32 || format > SFWI_SNAP_BF16)))
+        return fail(SFWI_E_ARG, "snapshots: interval %d, format %d", every, format);
+    if (every > 0 && h->want_rho) return fail(SFWI_E_STATE, "the density kernel needs the reconstruction");
+    h->snap_every = every;
+    h->snap_fmt = every > 0 ? format : SNAP_OFF;
     return SFWI_OK;
 }
 

@@ -41,6 +41,9 @@
 // FD2DGPU.cu:3873-3899).  Each is seen by exactly one stencil sweep, so here
 // each is applied to the staged shared-memory box of that sweep only and the
 // stored state is left untouched — the same arithmetic with no extra kernel.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "sfwi_launch.h"
 
 namespace sfwi {
@@ -556,6 +559,41 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
 }
 
 // ---------------------------------------------------------------------------
+// forward snapshots
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool snap_step(const Params &p, int it) {
+    return p.snap != nullptr && it % p.snap_every == 0;
+}
+// per-shot scales of snapshot k into shared memory (every thread of the CTA
+// takes part; ends with __syncthreads)
+__device__ __forceinline__ void load_snap_scales(const Params &p, int k, float *s_sc) {
+    const int n = 2 * min(p.nshots, SNAP_MAX_SHOTS);
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        s_sc[i] = p.sscale[((size_t)(i >> 1) * p.nsnap + k) * 2 + (i & 1)];
+    __syncthreads();
+}
+__device__ __forceinline__ uint32_t to16(float v, int fmt) {
+    return fmt == SNAP_F16 ? (uint32_t)__half_as_ushort(__float2half_rn(v))
+                           : (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+__device__ __forceinline__ float from16(uint16_t u, int fmt) {
+    return fmt == SNAP_F16 ? __half2float(__ushort_as_half(u)) : __bfloat162float(__ushort_as_bfloat16(u));
+}
+// four consecutive cells of one component of snapshot k
+__device__ __forceinline__ void store_snap4(const Params &p, int k, int comp, size_t cell, float4 v, float scale) {
+    const size_t o = ((size_t)(2 * k + comp) * p.X) * p.PS + cell;
+    if (p.snap_fmt == SNAP_F32) {
+        st4(reinterpret_cast<float *>(p.snap) + o, v);
+    } else {
+        const float inv = scale > 0.f ? 1.0f / scale : 0.f;
+        uint2 w;
+        w.x = to16(v.x * inv, p.snap_fmt) | (to16(v.y * inv, p.snap_fmt) << 16);
+        w.y = to16(v.z * inv, p.snap_fmt) | (to16(v.w * inv, p.snap_fmt) << 16);
+        *reinterpret_cast<uint2 *>(reinterpret_cast<uint16_t *>(p.snap) + o) = w;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // forward velocity sweep
 // ---------------------------------------------------------------------------
 template <bool BORN>
@@ -645,6 +683,25 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.bg, bg, ib, d, 1.f, ax, bz, dx_, cz);
             if (BORN) v_apply<false>(p, m, p.sc, sc, ib, d, 1.f, sax, sbz, sdx, scz);
         }
+        if (snap_step(p, it) && p.snap_fmt != SNAP_F32) {
+            // scale of this step's snapshot: max |v| over the shot (the bits of
+            // non-negative floats order as unsigned integers)
+            float mx = 0.f, mz = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (m.ok[j]) {
+                    mx = fmaxf(mx, fabsf(bg.vx[j]));
+                    mz = fmaxf(mz, fabsf(bg.vz[j]));
+                }
+            const unsigned am = __activemask();
+            const unsigned rx = __reduce_max_sync(am, __float_as_uint(mx));
+            const unsigned rz = __reduce_max_sync(am, __float_as_uint(mz));
+            if ((threadIdx.x & 31) == __ffs(am) - 1) {
+                unsigned *sc = reinterpret_cast<unsigned *>(p.sscale) + ((size_t)c.t.shot * p.nsnap + it / p.snap_every) * 2;
+                atomicMax(sc, rx);
+                atomicMax(sc + 1, rz);
+            }
+        }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body);
 }
@@ -665,6 +722,7 @@ template <bool BORN>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdS<BORN>;
+    __shared__ float s_sc[2 * SNAP_MAX_SHOTS];  // snapshot scales of this step (16-bit formats)
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME;
         uint32_t bytes = S::NB * BOX_BYTES + (BORN ? 10 : 5) * CORE_BYTES;
@@ -745,6 +803,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 }
             }
         }
+        // snapshot of the background velocity after this step (the staged box
+        // holds it): the tile's core cells of this shot's rows and of the
+        // row pitch (a tile's last columns can reach past it)
+        if (snap_step(p, it) && m.lx < c.g.nxpml && m.lz < p.PS) {
+            const int k = it / p.snap_every;
+            const size_t cell = (size_t)(c.g.row0 + m.lx) * p.PS + m.lz;
+            const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
+            store_snap4(p, k, 0, cell, ld4(s_vx + m.r * BZ + m.c), sc[0]);
+            store_snap4(p, k, 1, cell, ld4(s_vz + m.r * BZ + m.c), sc[1]);
+        }
         if (!m.live) return;
         // everything this thread needs from the stage, then release it
         float lam[4], mu[4], ex[4], ez[4];
@@ -817,12 +885,79 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 s_apply<false>(p, m, p.sc, sc, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
         }
     };
+    if (snap_step(p, it) && p.snap_fmt != SNAP_F32) load_snap_scales(p, it / p.snap_every, s_sc);
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body);
 }
 
 // ---------------------------------------------------------------------------
 // backward stress sweeps + imaging
 // ---------------------------------------------------------------------------
+// adjoint stress update of the four cells (txx' keeps only an x-part and
+// tzz' only a z-part; txz' is split, its x-part in amxz) and its stores
+__device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m, bool frame, const Damp &dm,
+                                               float adj_dir, const V4 &aa, const V4 &ba, const V4 &ca, const V4 &da,
+                                               float axx[4], float azz[4], float axz[4], float amxz[4]) {
+    if (!frame) {
+        const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            S2(axx, h, fma2(tx, P2(aa.v, h), P2(axx, h)));
+            S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
+            S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
+        }
+    } else {
+        // PML tile: damping factors are 1 away from the PML
+        const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz), neg = B2(-1.f);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
+            const float2 nxx = mul2(fma2(d1, P2(axx, h), mul2(tx, P2(aa.v, h))), r2);
+            const float2 nzz = mul2(fma2(d3, P2(azz, h), mul2(tz, P2(ba.v, h))), r4);
+            const float2 nx_ = mul2(fma2(d1, P2(amxz, h), mul2(tx, P2(da.v, h))), r2);
+            const float2 nz_ = mul2(fma2(d3, fma2(P2(amxz, h), neg, P2(axz, h)), mul2(tz, P2(ca.v, h))), r4);
+            sel2(axx, h, nxx, m.ok);
+            sel2(azz, h, nzz, m.ok);
+            sel2(amxz, h, nx_, m.ok);
+            sel2(axz, h, add2(nx_, nz_), m.ok);
+        }
+    }
+    st4(p.ad.txx + m.gi, to_f4(axx));
+    st4(p.ad.tzz + m.gi, to_f4(azz));
+    st4(p.ad.txz + m.gi, to_f4(axz));
+    if (frame) st4(p.ad.mtxz + m.gi, to_f4(amxz));
+}
+
+// zero-lag imaging of the lambda and mu kernels (doimage_gradient,
+// FD2DGPU.cu:3350-3382) on the imaging cells, weight w:
+//   G_lam += w * -(gxx + gzz)(txx' + tzz')
+//   G_mu  += w * (-2 (gxx txx' + gzz tzz') - (gxz + gzx) txz')
+// with the forward strains gxx = a/dx, gzz = b/dz, gxz = c/dz, gzx = d/dx
+__device__ __forceinline__ void image_lam_mu(const Params &p, const CellMap &m, float w, const V4 &a, const V4 &b,
+                                             const V4 &cc, const V4 &d, const float axx[4], const float azz[4],
+                                             const float axz[4], float gl[4], float gm[4]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
+        const float2 gxz = mul2(P2(cc.v, h), B2(p.idz)), gzx = mul2(P2(d.v, h), B2(p.idx));
+        const float2 x2 = P2(axx, h), z2 = P2(azz, h);
+        float2 lg = mul2(B2(-1.f), mul2(add2(gxx, gzz), add2(x2, z2)));
+        float2 mg = fma2(B2(-2.f), fma2(gxx, x2, mul2(gzz, z2)), mul2(B2(-1.f), mul2(add2(gxz, gzx), P2(axz, h))));
+        if (w != 1.f) {
+            lg = mul2(B2(w), lg);
+            mg = mul2(B2(w), mg);
+        }
+        const float2 ngl = add2(P2(gl, h), lg), ngm = add2(P2(gm, h), mg);
+        if (m.image[2 * h]) {
+            gl[2 * h] = ngl.x;
+            gm[2 * h] = ngm.x;
+        }
+        if (m.image[2 * h + 1]) {
+            gl[2 * h + 1] = ngl.y;
+            gm[2 * h + 1] = ngm.y;
+        }
+    }
+}
+
 struct BwdS {
     static constexpr int NB = 4;  // vx, vz, avx, avz
     // core: 0 lam, 1 mu, 2 txx, 3 tzz, 4 txz, 5 atxx, 6 atzz, 7 atxz,
@@ -861,6 +996,23 @@ __device__ __forceinline__ StripPick strip_pick(const TileCtx &c, int pml, int n
 }
 // bit pattern marking a packed row without a receiver in the residual source
 constexpr uint32_t NO_RECEIVER = 0xFFFFFFFFu;
+
+// the residual of step `it` replaces the adjoint velocity at the receivers
+// in this sweep's view of the adjoint boxes (rs: the staged residual-source
+// box; rows without a receiver carry the NO_RECEIVER pattern)
+__device__ __forceinline__ void patch_residual(const TileCtx &c, const float *rs_box, int it, float *a_vx,
+                                               float *a_vz) {
+    if (threadIdx.x >= BX) return;
+    const int lx = c.t.x0 - HALO + threadIdx.x;
+    const int zc = c.g.igz - c.bcol;
+    if (lx >= 0 && lx < c.g.nxpml && zc >= 0 && zc < BZ) {
+        const float *rs = rs_box + threadIdx.x * 4 + (2 * it - ((2 * it) & ~3));
+        if (__float_as_uint(rs[0]) != NO_RECEIVER) {
+            a_vz[threadIdx.x * BZ + zc] = rs[0];
+            a_vx[threadIdx.x * BZ + zc] = rs[1];
+        }
+    }
+}
 
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
@@ -952,20 +1104,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 }
             }
         }
-        if ((c.t.flags & TILE_RECV) && threadIdx.x < BX) {
-            // the residual of step `it` replaces the adjoint velocity at the
-            // receivers in this sweep's view (rows without a receiver carry
-            // the NO_RECEIVER pattern)
-            const int lx = c.t.x0 - HALO + threadIdx.x;
-            const int zc = c.g.igz - c.bcol;
-            if (lx >= 0 && lx < nxpml && zc >= 0 && zc < BZ) {
-                const float *rs = s + S::RS + threadIdx.x * 4 + (2 * it - ((2 * it) & ~3));
-                if (__float_as_uint(rs[0]) != NO_RECEIVER) {
-                    a_vz[threadIdx.x * BZ + zc] = rs[0];
-                    a_vx[threadIdx.x * BZ + zc] = rs[1];
-                }
-            }
-        }
+        if (c.t.flags & TILE_RECV) patch_residual(c, s + S::RS, it, a_vx, a_vz);
         consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
@@ -1014,60 +1153,38 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             s_apply<true>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
         else
             s_apply<false>(p, m, p.bg, st, lam, mu, dm, -1.f, a, b, cc, d, nullptr);
-        if (!frame) {
-            const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz);
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                S2(axx, h, fma2(tx, P2(aa.v, h), P2(axx, h)));
-                S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
-                S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
-            }
-        } else {
-            // PML tile: txx' keeps only an x-part and tzz' only a z-part, txz'
-            // is split (x-part in amxz); damping factors are 1 away from the PML
-            const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz), neg = B2(-1.f);
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
-                const float2 nxx = mul2(fma2(d1, P2(axx, h), mul2(tx, P2(aa.v, h))), r2);
-                const float2 nzz = mul2(fma2(d3, P2(azz, h), mul2(tz, P2(ba.v, h))), r4);
-                const float2 nx_ = mul2(fma2(d1, P2(amxz, h), mul2(tx, P2(da.v, h))), r2);
-                const float2 nz_ = mul2(fma2(d3, fma2(P2(amxz, h), neg, P2(axz, h)), mul2(tz, P2(ca.v, h))), r4);
-                sel2(axx, h, nxx, m.ok);
-                sel2(azz, h, nzz, m.ok);
-                sel2(amxz, h, nx_, m.ok);
-                sel2(axz, h, add2(nx_, nz_), m.ok);
-            }
-        }
-        st4(p.ad.txx + m.gi, to_f4(axx));
-        st4(p.ad.tzz + m.gi, to_f4(azz));
-        st4(p.ad.txz + m.gi, to_f4(axz));
-        if (frame) st4(p.ad.mtxz + m.gi, to_f4(amxz));
+        adjoint_stress(p, m, frame, dm, adj_dir, aa, ba, ca, da, axx, azz, axz, amxz);
         // zero-lag imaging of the lambda and mu kernels (interior cells)
         if (image) {
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
-                const float2 gxz = mul2(P2(cc.v, h), B2(p.idz)), gzx = mul2(P2(d.v, h), B2(p.idx));
-                const float2 x2 = P2(axx, h), z2 = P2(azz, h);
-                const float2 lg = mul2(B2(-1.f), mul2(add2(gxx, gzz), add2(x2, z2)));
-                const float2 mg = fma2(B2(-2.f), fma2(gxx, x2, mul2(gzz, z2)),
-                                       mul2(B2(-1.f), mul2(add2(gxz, gzx), P2(axz, h))));
-                const float2 ngl = add2(P2(gl, h), lg), ngm = add2(P2(gm, h), mg);
-                if (m.image[2 * h]) {
-                    gl[2 * h] = ngl.x;
-                    gm[2 * h] = ngm.x;
-                }
-                if (m.image[2 * h + 1]) {
-                    gl[2 * h + 1] = ngl.y;
-                    gm[2 * h + 1] = ngm.y;
-                }
-            }
+            image_lam_mu(p, m, 1.f, a, b, cc, d, axx, azz, axz, gl, gm);
             st4(p.glam + m.gi, to_f4(gl));
             st4(p.gmu + m.gi, to_f4(gm));
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
+}
+
+// Lame-weighted adjoint stresses of a staged box, in place (consumers):
+//   P = (l+2m) txx + l tzz,  Q = l txx + (l+2m) tzz,  R = m txz
+__device__ __forceinline__ void lame_weight(float *s_P, float *s_Q, float *s_R, const float *s_l, const float *s_u) {
+    for (int i = threadIdx.x; i < BOX / 4; i += NTHREADS) {
+        float xx[4], zz[4], xz[4], l[4], u[4], P_[4], Q_[4], R_[4];
+        f4_to(ld4(s_P + 4 * i), xx);
+        f4_to(ld4(s_Q + 4 * i), zz);
+        f4_to(ld4(s_R + 4 * i), xz);
+        f4_to(ld4(s_l + 4 * i), l);
+        f4_to(ld4(s_u + 4 * i), u);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float l2m = l[j] + 2 * u[j];
+            P_[j] = l2m * xx[j] + l[j] * zz[j];
+            Q_[j] = l[j] * xx[j] + l2m * zz[j];
+            R_[j] = u[j] * xz[j];
+        }
+        st4(s_P + 4 * i, to_f4(P_));
+        st4(s_Q + 4 * i, to_f4(Q_));
+        st4(s_R + 4 * i, to_f4(R_));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1106,26 +1223,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         float *s_P = s + 3 * BOX, *s_Q = s + 4 * BOX, *s_R = s + 5 * BOX;
         const float *s_l = s + 6 * BOX, *s_u = s + 7 * BOX;
         const float *core = s + S::NB * BOX;
-        // Lame-weighted adjoint stresses, in place:
-        //   P = (l+2m) txx + l tzz,  Q = l txx + (l+2m) tzz,  R = m txz
-        for (int i = threadIdx.x; i < BOX / 4; i += NTHREADS) {
-            float xx[4], zz[4], xz[4], l[4], u[4], P_[4], Q_[4], R_[4];
-            f4_to(ld4(s_P + 4 * i), xx);
-            f4_to(ld4(s_Q + 4 * i), zz);
-            f4_to(ld4(s_R + 4 * i), xz);
-            f4_to(ld4(s_l + 4 * i), l);
-            f4_to(ld4(s_u + 4 * i), u);
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float l2m = l[j] + 2 * u[j];
-                P_[j] = l2m * xx[j] + l[j] * zz[j];
-                Q_[j] = l[j] * xx[j] + l2m * zz[j];
-                R_[j] = u[j] * xz[j];
-            }
-            st4(s_P + 4 * i, to_f4(P_));
-            st4(s_Q + 4 * i, to_f4(Q_));
-            st4(s_R + 4 * i, to_f4(R_));
-        }
+        lame_weight(s_P, s_Q, s_R, s_l, s_u);
         consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
@@ -1204,6 +1302,171 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 }
 
 // ---------------------------------------------------------------------------
+// backward sweeps from forward snapshots (no reconstruction, no edge strips)
+// ---------------------------------------------------------------------------
+// k_bwd_s_snap: the adjoint stress update of k_bwd_s; at snapshot steps the
+// imaging takes the forward strains from the snapshot box (vx, vz with their
+// halo, decompressed in shared memory) with the reconstruction's stencils,
+// weighted by the snapshot interval, and the illumination from the
+// snapshot's own cells.  k_bwd_v_snap: the adjoint velocity update only.
+template <int FMT>
+struct BwdSSnap {
+    static constexpr int NB = 2;  // adjoint vx, vz
+    // core: 0 atxx, 1 atzz, 2 atxz, 3 dampx, 4 dampz, 5 amtxz, 6 glam, 7 gmu, 8 illum
+    static constexpr int NC = 9;
+    static constexpr int SNAPF = NB * BOX + NC * CORE;  // snapshot vx, vz boxes as floats
+    static constexpr int RAW = SNAPF + 2 * BOX;         // 16-bit snapshot boxes as loaded
+    static constexpr int RS = RAW + (FMT == SNAP_F32 ? 0 : BOX);
+    static constexpr int STAGE = RS + BX * 4;
+};
+
+template <int FMT>
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
+    k_bwd_s_snap(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
+    using S = BwdSSnap<FMT>;
+    __shared__ float s_sc[2 * SNAP_MAX_SHOTS];
+    const bool sstep = snap_step(p, it);
+    const int k = it / p.snap_every;
+    const float w = (float)p.snap_every;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME, img = sstep && (c.t.flags & TILE_IMAGE);
+        const bool recv = c.t.flags & TILE_RECV;
+        const uint32_t bytes = S::NB * BOX_BYTES + (3 + (frame ? 3 : 0) + (img ? 3 : 0)) * CORE_BYTES +
+                               (img ? 2u * BOX * (FMT == SNAP_F32 ? 4u : 2u) : 0u) + (recv ? BX * 4u * 4u : 0u);
+        mbar_expect_tx(bar, bytes);
+        float *core = s + S::NB * BOX;
+        load_boxes(s, tm, c, AD_VX, 2, bar);
+        load_cores(core + 0 * CORE, tm, c, AD_TXX, 3, bar);
+        if (frame) {
+            load_cores(core + 3 * CORE, tm, c, C_DX, 2, bar);
+            load_cores(core + 5 * CORE, tm, c, AD_MTXZ, 1, bar);
+        }
+        if (img) {
+            load_cores(core + 6 * CORE, tm, c, G_LAM, 3, bar);  // G_lam, G_mu, illumination
+            tma_load(s + (FMT == SNAP_F32 ? S::SNAPF : S::RAW), &tm.snap, c.bcol, c.brow, 2 * k, bar);
+        }
+        if (recv) tma_load_2d(s + S::RS, &tm.rs, (2 * it) & ~3, c.brow, bar);
+    };
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
+        float *a_vx = s, *a_vz = s + BOX;
+        const float *core = s + S::NB * BOX;
+        float *sv = s + S::SNAPF;  // snapshot vx box, then vz box
+        const bool img = sstep && (c.t.flags & TILE_IMAGE);
+        if (c.t.flags & TILE_RECV) patch_residual(c, s + S::RS, it, a_vx, a_vz);
+        if (FMT != SNAP_F32 && img) {
+            const uint16_t *raw = reinterpret_cast<const uint16_t *>(s + S::RAW);
+            const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
+            for (int i = threadIdx.x; i < 2 * BOX; i += NTHREADS) sv[i] = from16(raw[i], FMT) * sc[i >= BOX];
+        }
+        consumer_sync();
+        const CellMap m = cell_map(p, c.t, c.g);
+        if (!m.live) return;
+        const bool frame = c.t.flags & TILE_FRAME;
+        // everything this thread needs from the stage, then release it
+        float ex[4], ez[4], axx[4], azz[4], axz[4], amxz[4], gl[4], gm[4], il[4], vx[4], vz[4];
+        core4(core, 0, m.ci, axx);
+        core4(core, 1, m.ci, azz);
+        core4(core, 2, m.ci, axz);
+        if (frame) {
+            core4(core, 3, m.ci, ex);
+            core4(core, 4, m.ci, ez);
+            core4(core, 5, m.ci, amxz);
+        }
+        const V4 aa = dxm(a_vx, m.r, m.c);
+        const V4 ca = dzp(loadw(a_vx, m.r, m.c));
+        const V4 ba = dzm(loadw(a_vz, m.r, m.c));
+        const V4 da = dxp(a_vz, m.r, m.c);
+        V4 a{}, b{}, cc{}, d{};
+        if (img) {
+            core4(core, 6, m.ci, gl);
+            core4(core, 7, m.ci, gm);
+            core4(core, 8, m.ci, il);
+            a = dxm(sv, m.r, m.c);
+            cc = dzp(loadw(sv, m.r, m.c));
+            b = dzm(loadw(sv + BOX, m.r, m.c));
+            d = dxp(sv + BOX, m.r, m.c);
+            f4_to(ld4(sv + m.r * BZ + m.c), vx);
+            f4_to(ld4(sv + BOX + m.r * BZ + m.c), vz);
+        }
+        release();
+        Damp dm{};
+        if (frame) dm = make_damp(p, ex, ez);
+        adjoint_stress(p, m, frame, dm, adj_dir, aa, ba, ca, da, axx, azz, axz, amxz);
+        if (img) {
+            image_lam_mu(p, m, w, a, b, cc, d, axx, azz, axz, gl, gm);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (m.image[j]) il[j] += w * (vx[j] * vx[j] + vz[j] * vz[j]);
+            st4(p.glam + m.gi, to_f4(gl));
+            st4(p.gmu + m.gi, to_f4(gm));
+            st4(p.illum + m.gi, to_f4(il));
+        }
+    };
+    if (sstep && FMT != SNAP_F32) load_snap_scales(p, k, s_sc);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
+}
+
+struct BwdVSnap {
+    static constexpr int NB = 5;  // atxx->P, atzz->Q, atxz->R, lam, mu
+    // core: 0 ib, 1 avx, 2 avz, 3 dampx, 4 dampz, 5 amvx, 6 amvz
+    static constexpr int NC = 7;
+    static constexpr int STAGE = NB * BOX + NC * CORE;
+};
+
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
+    k_bwd_v_snap(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
+    using S = BwdVSnap;
+    auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
+        const bool frame = c.t.flags & TILE_FRAME;
+        mbar_expect_tx(bar, S::NB * BOX_BYTES + (3 + (frame ? 4 : 0)) * CORE_BYTES);
+        float *core = s + S::NB * BOX;
+        load_boxes(s, tm, c, AD_TXX, 3, bar);
+        load_boxes(s + 3 * BOX, tm, c, C_LAM, 2, bar);
+        load_cores(core + 0 * CORE, tm, c, C_IB, 1, bar);
+        load_cores(core + 1 * CORE, tm, c, AD_VX, 2, bar);
+        if (frame) {
+            load_cores(core + 3 * CORE, tm, c, C_DX, 2, bar);
+            load_cores(core + 5 * CORE, tm, c, AD_MVX, 2, bar);
+        }
+    };
+    auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
+        float *s_P = s, *s_Q = s + BOX, *s_R = s + 2 * BOX;
+        const float *core = s + S::NB * BOX;
+        lame_weight(s_P, s_Q, s_R, s + 3 * BOX, s + 4 * BOX);
+        consumer_sync();
+        const CellMap m = cell_map(p, c.t, c.g);
+        if (!m.live) return;
+        const bool frame = c.t.flags & TILE_FRAME;
+        float ib[4], ex[4], ez[4];
+        core4(core, 0, m.ci, ib);
+        if (frame) {
+            core4(core, 3, m.ci, ex);
+            core4(core, 4, m.ci, ez);
+        }
+        VState ad;
+        core4(core, 1, m.ci, ad.vx);
+        core4(core, 2, m.ci, ad.vz);
+        if (frame) {
+            core4(core, 5, m.ci, ad.mx);
+            core4(core, 6, m.ci, ad.mz);
+        }
+        const V4 aax = dxp(s_P, m.r, m.c);
+        const V4 abz = dzm(loadw(s_R, m.r, m.c));
+        const V4 adx = dxm(s_R, m.r, m.c);
+        const V4 acz = dzp(loadw(s_Q, m.r, m.c));
+        release();
+        if (frame) {
+            const Damp dm = make_damp(p, ex, ez);
+            v_apply<true>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
+        } else {
+            const Damp dm{};
+            v_apply<false>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
+        }
+    };
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
+}
+
+// ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
 constexpr size_t SMEM_ALIGN_SLACK = 1024;
@@ -1224,6 +1487,10 @@ cudaError_t configure_step_kernels() {
     SET_SMEM(k_fwd_s<false>, stage_smem<FwdS<false>::STAGE>());
     SET_SMEM(k_bwd_s, stage_smem<BwdS::STAGE>());
     SET_SMEM(k_bwd_v, stage_smem<BwdV::STAGE>());
+    SET_SMEM(k_bwd_s_snap<SNAP_F32>, stage_smem<BwdSSnap<SNAP_F32>::STAGE>());
+    SET_SMEM(k_bwd_s_snap<SNAP_F16>, stage_smem<BwdSSnap<SNAP_F16>::STAGE>());
+    SET_SMEM(k_bwd_s_snap<SNAP_BF16>, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>());
+    SET_SMEM(k_bwd_v_snap, stage_smem<BwdVSnap::STAGE>());
 #undef SET_SMEM
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -1250,10 +1517,23 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
                 k_fwd_s<false><<<grid, BLOCK_THREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm, it);
             break;
         case 2:
-            k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm, it, adj_dir);
+            if (!p.snap)
+                k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm, it, adj_dir);
+            else if (p.snap_fmt == SNAP_F32)
+                k_bwd_s_snap<SNAP_F32>
+                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_F32>::STAGE>(), st>>>(p, tm, it, adj_dir);
+            else if (p.snap_fmt == SNAP_F16)
+                k_bwd_s_snap<SNAP_F16>
+                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_F16>::STAGE>(), st>>>(p, tm, it, adj_dir);
+            else
+                k_bwd_s_snap<SNAP_BF16>
+                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>(), st>>>(p, tm, it, adj_dir);
             break;
         default:
-            k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm, it, adj_dir);
+            if (!p.snap)
+                k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm, it, adj_dir);
+            else
+                k_bwd_v_snap<<<grid, BLOCK_THREADS, stage_smem<BwdVSnap::STAGE>(), st>>>(p, tm, it, adj_dir);
             break;
     }
 }

@@ -17,6 +17,7 @@ struct TmaMaps {
     CUtensorMap box[3], core[3];
     CUtensorMap tb, lr;  // edge strips (top/bottom, left/right layouts)
     CUtensorMap rs;      // residual source per packed row [X][2 nt]
+    CUtensorMap snap;    // forward snapshots [snapshot * 2 + comp][X][PS], vx and vz per box (depth 2)
 };
 cudaError_t configure_step_kernels();
 void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st);

@@ -44,6 +44,13 @@ WORKLOADS = {
     "salt401": dict(name="stage2-salt-401x301-80shots-uneven-apertures", allnx=401, allnz=301, dx=12.5, pml=20,
                     nt=4000, dt=1e-3, f0=15.0, nshots=80, spacing=5, sy=2, gy=0, model="salt", aperture=(150, 401),
                     misfit="L2"),
+    # compressed-snapshot gradient at 2001x801, 5 m, dt 0.5 ms, 25 Hz: FP16
+    # snapshots of vx, vz every 4th step instead of the reconstruction
+    "snap2001": dict(name="snapshot-gradient-2001x801-16shots-fp16-every4", allnx=2001, allnz=801, dx=5.0, pml=20,
+                     nt=6000, dt=5e-4, f0=25.0, nshots=16, spacing=125, sy=2, gy=0, model="layered", aperture=None,
+                     misfit="OT", snap=(4, "f16"),
+                     # forward 152 + adjoint 72 + imaging 32/4 + snapshot write and read 2 comps x 2 B x 2 / 4
+                     pass_bytes=234),
 }
 WORKLOAD = WORKLOADS["fwi376"]
 METRIC = "shot-gradients/s"
@@ -56,6 +63,12 @@ KERNEL_BYTES = {
     "k_fwd_s<born>": 80,   # read v(2) + v_s(2) + lam, mu, bp, bs; RMW sigma(3) + sigma_s(3)
     "k_bwd_s": 88,         # read v(2) + v_adj(2) + lam, mu; RMW sigma(3) + sigma_adj(3) + G_lam, G_mu
     "k_bwd_v": 76,         # read sigma(3) + sigma_adj(3) + lam, mu, 1/rho; RMW v(2) + v_adj(2) + illum
+    # snapshot mode, every 4th step imaging (per-launch average): read v_adj(2), RMW sigma_adj(3);
+    # at 1 launch in 4: snapshot vx, vz (2 x 2 B) + RMW G_lam, G_mu, illum
+    "k_bwd_s_snap<f16>": 32 + (4 + 24) / 4,
+    "k_bwd_s_snap<bf16>": 32 + (4 + 24) / 4,
+    "k_bwd_s_snap<f32>": 32 + (8 + 24) / 4,
+    "k_bwd_v_snap": 40,    # read sigma_adj(3) + lam, mu, 1/rho; RMW v_adj(2)
 }
 # algorithmic bytes per padded cell per time step of a Born shot-gradient:
 # forward 72 + reconstruction 72 + adjoint 72 + imaging 32 + Born add-on 80
@@ -247,6 +260,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=4, help="shots timed one at a time for the plain form")
     ap.add_argument("--serving-requests", type=int, default=24, help="requests of the serving-loop measurement")
+    ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
@@ -294,6 +308,8 @@ def main():
     fd.GPUbufferM(data["dvp"], data["dvs"])
     if w["misfit"] == "OT":
         fd.set_misfit(sg.MISFIT_OT)
+    if w.get("snap"):
+        fd.set_snapshots(*w["snap"])
 
     def step():
         for d, (pz, px) in zip(shots, obs):
@@ -354,7 +370,7 @@ def main():
                 "traffic_note": "DRAM bytes per launch: ncu capture of a 16-shot launch scaled by cells",
                 "alg_bytes_per_launch": KERNEL_BYTES[dom] * cells, "peak_source": peak_kind,
                 "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()}}
-    alg_bytes_step = PASS_BYTES_PER_CELL_STEP * cells * nt
+    alg_bytes_step = w.get("pass_bytes", PASS_BYTES_PER_CELL_STEP) * cells * nt
 
     # plain form: the same engine, one shot per run (the reference's per-shot
     # call pattern), device-timed on an evenly spread sample of the shots
@@ -373,6 +389,29 @@ def main():
         pv = len(pick) / (sum(plain_ms) / 1000.0)
         plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick),
                  "ms_per_shot": round(float(np.mean(plain_ms)), 2), "batched_over_plain": round(value / pv, 2)}
+    # compressed snapshots against FP32 snapshots at full size, on a few shots
+    snap_err = None
+    if w.get("snap") and args.snap_check > 0:
+        pick = shots[:: max(1, len(shots) // args.snap_check)][: args.snap_check]
+        grads = {}
+        for fmt in ("f32", "f16", "bf16"):
+            fd.set_snapshots(w["snap"][0], fmt)
+            for d in pick:
+                i = shots.index(d)
+                fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"],
+                                obs[i][0].array, obs[i][1].array)
+            fd.run()
+            grads[fmt] = fd.read_gradients_f64()
+            fd.imagebuffer_resettozero()
+        fd.set_snapshots(*w["snap"])
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+        snap_err = {"shots": len(pick), "reference": "FP32 snapshots, same interval"}
+        for fmt in ("f16", "bf16"):
+            snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
+                             for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, el = cpu_baseline_sample(w, data, 1, 150, "port")
@@ -390,13 +429,15 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
-                       "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"], "parallelism": "shots-per-gpu",
+                       "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"],
+                       "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
+                                   else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
                        "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),
                        "alg_bytes_per_step_GB": round(alg_bytes_step / 1e9, 2),
                        "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving, "snapshot_error": snap_err,
             "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2)}}
     print(json.dumps(line), flush=True)
     return 0

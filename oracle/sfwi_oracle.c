@@ -360,8 +360,8 @@ static void edge_strips(const grid_t *g, real *vx, real *vz, real *up_x, real *u
  * the reference only declares OT/OT_power/OT_alltrace, FD2DGPU.cuh:21-25).
  *
  * Transform to positive weights, kind 1/3: p(u) = exp((u-max u)/sigma), kind 2:
- * p(u) = u^2 + 1e-3 sigma^2, with sigma = max|obs| of the trace (kind 1, 2)
- * or of the whole gather (kind 3).  f = p(syn)/sum p(syn), g likewise for obs,
+ * p(u) = u^2 + 1e-3 sigma^2, with sigma = max|obs| of the trace, floored at
+ * 1e-3 max|obs| of the gather (kind 1, 2), or of the whole gather (kind 3).  f = p(syn)/sum p(syn), g likewise for obs,
  * F, G their running sums (the CDF at the right end of sample k), and
  * T_k = G^-1(F_k) by linear interpolation inside the containing sample:
  *   T = dt * (m + (F_k - G_{m-1}) / g_m),  G_{m-1} <= F_k < G_m.
@@ -372,6 +372,8 @@ static void edge_strips(const grid_t *g, real *vx, real *vz, real *up_x, real *u
  *   dW/dp_i = (A_i - sum_j f_j A_j) / sum p,   dW/dsyn_i = dW/dp_i * p'(syn_i).
  * All of it runs in double precision.
  * ---------------------------------------------------------------------- */
+#define OT_SIGMA_FLOOR 1e-3 /* per-trace scale floor, relative to the gather's max |obs| */
+
 static double ot_trace(int kind, int n, double dt, double sigma, const float *syn, const float *obs, double *res,
                        double *work) {
     double *f = work, *F = work + n, *g = work + 2 * n, *G = work + 3 * n, *A = work + 4 * n, *T = work + 5 * n;
@@ -454,12 +456,17 @@ void FN(ot_gather)(int kind, float dt, const float *obs_x, const float *obs_z, c
         size_t o = (size_t)tr * length;
         double sx = gmax_x, sz = gmax_z;
         if (kind != 3) {
+            /* the trace's own max |obs|, floored at a fraction of the gather's
+             * so that a trace the wave has not reached (|obs| ~ 0) does not
+             * blow the transform up */
             sx = 0;
             sz = 0;
             for (int k = 0; k < length; k++) {
                 if (fabs(obs_x[o + k]) > sx) sx = fabs(obs_x[o + k]);
                 if (fabs(obs_z[o + k]) > sz) sz = fabs(obs_z[o + k]);
             }
+            if (sx < OT_SIGMA_FLOOR * gmax_x) sx = OT_SIGMA_FLOOR * gmax_x;
+            if (sz < OT_SIGMA_FLOOR * gmax_z) sz = OT_SIGMA_FLOOR * gmax_z;
         }
         W += ot_trace(kind, length, dt, sz, cal_z + o, obs_z + o, res_z + o, work);
         W += ot_trace(kind, length, dt, sx, cal_x + o, obs_x + o, res_x + o, work);

@@ -150,6 +150,7 @@ class FD2DGPU_ELASTIC:
         "bf16"; every=0: reconstruction, as the reference)."""
         code = {"f32": SNAP_F32, "f16": SNAP_F16, "bf16": SNAP_BF16}[fmt] if every else 0
         _lib.check(_lib.load().sfwi_set_snapshots(self._h, int(every), code))
+        self._snap = (int(every), fmt) if every else None
 
     def read_density_gradient_f64(self):
         out = np.zeros((self.allnx, self.allnz), np.float64)
@@ -243,7 +244,9 @@ class FD2DGPU_ELASTIC:
         out = np.zeros(4, np.float32)
         _lib.check(_lib.load().sfwi_time_kernels(self._h, int(reps), _fp(out)))
         born = self.stage == 2
-        names = ["k_fwd_v<born>" if born else "k_fwd_v", "k_fwd_s<born>" if born else "k_fwd_s", "k_bwd_s", "k_bwd_v"]
+        snap = getattr(self, "_snap", None)
+        names = ["k_fwd_v<born>" if born else "k_fwd_v", "k_fwd_s<born>" if born else "k_fwd_s",
+                 "k_bwd_s_snap<%s>" % snap[1] if snap else "k_bwd_s", "k_bwd_v_snap" if snap else "k_bwd_v"]
         return {n: float(v) for n, v in zip(names, out)}
 
     def kernel_launches(self):

@@ -26,6 +26,7 @@ using namespace sfwi;
 namespace {
 
 constexpr int kTimeKernelsMaxReps = 64;
+constexpr double kOtSigmaFloor = OT_SIGMA_FLOOR;
 thread_local std::string g_err;
 
 int fail(int code, const char *fmt, ...) {
@@ -321,7 +322,9 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
                 if (in.isx >= bx0 && in.isx < bx1 && in.isz >= bz0 && in.isz < bz1) f |= TILE_SOURCE;
                 b.tiles.push_back(Tile{s, x0, z0, f});
             }
-        // OT scales: max|obs| per trace and component, or over the gather
+        // OT scales: max|obs| per trace and component (floored at a fraction of
+        // the gather's, so a trace without signal does not blow the transform
+        // up), or over the gather
         {
             std::vector<double> sz(in.ntr, 0.0), sx(in.ntr, 0.0);
             double gz = 0.0, gx = 0.0;
@@ -334,9 +337,10 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
                 gz = std::max(gz, sz[t]);
                 gx = std::max(gx, sx[t]);
             }
+            const bool all = h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE;
             for (int t = 0; t < in.ntr; t++) {
-                b.sigma.push_back(h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE ? gz : sz[t]);
-                b.sigma.push_back(h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE ? gx : sx[t]);
+                b.sigma.push_back(all ? gz : std::max(sz[t], kOtSigmaFloor * gz));
+                b.sigma.push_back(all ? gx : std::max(sx[t], kOtSigmaFloor * gx));
             }
         }
         row += nxpml;
@@ -916,11 +920,11 @@ int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x
         gz = std::max(gz, mz);
         gx = std::max(gx, mx);
     }
-    if (kind == SFWI_MISFIT_OT_ALLTRACE)
-        for (int t = 0; t < tracenum; t++) {
-            sig[2 * t] = gz;
-            sig[2 * t + 1] = gx;
-        }
+    for (int t = 0; t < tracenum; t++) {
+        const bool all = kind == SFWI_MISFIT_OT_ALLTRACE;
+        sig[2 * t] = all ? gz : std::max(sig[2 * t], kOtSigmaFloor * gz);
+        sig[2 * t + 1] = all ? gx : std::max(sig[2 * t + 1], kOtSigmaFloor * gx);
+    }
     int rc = SFWI_OK;
     std::vector<double> tm(2 * (size_t)tracenum);
     do {

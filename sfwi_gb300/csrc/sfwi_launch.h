@@ -62,6 +62,8 @@ void launch_trace_dots(const float *az, const float *ax, const float *bz, const 
                        double *ab, double *aa, cudaStream_t st);
 
 // sfwi_ot.cu
+// floor of the per-trace OT scale, relative to the gather's max |obs|
+constexpr double OT_SIGMA_FLOOR = 1e-3;
 struct OtArgs {
     int kind, nt, ntr, stage;
     double dt;

@@ -6,7 +6,8 @@
 // between positive-normalised traces, written from its definition:
 //   weights   p(u) = exp((u - max u)/sigma)          (OT, OT_alltrace)
 //             p(u) = u^2 + 1e-3 sigma^2              (OT_power)
-//             sigma = max|obs| of the trace (OT, OT_power) or of the gather
+//             sigma = max|obs| of the trace, floored at 1e-3 max|obs| of the
+//             gather (OT, OT_power), or max|obs| of the gather (OT_alltrace)
 //   densities f = p(cal)/sum p(cal), g = p(obs)/sum p(obs)
 //   CDFs      F_k = sum_{j<=k} f_j,  G_k likewise
 //   transport T_k = G^-1(F_k) = dt (m + (F_k - G_{m-1})/g_m), G_{m-1} <= F_k < G_m
@@ -213,15 +214,17 @@ __global__ void k_ot_trace_scale(const float *obs_z, const float *obs_x, int nt,
     if (threadIdx.x == 0) sigma[blockIdx.x] = t;
 }
 
-// gather-wide scale (kind 3): every trace of a component takes the largest
-__global__ void k_ot_gather_scale(double *sigma, int ntr) {
+// gather-wide scale: every trace of a component takes the largest (kind 3),
+// or its own floored at OT_SIGMA_FLOOR times the largest (kinds 1, 2)
+__global__ void k_ot_gather_scale(double *sigma, int ntr, int all) {
     __shared__ double wsum[32];
     const int comp = blockIdx.x;
     double m = 0.0;
     for (int t = threadIdx.x; t < ntr; t += blockDim.x) m = fmax(m, sigma[2 * t + comp]);
     const double g = block_max(m, wsum);
     __syncthreads();
-    for (int t = threadIdx.x; t < ntr; t += blockDim.x) sigma[2 * t + comp] = g;
+    for (int t = threadIdx.x; t < ntr; t += blockDim.x)
+        sigma[2 * t + comp] = all ? g : fmax(sigma[2 * t + comp], OT_SIGMA_FLOOR * g);
 }
 
 // misfit = sum over traces of the two components, in trace order
@@ -272,7 +275,7 @@ extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *sigma = scratch, *tmis = scratch + 2 * OT_NOALLOC_MAX_TRACES, *sum = scratch + 4 * OT_NOALLOC_MAX_TRACES;
     k_ot_trace_scale<<<2 * tracenum, 256, 0, st>>>(obs_z, obs_x, length, sigma);
-    if (kind == 3) k_ot_gather_scale<<<2, 256, 0, st>>>(sigma, tracenum);
+    k_ot_gather_scale<<<2, 256, 0, st>>>(sigma, tracenum, kind == 3);
     OtArgs o{};
     o.kind = kind;
     o.nt = length;

@@ -112,3 +112,40 @@ def test_gpu_shot_gradient_with_ot_adjoint_source_matches_oracle(case, kind):
     for k in ("res_z", "res_x", "grad_pp", "grad_ps", "illum"):
         assert rel(out[k], ref[k]) < TOL, (case, kind, k, rel(out[k], ref[k]))
     assert abs(out["misfit"] - ref["misfit"]) <= TOL * abs(ref["misfit"])
+
+
+def _gather_with_silent_trace(seed=9, ntr=6, nt=400):
+    obs_x, obs_z, cal_x, cal_z = _gather(seed, ntr, nt)
+    rng = np.random.default_rng(seed)
+    # trace 2 has not been reached by the wave: its observed samples are noise
+    # some 30 orders of magnitude below the gather
+    obs_z[2] = (1e-30 * rng.standard_normal(nt)).astype(np.float32)
+    obs_x[2] = (1e-30 * rng.standard_normal(nt)).astype(np.float32)
+    return obs_x, obs_z, cal_x, cal_z
+
+
+@pytest.mark.parametrize("kind", (1, 2))
+def test_oracle_ot_trace_without_signal_stays_bounded(kind):
+    obs_x, obs_z, cal_x, cal_z = _gather_with_silent_trace()
+    m, rx, rz = po.ot_gather(kind, 1e-3, obs_x, obs_z, cal_x, cal_z)
+    assert np.isfinite(m) and np.all(np.isfinite(rx)) and np.all(np.isfinite(rz))
+    # the per-trace scale is floored at 1e-3 of the gather's: the silent
+    # trace's adjoint source is bounded by about (1/floor)^2 times the
+    # others' (with its own max |obs| ~ 1e-30 as the scale it would be some
+    # 30 orders of magnitude larger and overflow a float wavefield)
+    others = np.abs(np.delete(rz, 2, axis=0)).max()
+    assert np.abs(rz[2]).max() < 1e7 * others
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", KINDS)
+def test_gpu_ot_trace_without_signal_matches_oracle(kind):
+    import sfwi_gb300 as sg
+    fn = {1: sg.OT, 2: sg.OT_power, 3: sg.OT_alltrace}[kind]
+    obs_x, obs_z, cal_x, cal_z = _gather_with_silent_trace()
+    m_ref, rx_ref, rz_ref = po.ot_gather(kind, 1e-3, obs_x, obs_z, cal_x, cal_z)
+    rx, rz, m = fn(obs_x, obs_z, cal_x, cal_z, 1e-3)
+    assert np.all(np.isfinite(rx)) and np.all(np.isfinite(rz))
+    assert np.linalg.norm(rz - rz_ref) <= TOL * np.linalg.norm(rz_ref)
+    assert np.linalg.norm(rx - rx_ref) <= TOL * np.linalg.norm(rx_ref)
+    assert abs(m - m_ref) <= TOL * abs(m_ref)

@@ -1,4 +1,5 @@
-"""Build the CUDA library in-tree: sfwi_gb300/lib/libsfwi_gb300.so.
+"""Build the CUDA library in-tree: sfwi_gb300/lib/libsfwi_gb300.so, plus the
+host library libsfwi_host.so and the sfwi_fwi driver next to it.
 
     python -m sfwi_gb300.build
 
@@ -62,7 +63,35 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    build_host(force)
     return LIB
+
+
+HOST = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(LIBDIR, "libsfwi_host.so")
+DRIVER = os.path.join(LIBDIR, "sfwi_fwi")
+# host code: the same results on x86 and Arm (no contraction into FMA)
+CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-Wall"]
+
+
+def build_host(force=False):
+    """The host library (SU I/O, shot index, parameter files) and the
+    sfwi_fwi inversion driver, with the system C++ compiler."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    src = os.path.join(HOST, "sfwi_host.cpp")
+    hdr = [os.path.join(HOST, "sfwi_host.h"), os.path.join(ROOT, "include", "sfwi_gb300.h")]
+    if force or _stale(HOST_LIB, [src] + hdr):
+        r = subprocess.run([cxx] + CXXFLAGS + ["-fPIC", "-shared", "-o", HOST_LIB, src], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host library failed:\n%s%s" % (r.stdout, r.stderr))
+    drv = os.path.join(HOST, "sfwi_fwi.cpp")
+    if force or _stale(DRIVER, [drv, HOST_LIB, LIB] + hdr):
+        cmd = [cxx] + CXXFLAGS + ["-o", DRIVER, drv, "-L", LIBDIR, "-lsfwi_host", "-lsfwi_gb300",
+                                  "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver failed:\n%s%s" % (r.stdout, r.stderr))
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -1,0 +1,315 @@
+// sfwi_fwi.cpp — the stage-1 and stage-2 inversion drivers on one GPU.
+//
+//   sfwi_fwi <para_file> [--stage 1|2] [--iters N] [--misfit l2|ot|ot_power|ot_alltrace]
+//            [--snapshots K f32|f16|bf16] [--gradient-only]
+//
+// The reference runs these as MPI programs (sfwi-stage1/main.cpp,
+// sfwi-stage2/main.cpp): a master hands shots to one worker per GPU, each
+// worker calls IMAGE_SINGLESHOT shot by shot, the gradients are reduced, and
+// the master updates the model.  Here every shot of an iteration advances in
+// the same kernel launches on one GPU (sfwi_enqueue_shot / sfwi_run), and the
+// line search runs all shots and trial models in one batch as well.  The
+// update arithmetic per iteration is the reference's:
+//
+// stage 1 (main.cpp:636-1290; the Hessian inner loop has max_inner = 0):
+//   g = grad / illumination, zero above layer 26; beta_num = sum(grad . g);
+//   beta = beta_num / beta_num(previous) (0 at the first iteration);
+//   cg = g + beta cg_old; d = cg normalised by the largest |cg_pp|, |cg_ps|;
+//   misfits at steps 0, 30, 150 along -d (CALCULATE_ALPHA_parabola_mb);
+//   alpha = vertex of the parabola (cal_step2), clamped to [-100, 300];
+//   vp -= alpha d_pp, vs -= alpha d_ps; layers above 26 take vp[0][0], vs[0][0].
+// stage 2 (sfwi-stage2/main.cpp:600-890): the model perturbation (image)
+//   starts at zero; below layer 26 cg = grad / illumination, above it grad =
+//   cg = 0; beta_num = sum(grad^2 / illumination); cg += beta cg_old;
+//   alpha = fenzi / fenmu (CALCULATE_ALPHA); image -= alpha cg.
+// Output files (float32 [allnx][allnz]) carry the reference's names.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/sfwi_gb300.h"
+#include "sfwi_host.h"
+
+namespace {
+
+constexpr int kCutLayer = 26;
+constexpr float kStep1 = 30.f, kStep2 = 150.f;
+
+void die(const char *what) {
+    std::fprintf(stderr, "sfwi_fwi: %s\n", what);
+    std::exit(1);
+}
+void check(int rc, const char *what) {
+    if (rc) {
+        std::fprintf(stderr, "sfwi_fwi: %s: %s\n", what, sfwi_last_error());
+        std::exit(1);
+    }
+}
+
+std::vector<float> read_model(const char *path, size_t n) {
+    std::vector<float> v(n);
+    FILE *f = std::fopen(path, "rb");
+    if (!f || std::fread(v.data(), sizeof(float), n, f) != n) {
+        std::fprintf(stderr, "sfwi_fwi: cannot read %zu floats from %s\n", n, path);
+        std::exit(1);
+    }
+    std::fclose(f);
+    return v;
+}
+
+void write_model(const std::string &dir, const char *name, int iter, int allnx, int allnz, const float *a) {
+    char path[2048];
+    std::snprintf(path, sizeof path, "%s/%s_%d_%d_%d.dat", dir.c_str(), name, iter, allnx, allnz);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) die("cannot write an output file");
+    std::fwrite(a, sizeof(float), (size_t)allnx * allnz, f);
+    std::fclose(f);
+}
+
+// ricker_wave, sfwi-stage1/main.cpp:251-260 (PI a double literal, the
+// exponent a float product)
+std::vector<float> ricker(int nt, float dt, float fm) {
+    const double PI = 3.14159265358979;
+    const float Nk = (float)(PI * PI * fm * fm * dt * dt);
+    const int t0 = (int)std::ceil(1.0 / (fm * dt));
+    std::vector<float> w(nt);
+    for (int t = 0; t < nt; t++)
+        w[t] = (float)((1.0 - 2.0 * Nk * (t - t0) * (t - t0)) * std::exp(-Nk * (t - t0) * (t - t0)));
+    return w;
+}
+
+// normalize_all, main.cpp:35-49: both arrays divided by their joint max |.|
+void normalize_all(std::vector<float> &a, std::vector<float> &b) {
+    float m = 0;
+    for (float v : a) m = std::fabs(v) > m ? std::fabs(v) : m;
+    for (float v : b) m = std::fabs(v) > m ? std::fabs(v) : m;
+    if (m == 0) return;
+    for (float &v : a) v = v / m;
+    for (float &v : b) v = v / m;
+}
+
+// cal_step2, main.cpp:64-73: vertex of the parabola through the three misfits
+double cal_step2(double m0, double m1, double m2, float s1, float s2) {
+    const double fenzi = (s1 * s1 - s2 * s2) * m0 + (s2 * s2) * m1 + (-s1 * s1) * m2;
+    const double fenmu = (s1 - s2) * m0 + (s2)*m1 + (-s1) * m2;
+    return fenzi / fenmu / 2.0f;
+}
+
+struct Shot {
+    sfwi_shot_desc d;
+    std::vector<int> gc;
+    std::vector<float> rz, rx;
+};
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc < 2) die("usage: sfwi_fwi <para_file> [--stage 1|2] [--iters N] [--misfit l2|ot|...] "
+                      "[--snapshots K f32|f16|bf16] [--gradient-only]");
+    int stage = 1, iters = -1, misfit_kind = SFWI_MISFIT_L2, snap_k = 0, snap_fmt = SFWI_SNAP_F16;
+    bool gradient_only = false;
+    for (int i = 2; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--stage") && i + 1 < argc)
+            stage = std::atoi(argv[++i]);
+        else if (!std::strcmp(argv[i], "--iters") && i + 1 < argc)
+            iters = std::atoi(argv[++i]);
+        else if (!std::strcmp(argv[i], "--misfit") && i + 1 < argc) {
+            const char *m = argv[++i];
+            misfit_kind = !std::strcmp(m, "ot")            ? SFWI_MISFIT_OT
+                          : !std::strcmp(m, "ot_power")    ? SFWI_MISFIT_OT_POWER
+                          : !std::strcmp(m, "ot_alltrace") ? SFWI_MISFIT_OT_ALLTRACE
+                                                           : SFWI_MISFIT_L2;
+        } else if (!std::strcmp(argv[i], "--snapshots") && i + 2 < argc) {
+            snap_k = std::atoi(argv[++i]);
+            const char *f = argv[++i];
+            snap_fmt = !std::strcmp(f, "f32") ? SFWI_SNAP_F32 : !std::strcmp(f, "bf16") ? SFWI_SNAP_BF16 : SFWI_SNAP_F16;
+        } else if (!std::strcmp(argv[i], "--gradient-only"))
+            gradient_only = true;
+        else
+            die("unknown argument");
+    }
+    if (stage != 1 && stage != 2) die("--stage must be 1 or 2");
+    sfwi_para par;
+    if (sfwi_para_read(argv[1], &par)) die("cannot read the parameter file");
+    const int maxiter = iters >= 0 ? iters : par.maxiter;
+    const int allnx = par.allnx, allnz = par.allnz, pml = par.pml;
+    const size_t n = (size_t)allnx * allnz;
+    mkdir(par.outdir, 0755);
+
+    // shots of the record files (index_shot, main.cpp:76-165)
+    int nt = 0, nsh = 0;
+    float dt = 0;
+    if (sfwi_su_index(par.rec_z, &nt, &dt, nullptr, 0, &nsh) || nsh < 1) die("cannot index the z records");
+    std::vector<sfwi_su_shot> table(nsh);
+    check(sfwi_su_index(par.rec_z, &nt, &dt, table.data(), nsh, &nsh), "index");
+    int all_left = table[0].cx_min;
+    for (auto &t : table) all_left = std::min(all_left, t.cx_min);
+    std::printf("shots %d, nt %d, dt %g s\n", nsh, nt, dt);
+
+    // per-shot geometry (main.cpp:585-625) and records
+    std::vector<Shot> shots;
+    int max_nx = 0;
+    for (auto &t : table) {
+        if (t.no < par.minshot || t.no > par.maxshot) continue;
+        Shot s;
+        s.gc.resize(t.ntr);
+        s.rz.resize((size_t)t.ntr * nt);
+        s.rx.resize((size_t)t.ntr * nt);
+        if (sfwi_su_read(par.rec_z, t.pos, t.ntr, nt, s.rz.data(), s.gc.data()) ||
+            sfwi_su_read(par.rec_x, t.pos, t.ntr, nt, s.rx.data(), nullptr))
+            die("cannot read a shot gather");
+        const int nx = (int)(t.cx_max / par.dx + 0.5f) - (int)(t.cx_min / par.dx + 0.5f) + 1;
+        max_nx = std::max(max_nx, nx);
+        s.d.nx = nx;
+        s.d.isx = pml + (int)((t.sx - t.cx_min) / par.dx);
+        s.d.isz = pml + par.sy;
+        s.d.igz = pml + par.gy;
+        s.d.ngx_left = t.cx_min;
+        s.d.delta_left = (int)((t.cx_min - all_left) / par.dx);
+        s.d.record_left_in_v = 0;
+        s.d.ntr = t.ntr;
+        shots.push_back(std::move(s));
+    }
+    if (shots.empty()) die("no shot in [minshot, maxshot]");
+    for (auto &s : shots) {  // pointers into the vectors, which no longer move
+        s.d.gc = s.gc.data();
+        s.d.rec_z = s.rz.data();
+        s.d.rec_x = s.rx.data();
+    }
+
+    // models: vp, vs from the parameter file; rho = 2000 (main.cpp:1472-1475)
+    std::vector<float> vp = read_model(par.vp, n), vs = read_model(par.vs, n), rho(n, 2000.f);
+    std::vector<float> sou = ricker(nt, dt, par.f0);
+    sfwi_handle *h = nullptr;
+    check(sfwi_create(&h, stage, sou.data(), par.dx, par.dz, dt, max_nx + 2 * pml, allnz + 2 * pml, allnx, allnz, 1,
+                      pml, nt, 4, shots[0].d.ntr),
+          "sfwi_create");
+    check(sfwi_set_misfit(h, misfit_kind), "misfit");
+    if (snap_k > 0) check(sfwi_set_snapshots(h, snap_k, snap_fmt), "snapshots");
+
+    std::vector<float> grad_pp(n), grad_ps(n), illum(n), cg_pp(n), cg_ps(n), cg_pp_old(n, 0.f), cg_ps_old(n, 0.f);
+    std::vector<float> image_pp(n, 0.f), image_ps(n, 0.f);  // stage 2: model perturbation
+    double beta_fenmu = 0.0, max_misfit = 0.0;
+    const std::string out = par.outdir;
+    auto enqueue_all = [&]() {
+        for (auto &s : shots) check(sfwi_enqueue_shot(h, &s.d), "enqueue");
+    };
+
+    for (int iter = 0; iter < std::max(maxiter, gradient_only ? 1 : 0); iter++) {
+        if (stage == 1) {
+            check(sfwi_gpu_buffer_vpvs(h, vp.data(), vs.data(), rho.data()), "model");
+        } else {
+            check(sfwi_gpu_buffer_vpvs(h, vp.data(), vs.data(), nullptr), "model");
+            check(sfwi_gpu_buffer_m(h, image_pp.data(), image_ps.data()), "perturbation");
+        }
+        double misfit = 0.0;
+        enqueue_all();
+        check(sfwi_run(h, &misfit, nullptr), "gradient pass");
+        check(sfwi_imagebuffer_resettozero(h, grad_pp.data(), grad_ps.data(), illum.data(), nullptr, nullptr, nullptr,
+                                           nullptr),
+              "gradients");
+        if (iter == 0) max_misfit = misfit;
+        {
+            FILE *f = std::fopen((out + "/misfit.txt").c_str(), "a");
+            if (f) {
+                std::fprintf(f, "i = %d,misfit = %4.3e,rms = %f\n", iter, misfit, misfit / max_misfit);
+                std::fclose(f);
+            }
+        }
+        std::printf("iter %d misfit %.6e\n", iter, misfit);
+        if (gradient_only) {
+            write_model(out, "sum_grad_pp", iter, allnx, allnz, grad_pp.data());
+            write_model(out, "sum_grad_ps", iter, allnx, allnz, grad_ps.data());
+            write_model(out, "sum_illum", iter, allnx, allnz, illum.data());
+            break;
+        }
+        // preconditioning and the conjugate-gradient direction
+        double beta_fenzi = 0.0;
+        for (int i = 0; i < allnx; i++)
+            for (int j = 0; j < allnz; j++) {
+                const size_t k = (size_t)i * allnz + j;
+                if (stage == 1) {
+                    float gp = grad_pp[k] / illum[k], gs = grad_ps[k] / illum[k];
+                    if (j < kCutLayer) gp = gs = 0.f;
+                    cg_pp[k] = gp;
+                    cg_ps[k] = gs;
+                    beta_fenzi += grad_pp[k] * gp + grad_ps[k] * gs;
+                } else {
+                    if (j >= kCutLayer) {
+                        cg_pp[k] = grad_pp[k] / illum[k];
+                        cg_ps[k] = grad_ps[k] / illum[k];
+                    } else {
+                        grad_pp[k] = grad_ps[k] = 0.f;
+                        cg_pp[k] = cg_ps[k] = 0.f;
+                    }
+                    beta_fenzi += grad_pp[k] * grad_pp[k] / illum[k] + grad_ps[k] * grad_ps[k] / illum[k];
+                }
+            }
+        const double beta = iter == 0 ? 0.0 : beta_fenzi / beta_fenmu;
+        for (size_t k = 0; k < n; k++) {
+            cg_pp[k] = cg_pp[k] + beta * cg_pp_old[k];
+            cg_ps[k] = cg_ps[k] + beta * cg_ps_old[k];
+        }
+        cg_pp_old = cg_pp;
+        cg_ps_old = cg_ps;
+        beta_fenmu = beta_fenzi;
+        write_model(out, "sum_grad_pp", iter, allnx, allnz, grad_pp.data());
+        write_model(out, "sum_grad_ps", iter, allnx, allnz, grad_ps.data());
+        if (stage == 1) {
+            write_model(out, "sum_cg_pp", iter, allnx, allnz, cg_pp.data());
+            // line search along the normalised direction, all shots and the
+            // three trial models in one batch
+            std::vector<float> d_pp = cg_pp, d_ps = cg_ps;
+            normalize_all(d_pp, d_ps);
+            double m3[3] = {0.0, 0.0, 0.0};
+            enqueue_all();
+            check(sfwi_line_search_parabola(h, d_pp.data(), d_ps.data(), kStep1, kStep2, m3, nullptr), "line search");
+            double alpha = cal_step2(m3[0], m3[1], m3[2], kStep1, kStep2);
+            if (alpha > 300) alpha = 300;
+            if (alpha < -100) alpha = -100;
+            {
+                FILE *f = std::fopen((out + "/misfit.txt").c_str(), "a");
+                if (f) {
+                    std::fprintf(f, "i = %d,alpha = %5.3e\n", iter, alpha);
+                    std::fclose(f);
+                }
+            }
+            std::printf("iter %d line search misfits %.6e %.6e %.6e alpha %.4g\n", iter, m3[0], m3[1], m3[2], alpha);
+            for (size_t k = 0; k < n; k++) {
+                vp[k] = vp[k] - alpha * d_pp[k];
+                vs[k] = vs[k] - alpha * d_ps[k];
+            }
+            for (int i = 0; i < allnx; i++)
+                for (int j = 0; j < kCutLayer && j < allnz; j++) {
+                    vp[(size_t)i * allnz + j] = vp[0];
+                    vs[(size_t)i * allnz + j] = vs[0];
+                }
+            write_model(out, "vel_p", iter, allnx, allnz, vp.data());
+            write_model(out, "vel_s", iter, allnx, allnz, vs.data());
+        } else {
+            write_model(out, "sum_cggrad_pp", iter, allnx, allnz, cg_pp.data());
+            write_model(out, "sum_cggrad_ps", iter, allnx, allnz, cg_ps.data());
+            write_model(out, "sum_illum", iter, allnx, allnz, illum.data());
+            double fenzi = 0.0, fenmu = 0.0;
+            enqueue_all();
+            check(sfwi_line_search_exact(h, image_pp.data(), image_ps.data(), cg_pp.data(), cg_ps.data(), &fenzi, &fenmu,
+                                         nullptr),
+                  "step length");
+            const double alpha = fenzi / fenmu;
+            std::printf("iter %d fenzi %.6e fenmu %.6e alpha %.4g\n", iter, fenzi, fenmu, alpha);
+            for (size_t k = 0; k < n; k++) {
+                image_pp[k] = image_pp[k] - alpha * cg_pp[k];
+                image_ps[k] = image_ps[k] - alpha * cg_ps[k];
+            }
+            write_model(out, "sum_image_pp", iter, allnx, allnz, image_pp.data());
+            write_model(out, "sum_image_ps", iter, allnx, allnz, image_ps.data());
+        }
+    }
+    sfwi_destroy(h);
+    return 0;
+}

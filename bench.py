@@ -262,6 +262,7 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=24, help="requests of the serving-loop measurement")
     ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
+    ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or TXxTZ")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.nt:
@@ -319,9 +320,20 @@ def main():
         g = fd.imagebuffer_resettozero()
         return m, g
 
+    tune = None
+    if args.tile != "auto":
+        fd.set_tile_shape(tuple(int(v) for v in args.tile.split("x")))
     t0 = time.perf_counter()
-    for _ in range(args.warmup):
+    for i in range(args.warmup):
         m, g = step()
+        if i == 0 and args.tile == "auto":
+            # tile shape: time every shape on the resident batch, keep the
+            # fastest; the remaining warm-up steps capture its graphs
+            choice, tms = fd.autotune(reps=5)
+            tune = {"choice": "%dx%d" % choice, "ms_per_step": {"%dx%d" % k: round(v, 4) for k, v in tms.items()}}
+            log("autotune: %s" % tune)
+    if tune and args.warmup < 2:
+        m, g = step()  # the chosen shape's graphs are captured outside the timed steps
     log("warm-up: %d steps in %.2f s, misfit %.6e" % (args.warmup, time.perf_counter() - t0, m))
     if args.profile_kernels:
         return 0
@@ -356,7 +368,8 @@ def main():
     d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots)
 
     # per-kernel average launch durations (CUDA events on the engine stream)
-    kt = fd.time_kernels(reps=20) if hasattr(fd, "time_kernels") else {}
+    kt = fd.time_kernels(reps=20)
+    fd_tile = fd.tile_shape()
     peak, peak_kind = measured_peak_hbm()
     cells = sum((d["nx"] + 2 * pml) * nzpml for d in shots)
     roof = None
@@ -430,6 +443,7 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
                        "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"],
+                       "tile": "%dx%d" % fd_tile, "autotune": tune,
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
                                    else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
                        "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),

@@ -213,6 +213,30 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
  * launches overwrite the wavefields of the last run (its records and
  * gradients, already read or accumulated, are untouched). */
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
+
+/* Tile shapes of the step kernels (cells of a tile's core, x by z): each is
+ * compiled as its own set of kernels.  16x32 runs two CTAs per SM, the larger
+ * tiles one (their two pipeline stages fill the shared memory); the larger
+ * tiles re-read less halo, the smaller keep more CTAs in flight. */
+#define SFWI_TILE_16x32 0
+#define SFWI_TILE_32x32 1
+#define SFWI_TILE_16x64 2
+#define SFWI_NUM_TILE_SHAPES 3
+
+/* Select the tile shape for this handle's runs (default SFWI_TILE_16x32).
+ * A batch already on the device is re-tiled; results do not depend on the
+ * shape beyond FP32 rounding of the same arithmetic (they are bit-identical:
+ * every cell's update reads the same values in the same order). */
+int sfwi_set_tile_shape(sfwi_handle *h, int shape);
+int sfwi_get_tile_shape(sfwi_handle *h, int *shape, int *tx, int *tz);
+
+/* Autotuner: after a gradient run (sfwi_run / sfwi_run_noalloc), time one
+ * step of the four step kernels for every tile shape on the resident batch
+ * (reps steps each, as sfwi_time_kernels) and keep the fastest.  *choice gets
+ * its SFWI_TILE_* index, out_ms (optional, SFWI_NUM_TILE_SHAPES floats) the
+ * per-step time of each shape.  Like sfwi_time_kernels it overwrites the
+ * last run's wavefields; its gradients, already accumulated, are untouched. */
+int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms);
 /* page-locked host buffers (cudaMallocHost) for records that are copied every
  * iteration; free with sfwi_host_free */
 int sfwi_host_alloc(size_t bytes, void **ptr);

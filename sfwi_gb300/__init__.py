@@ -249,6 +249,27 @@ class FD2DGPU_ELASTIC:
                  "k_bwd_s_snap<%s>" % snap[1] if snap else "k_bwd_s", "k_bwd_v_snap" if snap else "k_bwd_v"]
         return {n: float(v) for n, v in zip(names, out)}
 
+    def set_tile_shape(self, shape):
+        """Tile shape of the step kernels: an index into TILE_SHAPES or a
+        (tx, tz) pair; a batch already on the device is re-tiled."""
+        if not isinstance(shape, int):
+            shape = TILE_SHAPES.index(tuple(shape))
+        _lib.check(_lib.load().sfwi_set_tile_shape(self._h, int(shape)))
+
+    def tile_shape(self):
+        s, tx, tz = C.c_int(), C.c_int(), C.c_int()
+        _lib.check(_lib.load().sfwi_get_tile_shape(self._h, C.byref(s), C.byref(tx), C.byref(tz)))
+        return tx.value, tz.value
+
+    def autotune(self, reps=10):
+        """Time one step of the four step kernels for every tile shape on the
+        last run's batch and keep the fastest; returns (chosen (tx, tz),
+        {(tx, tz): ms per step}).  Overwrites the last run's wavefields."""
+        choice = C.c_int()
+        ms = np.zeros(len(TILE_SHAPES), np.float32)
+        _lib.check(_lib.load().sfwi_autotune(self._h, int(reps), C.byref(choice), _fp(ms)))
+        return TILE_SHAPES[choice.value], {t: float(v) for t, v in zip(TILE_SHAPES, ms)}
+
     def kernel_launches(self):
         return int(_lib.load().sfwi_kernel_launches(self._h))
 
@@ -292,6 +313,8 @@ def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
 
 
 SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
+# tile shapes (core cells x by z) of the step kernels, SFWI_TILE_* order
+TILE_SHAPES = [(16, 32), (32, 32), (16, 64)]
 
 
 class PinnedArray:

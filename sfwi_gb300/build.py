@@ -4,7 +4,9 @@ host library libsfwi_host.so and the sfwi_fwi driver next to it.
     python -m sfwi_gb300.build
 
 Each .cu under sfwi_gb300/csrc is compiled for sm_103a in parallel and linked
-into one shared library with the C ABI of include/sfwi_gb300.h.
+into one shared library with the C ABI of include/sfwi_gb300.h.  The step
+kernels (sfwi_kernels.cu) are compiled once per tile shape into their own
+namespace; the engine picks one of them at run time (sfwi_autotune).
 """
 import os
 import shutil
@@ -18,7 +20,14 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libsfwi_gb300.so")
 OBJDIR = os.path.join(ROOT, "_build", "obj")
-SOURCES = ["sfwi_kernels.cu", "sfwi_aux.cu", "sfwi_ot.cu", "sfwi_engine.cu"]
+# (source, object, defines): the step kernels once per tile shape
+# (core TX x TZ cells, CTAs per SM), then the rest
+TILE_SHAPES = [(16, 32, 2), (32, 32, 1), (16, 64, 1)]
+UNITS = [("sfwi_kernels.cu", "sfwi_kernels_%dx%d.o" % (tx, tz),
+          ["-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c,
+           "-DSFWI_VARIANT_NS=v%dx%d" % (tx, tz), "-DSFWI_VARIANT_FN=tile_variant_%dx%d" % (tx, tz)])
+         for tx, tz, c in TILE_SHAPES]
+UNITS += [(f, f.replace(".cu", ".o"), []) for f in ("sfwi_aux.cu", "sfwi_ot.cu", "sfwi_engine.cu")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 
@@ -44,11 +53,12 @@ def build(force=False, verbose=False):
     headers.append(os.path.join(ROOT, "include", "sfwi_gb300.h"))
     nv = nvcc()
 
-    def compile_one(src):
+    def compile_one(unit):
+        src, obj, defs = unit
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJDIR, src.replace(".cu", ".o"))
+        o = os.path.join(OBJDIR, obj)
         if force or _stale(o, [s] + headers):
-            cmd = [nv] + ARCH + FLAGS + ["-c", s, "-o", o]
+            cmd = [nv] + ARCH + FLAGS + defs + ["-c", s, "-o", o]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed on %s:\n%s%s" % (src, r.stdout, r.stderr))
@@ -56,8 +66,8 @@ def build(force=False, verbose=False):
                 sys.stdout.write(r.stdout + r.stderr)
         return o
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(compile_one, UNITS))
     if force or _stale(LIB, objs):
         cmd = [nv] + ARCH + ["-shared", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)

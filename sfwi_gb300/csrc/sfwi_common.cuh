@@ -16,14 +16,26 @@
 namespace sfwi {
 
 constexpr int NOP = 4;          // stencil half-width (8th order)
-constexpr int TX = 16;          // tile rows (x)
-constexpr int TZ = 32;          // tile columns (z)
+// Tile shape of the step kernels.  The kernel file is compiled once per
+// shape (SFWI_TILE_X x SFWI_TILE_Z cells, SFWI_CTAS persistent CTAs per SM);
+// the engine picks one per batch at run time (sfwi_autotune).
+#ifndef SFWI_TILE_X
+#define SFWI_TILE_X 16
+#endif
+#ifndef SFWI_TILE_Z
+#define SFWI_TILE_Z 32
+#endif
+#ifndef SFWI_CTAS
+#define SFWI_CTAS 2
+#endif
+constexpr int TX = SFWI_TILE_X;  // tile rows (x)
+constexpr int TZ = SFWI_TILE_Z;  // tile columns (z)
 constexpr int HALO = 4;
 constexpr int BX = TX + 2 * HALO;  // staged box rows
 constexpr int BZ = TZ + 2 * HALO;  // staged box columns (multiple of 4)
 constexpr int BOX = BX * BZ;       // floats per staged box
 constexpr int NTHREADS = TX * TZ / 4;  // compute threads of a tile: one float4 of cells each
-constexpr int CTAS_PER_SM = 2;         // persistent CTAs per SM (two independent tile pipelines)
+constexpr int CTAS_PER_SM = SFWI_CTAS;  // persistent CTAs per SM (independent tile pipelines)
 
 // Arrays of the packed batch grid, in allocation order: one [X][P] array each,
 // consecutive in one allocation (array k starts at k*X*P floats), so a single

@@ -95,6 +95,7 @@ struct Batch {
     int nshots = 0, ntiles = 0, X = 0, P = 0, ntr_tot = 0, max_nxpml = 0;
     std::vector<ShotGeo> geo;
     std::vector<Tile> tiles;
+    std::vector<std::vector<int>> rcols;  // per shot: recording and injection columns (tile flags)
     std::vector<int> trow;      // packed receiver row of each trace, -1 outside the update region
     std::vector<int> rtr;       // per packed row: the trace whose residual is injected there, or -1
     std::vector<double> sigma;  // OT scale per trace/component
@@ -160,6 +161,7 @@ struct sfwi_handle {
     float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
     bool use_graphs = true;
     bool last_forward_only = false;
+    const TileVariant *tv = nullptr;  // tile shape of the step kernels
     // trial models of a line search: while set, shots cut their windows from
     // these slot arrays instead of the uploaded model
     const float *slot_vp = nullptr, *slot_vs = nullptr, *slot_dvp = nullptr, *slot_dvs = nullptr;
@@ -232,20 +234,93 @@ int encode_2d_map(CUtensorMap *m, float *base, unsigned long long inner, unsigne
 }
 
 // 3-D map over the snapshots [depth][X][PS] (FP32 or raw 16-bit elements),
-// boxes of BZ x BX x 2 (vx and vz of one snapshot)
-int encode_snap_map(CUtensorMap *m, void *base, int fmt, int PS, int X, int depth) {
+// boxes of bz x bx x 2 (vx and vz of one snapshot)
+int encode_snap_map(CUtensorMap *m, void *base, int fmt, int PS, int X, int depth, int bx, int bz) {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     const size_t es = fmt == SNAP_F32 ? 4 : 2;
     const cuuint64_t dims[3] = {(cuuint64_t)PS, (cuuint64_t)X, (cuuint64_t)depth};
     const cuuint64_t strides[2] = {(cuuint64_t)PS * es, (cuuint64_t)PS * X * es};
-    const cuuint32_t box[3] = {(cuuint32_t)BZ, (cuuint32_t)BX, 2};
+    const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, 2};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(m, fmt == SNAP_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, base,
                      dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SFWI_E_CUDA, "cuTensorMapEncodeTiled (snapshots) failed (%d)", (int)r);
     return SFWI_OK;
+}
+
+// The step kernels compiled for each tile shape, in the order of the
+// SFWI_TILE_* shape indices.
+const TileVariant *tile_variant(int shape) {
+    switch (shape) {
+    case SFWI_TILE_32x32: return tile_variant_32x32();
+    case SFWI_TILE_16x64: return tile_variant_16x64();
+    default: return tile_variant_16x32();
+    }
+}
+
+// The tile table of the batch for the handle's tile shape: tiles over each
+// shot's update region [NOP, n-NOP), flagged by what their core or halo box
+// touches (PML frame, edge-strip bands, receiver cells, imaging interior,
+// source cell).
+void build_tiles(sfwi_handle *h) {
+    Batch &b = h->b;
+    const int pml = h->pml, nzpml = h->nzpml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
+    b.tiles.clear();
+    for (int s = 0; s < b.nshots; s++) {
+        const ShotGeo &g = b.geo[s];
+        const int nxpml = g.nxpml;
+        const std::vector<int> &cols = b.rcols[s];
+        for (int x0 = NOP; x0 < nxpml - NOP; x0 += tx)
+            for (int z0 = NOP; z0 < nzpml - NOP; z0 += tz) {
+                const int cx1 = std::min(x0 + tx, nxpml - NOP), cz1 = std::min(z0 + tz, nzpml - NOP);
+                const int bx0 = x0 - halo, bx1 = x0 + tx + halo, bz0 = z0 - halo, bz1 = z0 + tz + halo;
+                int f = 0;
+                // frame: cells with lx < pml, lx > nxpml-pml, lz < pml or lz > nzpml-pml
+                if (x0 < pml || cx1 - 1 > nxpml - pml || z0 < pml || cz1 - 1 > nzpml - pml) f |= TILE_FRAME;
+                if (box_hits(x0, cx1, z0, cz1, pml, nxpml - pml, pml, nzpml - pml)) f |= TILE_IMAGE;
+                if (box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, pml - NOP, pml + NOP) ||
+                    box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, nzpml - pml - NOP, nzpml - pml + NOP) ||
+                    box_hits(bx0, bx1, bz0, bz1, pml - NOP, pml + NOP, pml, nzpml - pml) ||
+                    box_hits(bx0, bx1, bz0, bz1, nxpml - pml - NOP, nxpml - pml + NOP, pml, nzpml - pml))
+                    f |= TILE_STRIP;
+                if (g.igz >= bz0 && g.igz < bz1)
+                    for (int c : cols)
+                        if (c >= bx0 && c < bx1) {
+                            f |= TILE_RECV;
+                            break;
+                        }
+                if (g.isx >= bx0 && g.isx < bx1 && g.isz >= bz0 && g.isz < bz1) f |= TILE_SOURCE;
+                b.tiles.push_back(Tile{s, x0, z0, f});
+            }
+    }
+    b.ntiles = (int)b.tiles.size();
+}
+
+// Tensor maps of the batch's arrays with the boxes of the handle's tile shape
+// (halo boxes BX x BZ, core tiles TX x TZ); the strip, residual-source and
+// snapshot maps only exist for gradient runs.
+int encode_tile_maps(sfwi_handle *h, bool forward_only) {
+    Batch &b = h->b;
+    const int tx = h->tv->tx, tz = h->tv->tz, bx = tx + 2 * h->tv->halo, bz = tz + 2 * h->tv->halo;
+    const int nt = h->nt;
+    for (int d = 0; d < 3; d++) {
+        if (int rc = encode_grid_map(&b.tm.box[d], b.grid.p, b.P, b.X, bz, bx, d + 1)) return rc;
+        if (int rc = encode_grid_map(&b.tm.core[d], b.grid.p, b.P, b.X, tz, tx, d + 1)) return rc;
+    }
+    if (forward_only) return SFWI_OK;
+    if (h->snap_every > 0) {
+        // snapshots: [snapshot * 2 + comp][X][PS], vx and vz in one box
+        if (int rc = encode_snap_map(&b.tm.snap, b.snap.p, h->snap_fmt, b.PS, b.X, 2 * b.nsnap, bx, bz)) return rc;
+    } else {
+        // strips: boxes of (BX rows x 8) and (8 rows x BZ)
+        if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, bx)) return rc;
+        if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, bz, 8))
+            return rc;
+    }
+    // residual source: BX rows x 4
+    return encode_2d_map(&b.tm.rs, b.rsrc.p, b.rsp, b.X, 4, bx);
 }
 
 int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
@@ -255,6 +330,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     b.P = (nzpml + 3) & ~3;
     b.geo.assign(b.nshots, ShotGeo{});
     b.tiles.clear();
+    b.rcols.clear();
     b.trow.clear();
     b.rtr.clear();
     b.sigma.clear();
@@ -298,30 +374,11 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
             b.trow.push_back(live ? row + rix[t] : -1);
             b.rtr[(size_t)row + iix[t]] = std::max(b.rtr[(size_t)row + iix[t]], tr0 + t);
         }
-        // tiles over the update region [NOP, n-NOP)
-        for (int x0 = NOP; x0 < nxpml - NOP; x0 += TX)
-            for (int z0 = NOP; z0 < nzpml - NOP; z0 += TZ) {
-                const int cx1 = std::min(x0 + TX, nxpml - NOP), cz1 = std::min(z0 + TZ, nzpml - NOP);
-                const int bx0 = x0 - HALO, bx1 = x0 + TX + HALO, bz0 = z0 - HALO, bz1 = z0 + TZ + HALO;
-                int f = 0;
-                // frame: cells with lx < pml, lx > nxpml-pml, lz < pml or lz > nzpml-pml
-                if (x0 < pml || cx1 - 1 > nxpml - pml || z0 < pml || cz1 - 1 > nzpml - pml) f |= TILE_FRAME;
-                const int ix0 = pml, ix1 = nxpml - pml, iz0 = pml, iz1 = nzpml - pml;
-                if (box_hits(x0, cx1, z0, cz1, ix0, ix1, iz0, iz1)) f |= TILE_IMAGE;
-                if (box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, pml - NOP, pml + NOP) ||
-                    box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, nzpml - pml - NOP, nzpml - pml + NOP) ||
-                    box_hits(bx0, bx1, bz0, bz1, pml - NOP, pml + NOP, pml, nzpml - pml) ||
-                    box_hits(bx0, bx1, bz0, bz1, nxpml - pml - NOP, nxpml - pml + NOP, pml, nzpml - pml))
-                    f |= TILE_STRIP;
-                if (in.igz >= bz0 && in.igz < bz1)
-                    for (int t = 0; t < in.ntr; t++)
-                        if ((rix[t] >= bx0 && rix[t] < bx1) || (iix[t] >= bx0 && iix[t] < bx1)) {
-                            f |= TILE_RECV;
-                            break;
-                        }
-                if (in.isx >= bx0 && in.isx < bx1 && in.isz >= bz0 && in.isz < bz1) f |= TILE_SOURCE;
-                b.tiles.push_back(Tile{s, x0, z0, f});
-            }
+        {
+            std::vector<int> cols(rix);
+            cols.insert(cols.end(), iix.begin(), iix.end());
+            b.rcols.push_back(std::move(cols));
+        }
         // OT scales: max|obs| per trace and component (floored at a fraction of
         // the gather's, so a trace without signal does not blow the transform
         // up), or over the gather
@@ -349,7 +406,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     }
     b.X = row;
     b.ntr_tot = tr0;
-    b.ntiles = (int)b.tiles.size();
+    build_tiles(h);
     b.rsp = (2 * nt + 3) & ~3;
     b.cells = (size_t)b.X * b.P;
     h->last_ntr.clear();
@@ -448,23 +505,8 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     const size_t nctr = 4 * (size_t)std::max(h->nt, kTimeKernelsMaxReps + 1);
     CK(b.dctr.ensure(nctr));
     CK(cudaMemsetAsync(b.dctr.p, 0, nctr * sizeof(int), h->st));
-    for (int d = 0; d < 3; d++) {
-        if (int rc = encode_grid_map(&b.tm.box[d], b.grid.p, b.P, b.X, BZ, BX, d + 1)) return rc;
-        if (int rc = encode_grid_map(&b.tm.core[d], b.grid.p, b.P, b.X, TZ, TX, d + 1)) return rc;
-    }
-    if (!forward_only) {
-        if (snap) {
-            // snapshots: [snapshot * 2 + comp][X][PS], vx and vz in one box
-            if (int rc = encode_snap_map(&b.tm.snap, b.snap.p, h->snap_fmt, b.PS, b.X, 2 * b.nsnap)) return rc;
-        } else {
-            // strips: boxes of (BX rows x 8) and (8 rows x BZ)
-            if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, BX)) return rc;
-            if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, BZ, 8))
-                return rc;
-        }
-        // residual source: BX rows x 4
-        if (int rc = encode_2d_map(&b.tm.rs, b.rsrc.p, b.rsp, b.X, 4, BX)) return rc;
-    }
+    if (int rc = encode_tile_maps(h, forward_only)) return rc;
+
     cudaStream_t st = h->st;
     CK(cudaMemcpyAsync(b.dgeo.p, b.geo.data(), b.geo.size() * sizeof(ShotGeo), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, st));
@@ -524,6 +566,7 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, h->snap_every, h->snap_fmt,
+                                (long long)(uintptr_t)h->tv,
                                 (long long)(uintptr_t)b.snap.p, (long long)(uintptr_t)b.sscale.p, b.nshots, b.ntiles,
                                 b.X, b.P,
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
@@ -542,12 +585,18 @@ std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
 void enqueue_forward(sfwi_handle *h, const Params &p, bool forward_only) {
     const bool born = h->stage == 2;
     (void)forward_only;
-    for (int it = 0; it < h->nt; it++) launch_fwd_step(p, h->b.tm, it, born, h->st);
+    for (int it = 0; it < h->nt; it++) {
+        h->tv->launch(0, p, h->b.tm, it, born, 1.f, h->st);
+        h->tv->launch(1, p, h->b.tm, it, born, 1.f, h->st);
+    }
 }
 
 void enqueue_backward(sfwi_handle *h, const Params &p) {
     const float adj = h->stage == 1 ? 1.f : -1.f;
-    for (int it = h->nt - 1; it >= 0; it--) launch_bwd_step(p, h->b.tm, it, adj, h->st);
+    for (int it = h->nt - 1; it >= 0; it--) {
+        h->tv->launch(2, p, h->b.tm, it, false, adj, h->st);
+        h->tv->launch(3, p, h->b.tm, it, false, adj, h->st);
+    }
 }
 
 int capture(sfwi_handle *h, cudaGraphExec_t *out, bool fwd, const Params &p, bool forward_only) {
@@ -1009,8 +1058,10 @@ int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float 
     cudaGetDevice(&h->device);
     int rc = SFWI_OK;
     do {
-        cudaError_t e;
-        if ((e = configure_step_kernels()) != cudaSuccess) {
+        cudaError_t e = cudaSuccess;
+        h->tv = tile_variant(SFWI_TILE_16x32);
+        for (int v = 0; v < SFWI_NUM_TILE_SHAPES && e == cudaSuccess; v++) e = tile_variant(v)->configure();
+        if (e != cudaSuccess) {
             rc = fail(SFWI_E_CUDA, "kernel attributes: %s", cudaGetErrorString(e));
             break;
         }
@@ -1347,9 +1398,9 @@ int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
         // step indices 0..reps select fresh tile counters; the kernels read
         // records and strips at those steps, which exist for every run
         CK(cudaMemsetAsync(h->b.dctr.p, 0, 4 * (size_t)(reps + 1) * sizeof(int), h->st));
-        launch_step_kernel(k, p, h->b.tm, reps, born, adj, h->st);  // warm
+        h->tv->launch(k, p, h->b.tm, reps, born, adj, h->st);  // warm
         CK(cudaEventRecord(h->ev[0], h->st));
-        for (int r = 0; r < reps; r++) launch_step_kernel(k, p, h->b.tm, r, born, adj, h->st);
+        for (int r = 0; r < reps; r++) h->tv->launch(k, p, h->b.tm, r, born, adj, h->st);
         CK(cudaEventRecord(h->ev[1], h->st));
         CK(cudaEventSynchronize(h->ev[1]));
         CK(cudaGetLastError());
@@ -1358,6 +1409,56 @@ int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
         out_ms[k] = ms / reps;
         h->launches += reps + 1;
     }
+    return SFWI_OK;
+}
+
+int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
+    if (int rc = check(h)) return rc;
+    if (reps < 1) return fail(SFWI_E_ARG, "bad argument");
+    if (h->b.ntiles == 0 || !h->b.grid.p) return fail(SFWI_E_STATE, "no batch has been run");
+    if (h->last_forward_only) return fail(SFWI_E_STATE, "the last run was forward-only (no edge strips)");
+    CK(cudaSetDevice(h->device));
+    // one gradient step of the batch (the four step kernels) per tile shape;
+    // the kernels only read the state and the strips and write the
+    // accumulators, which the next run clears
+    float best = 0.f;
+    int pick = 0;
+    for (int v = 0; v < SFWI_NUM_TILE_SHAPES; v++) {
+        if (int rc = sfwi_set_tile_shape(h, v)) return rc;
+        float ms[4];
+        if (int rc = sfwi_time_kernels(h, reps, ms)) return rc;
+        const float t = ms[0] + ms[1] + ms[2] + ms[3];
+        if (out_ms) out_ms[v] = t;
+        if (v == 0 || t < best) best = t, pick = v;
+    }
+    if (choice) *choice = pick;
+    return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_set_tile_shape(sfwi_handle *h, int shape) {
+    if (int rc = check(h)) return rc;
+    if (shape < 0 || shape >= SFWI_NUM_TILE_SHAPES) return fail(SFWI_E_ARG, "tile shape %d out of range", shape);
+    if (h->tv == tile_variant(shape)) return SFWI_OK;
+    h->tv = tile_variant(shape);
+    Batch &b = h->b;
+    if (b.nshots == 0 || !b.grid.p) return SFWI_OK;  // applies to the next batch
+    // re-tile the resident batch and re-encode its maps for the new boxes
+    CK(cudaSetDevice(h->device));
+    build_tiles(h);
+    CK(b.dtiles.ensure(b.tiles.size()));
+    CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));  // b.tiles may change again before the copy ran
+    return encode_tile_maps(h, h->last_forward_only);
+}
+
+int sfwi_get_tile_shape(sfwi_handle *h, int *shape, int *tx, int *tz) {
+    if (int rc = check(h)) return rc;
+    for (int v = 0; v < SFWI_NUM_TILE_SHAPES; v++)
+        if (h->tv == tile_variant(v)) {
+            if (shape) *shape = v;
+            if (tx) *tx = h->tv->tx;
+            if (tz) *tz = h->tv->tz;
+        }
     return SFWI_OK;
 }
 

@@ -46,7 +46,13 @@
 
 #include "sfwi_launch.h"
 
+#ifndef SFWI_VARIANT_NS
+#define SFWI_VARIANT_NS v16x32
+#define SFWI_VARIANT_FN tile_variant_16x32
+#endif
+
 namespace sfwi {
+namespace SFWI_VARIANT_NS {
 
 // 8th-order staggered first-derivative weights, sfwi-stage1/FD2DGPU.cuh:16
 constexpr float K1 = (float)(1225.0 / 1024.0);
@@ -1475,7 +1481,17 @@ constexpr size_t stage_smem() {
     return (size_t)NSTAGE * STAGE * sizeof(float) + SMEM_ALIGN_SLACK;
 }
 
-static int g_nsm = 0;
+// CTAS_PER_SM CTAs of the largest kernel must fit the SM's 228 KB of shared
+// memory (227 KB at most per CTA, 1 KB of it reserved per resident CTA)
+template <int STAGE>
+constexpr bool fits_sm() {
+    return stage_smem<STAGE>() <= 227 * 1024 && CTAS_PER_SM * (stage_smem<STAGE>() + 1024) <= 228 * 1024;
+}
+static_assert(fits_sm<FwdV<true>::STAGE>() && fits_sm<FwdS<true>::STAGE>() && fits_sm<BwdS::STAGE>() &&
+                  fits_sm<BwdV::STAGE>() && fits_sm<BwdSSnap<SNAP_F32>::STAGE>() && fits_sm<BwdVSnap::STAGE>(),
+              "tile shape too large for CTAS_PER_SM resident CTAs");
+
+int g_nsm = 0;
 
 cudaError_t configure_step_kernels() {
     cudaError_t e;
@@ -1538,14 +1554,14 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
     }
 }
 
-void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st) {
-    launch_step_kernel(0, p, tm, it, born, 1.f, st);
-    launch_step_kernel(1, p, tm, it, born, 1.f, st);
-}
+}  // namespace SFWI_VARIANT_NS
 
-void launch_bwd_step(const Params &p, const TmaMaps &tm, int it, float adj_dir, cudaStream_t st) {
-    launch_step_kernel(2, p, tm, it, false, adj_dir, st);
-    launch_step_kernel(3, p, tm, it, false, adj_dir, st);
+#define SFWI_STR2(x) #x
+#define SFWI_STR(x) SFWI_STR2(x)
+const TileVariant *SFWI_VARIANT_FN() {
+    static const TileVariant v{TX, TZ, HALO, CTAS_PER_SM, SFWI_STR(SFWI_VARIANT_NS),
+                               &SFWI_VARIANT_NS::configure_step_kernels, &SFWI_VARIANT_NS::launch_step_kernel};
+    return &v;
 }
 
 }  // namespace sfwi

@@ -19,12 +19,19 @@ struct TmaMaps {
     CUtensorMap rs;      // residual source per packed row [X][2 nt]
     CUtensorMap snap;    // forward snapshots [snapshot * 2 + comp][X][PS], vx and vz per box (depth 2)
 };
-cudaError_t configure_step_kernels();
-void launch_fwd_step(const Params &p, const TmaMaps &tm, int it, bool born, cudaStream_t st);
-void launch_bwd_step(const Params &p, const TmaMaps &tm, int it, float adj_dir, cudaStream_t st);
-// one kernel of a step: 0 fwd v, 1 fwd s, 2 bwd s, 3 bwd v
-void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
-                        cudaStream_t st);
+// One build of the step kernels for one tile shape (sfwi_kernels.cu is
+// compiled once per shape): tx x tz cells per tile, `ctas` persistent CTAs
+// per SM.  launch runs one kernel of a time step: 0 fwd v, 1 fwd s, 2 bwd s,
+// 3 bwd v.
+struct TileVariant {
+    int tx, tz, halo, ctas;
+    const char *name;
+    cudaError_t (*configure)();
+    void (*launch)(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir, cudaStream_t st);
+};
+const TileVariant *tile_variant_16x32();
+const TileVariant *tile_variant_32x32();
+const TileVariant *tile_variant_16x64();
 
 // sfwi_aux.cu
 struct SetupArgs {

@@ -1,0 +1,91 @@
+"""Tile shapes of the step kernels (sfwi_set_tile_shape) and the autotuner
+(sfwi_autotune).  Every shape runs the same per-cell arithmetic in the same
+order, so its records, residuals and gradients equal the default shape's bit
+for bit, and each is within the 1e-4 relative L2 of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from tests.golden.make_golden import load_case
+from tests.helpers import make_engine, rel, run_ref_api
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+KEYS = ("syn_z", "syn_x", "res_z", "res_x", "grad_pp", "grad_ps", "illum")
+
+
+def _shapes():
+    import sfwi_gb300 as sg
+    return sg.TILE_SHAPES
+
+
+def _run(case, shape, snap=None):
+    shot, inputs, _ = load_case(case)
+    fd = make_engine(shot, inputs)
+    fd.set_tile_shape(shape)
+    assert fd.tile_shape() == tuple(shape)
+    if snap:
+        fd.set_snapshots(*snap)
+    out = run_ref_api(shot, inputs, fd=fd)
+    fd.close()
+    return shot, inputs, out
+
+
+@pytest.mark.parametrize("case", ["s1_full", "s2_window", "s2_dx12p5"])
+def test_every_shape_matches_default_and_oracle(case):
+    shot, inputs, base = _run(case, (16, 32))
+    ref = po.run_shot("f64", shot, inputs)
+    for shape in _shapes()[1:]:
+        _, _, out = _run(case, shape)
+        for k in KEYS:
+            assert np.array_equal(out[k], base[k]), (case, shape, k, rel(out[k], base[k]))
+            assert rel(out[k], ref[k]) < TOL, (case, shape, k, rel(out[k], ref[k]))
+        assert out["misfit"] == base["misfit"]
+
+
+def test_every_shape_with_compressed_snapshots():
+    _, _, base = _run("s1_full", (16, 32), snap=(4, "f16"))
+    for shape in _shapes()[1:]:
+        _, _, out = _run("s1_full", shape, snap=(4, "f16"))
+        for k in KEYS:
+            assert np.array_equal(out[k], base[k]), (shape, k, rel(out[k], base[k]))
+
+
+def test_autotune_picks_a_shape_and_keeps_results():
+    shot, inputs, _ = load_case("s1_full")
+    fd = make_engine(shot, inputs)
+    first = run_ref_api(shot, inputs, fd=fd)
+    choice, ms = fd.autotune(reps=3)
+    print("autotune:", choice, ms)
+    assert choice in [tuple(s) for s in _shapes()]
+    assert fd.tile_shape() == choice
+    assert all(v > 0 for v in ms.values()) and ms[choice] == min(ms.values())
+    # the gradients of the run before were accumulated already
+    g = fd.read_gradients_f64()
+    for k, a in zip(("grad_pp", "grad_ps", "illum"), g):
+        assert np.array_equal(a, first[k]), k
+    fd.imagebuffer_resettozero()
+    again = run_ref_api(shot, inputs, fd=fd)
+    fd.close()
+    for k in KEYS:
+        assert np.array_equal(again[k], first[k]), k
+
+
+def test_shape_switch_on_resident_batch_then_time_kernels():
+    shot, inputs, _ = load_case("s2_window")
+    fd = make_engine(shot, inputs)
+    run_ref_api(shot, inputs, fd=fd)
+    for shape in _shapes():
+        fd.set_tile_shape(shape)
+        ms = fd.time_kernels(reps=2)
+        assert all(v > 0 for v in ms.values()), (shape, ms)
+    fd.close()
+
+
+def test_bad_shape_is_refused():
+    import sfwi_gb300 as sg
+    shot, inputs, _ = load_case("s1_window")
+    fd = make_engine(shot, inputs)
+    with pytest.raises(sg.SfwiError):
+        fd.set_tile_shape(7)
+    fd.close()

@@ -262,7 +262,7 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=24, help="requests of the serving-loop measurement")
     ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
-    ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or TXxTZ")
+    ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or a name in sfwi_gb300.TILE_SHAPES")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.nt:
@@ -322,7 +322,7 @@ def main():
 
     tune = None
     if args.tile != "auto":
-        fd.set_tile_shape(tuple(int(v) for v in args.tile.split("x")))
+        fd.set_tile_shape(args.tile)
     t0 = time.perf_counter()
     for i in range(args.warmup):
         m, g = step()
@@ -330,7 +330,7 @@ def main():
             # tile shape: time every shape on the resident batch, keep the
             # fastest; the remaining warm-up steps capture its graphs
             choice, tms = fd.autotune(reps=5)
-            tune = {"choice": "%dx%d" % choice, "ms_per_step": {"%dx%d" % k: round(v, 4) for k, v in tms.items()}}
+            tune = {"choice": choice, "ms_per_step": {k: round(v, 4) for k, v in tms.items()}}
             log("autotune: %s" % tune)
     if tune and args.warmup < 2:
         m, g = step()  # the chosen shape's graphs are captured outside the timed steps
@@ -344,7 +344,7 @@ def main():
     clocks = Clocks()
     clocks.start()
     launches0 = fd.kernel_launches()
-    dev_ms, fwd_ms, bwd_ms = [], [], []
+    dev_ms, fwd_ms, bwd_ms, mis_ms = [], [], [], []
     wall0 = time.perf_counter()
     for _ in range(args.steps):
         m, g = step()
@@ -352,6 +352,7 @@ def main():
         dev_ms.append(t["total_ms"])
         fwd_ms.append(t["forward_ms"])
         bwd_ms.append(t["backward_ms"])
+        mis_ms.append(t["misfit_ms"])
     wall = time.perf_counter() - wall0
     launches = fd.kernel_launches() - launches0
     clk = clocks.stop()
@@ -427,10 +428,10 @@ def main():
                              for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, el = cpu_baseline_sample(w, data, 1, 150, "port")
+        v, el = cpu_baseline_sample(w, data, 1, min(nt, 1000), "port")
         cpu = {"value": v, "unit": "shot-gradients/s", "cores": 1, "kind": "port",
-               "sample": "one shot, 150 of %d time steps (%.1f s), FP32 single-thread transliteration, scaled by nt"
-                         % (nt, el)}
+               "sample": "one shot, %d of %d time steps (%.1f s), FP32 single-thread transliteration, scaled by nt"
+                         % (min(nt, 1000), nt, el)}
     fd.close()
     for pz, px in obs:
         pz.free()
@@ -443,7 +444,7 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
                        "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"],
-                       "tile": "%dx%d" % fd_tile, "autotune": tune,
+                       "tile": fd_tile, "autotune": tune,
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
                                    else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
                        "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),
@@ -452,7 +453,8 @@ def main():
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving, "snapshot_error": snap_err,
-            "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2)}}
+            "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2),
+                         "misfit": round(float(np.mean(mis_ms)), 2)}}
     print(json.dumps(line), flush=True)
     return 0
 

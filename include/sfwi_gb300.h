@@ -187,7 +187,7 @@ int sfwi_ot_alltrace(const float *obs_x, const float *obs_z, const float *cal_x,
  * stream may be NULL (default stream).  The call waits for its stream.
  * Working memory is a fixed 256 KB array that every device loading the
  * library keeps until the process exits: at most 8192 traces per call (larger
- * calls fail with SFWI_E_ARG) and length <= 7264.  The first call on a device
+ * calls fail with SFWI_E_ARG) and length <= 7160.  The first call on a device
  * looks up that array's device address, so make it before any stream
  * capture.  All calls on a device share the array: calls that overlap on the
  * GPU (other streams or threads at the same time) race and must be serialised
@@ -214,20 +214,27 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
  * gradients, already read or accumulated, are untouched). */
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
 
-/* Tile shapes of the step kernels (cells of a tile's core, x by z): each is
- * compiled as its own set of kernels.  16x32 runs two CTAs per SM, the larger
- * tiles one (their two pipeline stages fill the shared memory); the larger
- * tiles re-read less halo, the smaller keep more CTAs in flight. */
+/* Tile shapes of the step kernels (cells of a tile's core, x by z, and the
+ * CTAs per SM): each is compiled as its own set of kernels.  16x32 runs two
+ * CTAs per SM with two pipeline stages each; 32x32 and 16x64 one CTA (two
+ * stages fill the shared memory) and re-read less halo; 16x32_3CTA three
+ * CTAs with one stage each (more warps in flight, fewer registers each). */
 #define SFWI_TILE_16x32 0
 #define SFWI_TILE_32x32 1
 #define SFWI_TILE_16x64 2
-#define SFWI_NUM_TILE_SHAPES 3
+#define SFWI_TILE_16x32_3CTA 3
+#define SFWI_NUM_TILE_SHAPES 4
 
 /* Select the tile shape for this handle's runs (default SFWI_TILE_16x32).
  * A batch already on the device is re-tiled; results do not depend on the
  * shape beyond FP32 rounding of the same arithmetic (they are bit-identical:
  * every cell's update reads the same values in the same order). */
 int sfwi_set_tile_shape(sfwi_handle *h, int shape);
+/* Launch the time-step kernels with programmatic dependent launch (default
+ * on): each may be scheduled while the previous one drains and waits for its
+ * results on the device, which hides the launch gap between the sweeps.
+ * Results do not depend on it. */
+int sfwi_set_launch_overlap(sfwi_handle *h, int on);
 int sfwi_get_tile_shape(sfwi_handle *h, int *shape, int *tx, int *tz);
 
 /* Autotuner: after a gradient run (sfwi_run / sfwi_run_noalloc), time one

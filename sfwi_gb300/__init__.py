@@ -250,21 +250,26 @@ class FD2DGPU_ELASTIC:
         return {n: float(v) for n, v in zip(names, out)}
 
     def set_tile_shape(self, shape):
-        """Tile shape of the step kernels: an index into TILE_SHAPES or a
-        (tx, tz) pair; a batch already on the device is re-tiled."""
-        if not isinstance(shape, int):
-            shape = TILE_SHAPES.index(tuple(shape))
+        """Tile shape of the step kernels: a name in TILE_SHAPES or its
+        index; a batch already on the device is re-tiled."""
+        if isinstance(shape, str):
+            shape = TILE_SHAPES.index(shape)
         _lib.check(_lib.load().sfwi_set_tile_shape(self._h, int(shape)))
 
+    def set_launch_overlap(self, on=True):
+        """Programmatic dependent launch of the time-step kernels (default on)."""
+        _lib.check(_lib.load().sfwi_set_launch_overlap(self._h, int(bool(on))))
+
     def tile_shape(self):
+        """Name of the current tile shape (TILE_SHAPES)."""
         s, tx, tz = C.c_int(), C.c_int(), C.c_int()
         _lib.check(_lib.load().sfwi_get_tile_shape(self._h, C.byref(s), C.byref(tx), C.byref(tz)))
-        return tx.value, tz.value
+        return TILE_SHAPES[s.value]
 
     def autotune(self, reps=10):
         """Time one step of the four step kernels for every tile shape on the
-        last run's batch and keep the fastest; returns (chosen (tx, tz),
-        {(tx, tz): ms per step}).  Overwrites the last run's wavefields."""
+        last run's batch and keep the fastest; returns (chosen name,
+        {name: ms per step}).  Overwrites the last run's wavefields."""
         choice = C.c_int()
         ms = np.zeros(len(TILE_SHAPES), np.float32)
         _lib.check(_lib.load().sfwi_autotune(self._h, int(reps), C.byref(choice), _fp(ms)))
@@ -313,8 +318,9 @@ def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
 
 
 SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
-# tile shapes (core cells x by z) of the step kernels, SFWI_TILE_* order
-TILE_SHAPES = [(16, 32), (32, 32), (16, 64)]
+# tile shapes of the step kernels in SFWI_TILE_* order: core cells x by z,
+# and "x3" for three one-stage CTAs per SM
+TILE_SHAPES = ["16x32", "32x32", "16x64", "16x32x3"]
 
 
 class PinnedArray:

@@ -122,6 +122,7 @@ struct Params {
     int ntiles;
     int *err;                   // set to a nonzero code when a bounded device wait gives up
     int *counters;              // tile counters, one per (time step, kernel): counters[4*it + kernel]
+    int overlap;                // host side: launch step kernels with programmatic dependent launch
 };
 
 // Edge strips of vx and vz saved each forward step and restored in the

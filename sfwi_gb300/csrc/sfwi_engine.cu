@@ -160,6 +160,7 @@ struct sfwi_handle {
     long long launches = 0;
     float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
     bool use_graphs = true;
+    bool launch_overlap = true;  // programmatic dependent launch of the step kernels
     bool last_forward_only = false;
     const TileVariant *tv = nullptr;  // tile shape of the step kernels
     // trial models of a line search: while set, shots cut their windows from
@@ -256,6 +257,7 @@ const TileVariant *tile_variant(int shape) {
     switch (shape) {
     case SFWI_TILE_32x32: return tile_variant_32x32();
     case SFWI_TILE_16x64: return tile_variant_16x64();
+    case SFWI_TILE_16x32_3CTA: return tile_variant_16x32x3();
     default: return tile_variant_16x32();
     }
 }
@@ -421,6 +423,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
 Params make_params(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     Params p{};
+    p.overlap = h->launch_overlap ? 1 : 0;
     p.X = b.X;
     p.P = b.P;
     p.nzpml = h->nzpml;
@@ -566,7 +569,7 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, h->snap_every, h->snap_fmt,
-                                (long long)(uintptr_t)h->tv,
+                                (long long)(uintptr_t)h->tv, h->launch_overlap,
                                 (long long)(uintptr_t)b.snap.p, (long long)(uintptr_t)b.sscale.p, b.nshots, b.ntiles,
                                 b.X, b.P,
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
@@ -675,8 +678,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     CK(cudaSetDevice(h->device));
     int rc = build_batch(h, shots);
     if (rc) return rc;
-    if (mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2 && ot_smem_bytes(h->nt) > 227 * 1024)
-        return fail(SFWI_E_ARG, "OT misfit supports nt <= %d", (int)(227 * 1024 / 32));
+    if (mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2 && h->nt > ot_max_nt())
+        return fail(SFWI_E_ARG, "OT misfit supports nt <= %d", ot_max_nt());
     rc = upload_batch(h, shots, forward_only, mode != RUN_FORWARD);
     if (rc) return rc;
     Batch &b = h->b;
@@ -946,7 +949,7 @@ int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x
     if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z || !misfit || length < 1 || tracenum < 0)
         return fail(SFWI_E_ARG, "sfwi_ot: bad argument");
     if (tracenum == 0) return SFWI_OK;
-    if (ot_smem_bytes(length) > 227 * 1024) return fail(SFWI_E_ARG, "sfwi_ot: length %d too long", length);
+    if (length > ot_max_nt()) return fail(SFWI_E_ARG, "sfwi_ot: length %d exceeds %d samples", length, ot_max_nt());
     const size_t n = (size_t)length * tracenum;
     float *d = nullptr;
     double *dd = nullptr;
@@ -1433,6 +1436,12 @@ int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     }
     if (choice) *choice = pick;
     return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_set_launch_overlap(sfwi_handle *h, int on) {
+    if (int rc = check(h)) return rc;
+    h->launch_overlap = on != 0;
+    return SFWI_OK;
 }
 
 int sfwi_set_tile_shape(sfwi_handle *h, int shape) {

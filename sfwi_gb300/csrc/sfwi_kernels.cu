@@ -60,7 +60,13 @@ constexpr float K2 = (float)(-245.0 / 3072.0);
 constexpr float K3 = (float)(49.0 / 5120.0);
 constexpr float K4 = (float)(-5.0 / 7168.0);
 
-constexpr int NSTAGE = 2;
+#ifndef SFWI_STAGES
+#define SFWI_STAGES 2
+#endif
+// shared-memory pipeline stages per CTA; with one stage the consumers'
+// early release (all inputs in registers before the arithmetic) still lets
+// the next tile's loads overlap this tile's arithmetic
+constexpr int NSTAGE = SFWI_STAGES;
 constexpr int CORE = TX * TZ;  // floats of a core tile
 constexpr uint32_t BOX_BYTES = BOX * 4u, CORE_BYTES = CORE * 4u;
 // iterations of mbarrier.try_wait before a wait is declared lost (each try
@@ -76,6 +82,14 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Programmatic dependent launch: the step kernels are launched so that the
+// next one may start while this one drains.  griddep_wait blocks until the
+// previous kernel of the stream has completed and its writes are visible
+// (at once when there is no such kernel); every read of data another kernel
+// wrote, and every write, comes after it.  griddep_launch lets the next
+// kernel's CTAs be scheduled onto SMs this kernel's CTAs leave.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
@@ -521,13 +535,17 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
         fence_mbar_init();
     }
     __syncthreads();
+    griddep_launch();
     if (warp == PRODUCER_WARP) {
         if (lane != 0) return;
         // the next tile's index and table entries are fetched before the wait
         // for a free stage, so their global round trips overlap that wait
+        // (the counters and the tile table are written before the time loop,
+        // so these reads may also precede the wait for the previous kernel)
         int t = atomicAdd(counter, 1);
         TileCtx ctx;
         if (t < p.ntiles) ctx = tile_ctx(p, t);
+        griddep_wait();
         for (int k = 0;; k++) {
             const int s = k % NSTAGE;
             if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1))) {
@@ -545,6 +563,7 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
             if (t < p.ntiles) ctx = tile_ctx(p, t);
         }
     }
+    griddep_wait();
     for (int k = 0;; k++) {
         const int s = k % NSTAGE;
         const bool ok = mbar_wait(&full[s], (uint32_t)((k / NSTAGE) & 1));
@@ -552,7 +571,7 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
             if (threadIdx.x == 0) {
                 atomicExch(p.err, 1);
                 // the other stage may still be loading: let it land (bounded)
-                mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1));
+                if (NSTAGE > 1) mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1));
             }
             return;
         }
@@ -891,7 +910,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 s_apply<false>(p, m, p.sc, sc, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
         }
     };
-    if (snap_step(p, it) && p.snap_fmt != SNAP_F32) load_snap_scales(p, it / p.snap_every, s_sc);
+    if (snap_step(p, it) && p.snap_fmt != SNAP_F32) {
+        griddep_wait();  // the scales come from the velocity sweep just before
+        load_snap_scales(p, it / p.snap_every, s_sc);
+    }
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body);
 }
 
@@ -1408,7 +1430,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             st4(p.illum + m.gi, to_f4(il));
         }
     };
-    if (sstep && FMT != SNAP_F32) load_snap_scales(p, k, s_sc);
+    if (sstep && FMT != SNAP_F32) {
+        griddep_wait();
+        load_snap_scales(p, k, s_sc);
+    }
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
 }
 
@@ -1516,40 +1541,55 @@ cudaError_t configure_step_kernels() {
 
 static int persistent_grid(int ntiles) { return ntiles < CTAS_PER_SM * g_nsm ? ntiles : CTAS_PER_SM * g_nsm; }
 
+// one persistent launch with programmatic stream serialisation (when
+// p.overlap): the kernel may begin while the previous one in the stream
+// drains, and waits for it in griddep_wait
+template <class... KArgs, class... Args>
+static void launch_step(void (*k)(KArgs...), size_t smem, const Params &p, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(persistent_grid(p.ntiles));
+    cfg.blockDim = dim3(BLOCK_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = p.overlap ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, p, args...);
+}
+
 void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
                         cudaStream_t st) {
-    const int grid = persistent_grid(p.ntiles);
     switch (which) {
         case 0:
             if (born)
-                k_fwd_v<true><<<grid, BLOCK_THREADS, stage_smem<FwdV<true>::STAGE>(), st>>>(p, tm, it);
+                launch_step(k_fwd_v<true>, stage_smem<FwdV<true>::STAGE>(), p, st, tm, it);
             else
-                k_fwd_v<false><<<grid, BLOCK_THREADS, stage_smem<FwdV<false>::STAGE>(), st>>>(p, tm, it);
+                launch_step(k_fwd_v<false>, stage_smem<FwdV<false>::STAGE>(), p, st, tm, it);
             break;
         case 1:
             if (born)
-                k_fwd_s<true><<<grid, BLOCK_THREADS, stage_smem<FwdS<true>::STAGE>(), st>>>(p, tm, it);
+                launch_step(k_fwd_s<true>, stage_smem<FwdS<true>::STAGE>(), p, st, tm, it);
             else
-                k_fwd_s<false><<<grid, BLOCK_THREADS, stage_smem<FwdS<false>::STAGE>(), st>>>(p, tm, it);
+                launch_step(k_fwd_s<false>, stage_smem<FwdS<false>::STAGE>(), p, st, tm, it);
             break;
         case 2:
             if (!p.snap)
-                k_bwd_s<<<grid, BLOCK_THREADS, stage_smem<BwdS::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_s, stage_smem<BwdS::STAGE>(), p, st, tm, it, adj_dir);
             else if (p.snap_fmt == SNAP_F32)
-                k_bwd_s_snap<SNAP_F32>
-                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_F32>::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_s_snap<SNAP_F32>, stage_smem<BwdSSnap<SNAP_F32>::STAGE>(), p, st, tm, it, adj_dir);
             else if (p.snap_fmt == SNAP_F16)
-                k_bwd_s_snap<SNAP_F16>
-                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_F16>::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_s_snap<SNAP_F16>, stage_smem<BwdSSnap<SNAP_F16>::STAGE>(), p, st, tm, it, adj_dir);
             else
-                k_bwd_s_snap<SNAP_BF16>
-                    <<<grid, BLOCK_THREADS, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_s_snap<SNAP_BF16>, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>(), p, st, tm, it,
+                            adj_dir);
             break;
         default:
             if (!p.snap)
-                k_bwd_v<<<grid, BLOCK_THREADS, stage_smem<BwdV::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_v, stage_smem<BwdV::STAGE>(), p, st, tm, it, adj_dir);
             else
-                k_bwd_v_snap<<<grid, BLOCK_THREADS, stage_smem<BwdVSnap::STAGE>(), st>>>(p, tm, it, adj_dir);
+                launch_step(k_bwd_v_snap, stage_smem<BwdVSnap::STAGE>(), p, st, tm, it, adj_dir);
             break;
     }
 }
@@ -1559,7 +1599,7 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
 #define SFWI_STR2(x) #x
 #define SFWI_STR(x) SFWI_STR2(x)
 const TileVariant *SFWI_VARIANT_FN() {
-    static const TileVariant v{TX, TZ, HALO, CTAS_PER_SM, SFWI_STR(SFWI_VARIANT_NS),
+    static const TileVariant v{TX, TZ, HALO, CTAS_PER_SM, SFWI_VARIANT_NS::NSTAGE, SFWI_STR(SFWI_VARIANT_NS),
                                &SFWI_VARIANT_NS::configure_step_kernels, &SFWI_VARIANT_NS::launch_step_kernel};
     return &v;
 }

@@ -24,7 +24,7 @@ struct TmaMaps {
 // per SM.  launch runs one kernel of a time step: 0 fwd v, 1 fwd s, 2 bwd s,
 // 3 bwd v.
 struct TileVariant {
-    int tx, tz, halo, ctas;
+    int tx, tz, halo, ctas, stages;
     const char *name;
     cudaError_t (*configure)();
     void (*launch)(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir, cudaStream_t st);
@@ -32,6 +32,7 @@ struct TileVariant {
 const TileVariant *tile_variant_16x32();
 const TileVariant *tile_variant_32x32();
 const TileVariant *tile_variant_16x64();
+const TileVariant *tile_variant_16x32x3();
 
 // sfwi_aux.cu
 struct SetupArgs {
@@ -83,6 +84,7 @@ struct OtArgs {
 };
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st);
 size_t ot_smem_bytes(int nt);
+int ot_max_nt();
 
 // sfwi_engine.cu: set the calling thread's sfwi_last_error() message; returns code
 int record_error(int code, const char *fmt, ...);

@@ -93,11 +93,70 @@ __device__ void block_scan_array(double *a, int n, bool reverse, double *wsum) {
     __syncthreads();
 }
 
+// exclusive suffix sums over the threads of the block: thread t gets the sum
+// of v over threads t+1 .. blockDim.x-1 (cs: blockDim.x doubles of shared
+// memory; wsum as block_excl_scan)
+__device__ double block_excl_suffix(double v, double *cs, double *wsum) {
+    const int t = threadIdx.x, T = blockDim.x;
+    cs[t] = v;
+    __syncthreads();
+    const double e = block_excl_scan(cs[T - 1 - t], wsum);  // sum over threads after T-1-t
+    cs[T - 1 - t] = e;
+    __syncthreads();
+    const double r = cs[t];
+    __syncthreads();
+    return r;
+}
+
+// smallest m >= lo with G[m] > y, capped at n-1 (G non-decreasing and every
+// index below lo known to hold G <= y): a galloping search from lo, so
+// consecutive quantiles of one thread cost a few probes instead of a full
+// binary search; the answer is that of a binary search over [0, n-1)
+__device__ __forceinline__ int first_above(const double *G, int n, double y, int lo) {
+    if (lo >= n - 1) return n - 1;
+    if (G[lo] > y) return lo;
+    int prev = lo, step = 1, hi;
+    for (;;) {
+        const int nx = prev + step;
+        if (nx >= n - 1) {
+            hi = n - 1;
+            break;
+        }
+        if (G[nx] > y) {
+            hi = nx;
+            break;
+        }
+        prev = nx;
+        step <<= 1;
+    }
+    int l = prev + 1;
+    while (l < hi) {
+        const int mid = (l + hi) >> 1;
+        if (G[mid] > y)
+            hi = mid;
+        else
+            l = mid + 1;
+    }
+    return l;
+}
+
+// The GB300's FP64 rate is a small fraction of its FP32 rate, so the kernel
+// spends FP64 operations sparingly: each thread owns one contiguous chunk of
+// samples, the positivity transform (one exp per sample and trace) is
+// evaluated once and kept, the CDF of the synthetic trace is formed on the
+// fly from the chunk's running sum, the quantile search continues from the
+// previous sample's quantile, and divisions by per-trace constants are
+// multiplications by their reciprocals.
+constexpr int OT_MAX_CHUNK = 32;  // samples per thread: nt <= 32 * OT_THREADS
+
 __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
     extern __shared__ double ot_sm[];
     __shared__ double wsum[32];
+    __shared__ double cs[OT_THREADS];
     const int n = a.nt;
-    double *F = ot_sm, *G = F + n, *R = G + n, *Q = R + n;
+    // G: CDF of the observed trace; g: its density; P: p(cal); Q: the terms
+    // r f dt / g, then the adjoint weights A
+    double *G = ot_sm, *g = G + n, *P = g + n, *Q = P + n;
     const int tr = blockIdx.x >> 1, comp = blockIdx.x & 1;
     const size_t o = (size_t)tr * n;
     const float *cal = (comp ? a.cal_x : a.cal_z) + o;
@@ -106,76 +165,97 @@ __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
     float *res = (comp ? a.res_x : a.res_z) + o;
     double sigma = a.sigma[2 * tr + comp];
     if (!(sigma > 0.0)) sigma = 1.0;
+    const double inv_sigma = 1.0 / sigma;
     const bool pw = a.kind == 2;
     auto pred = [&](int k) -> double { return cal2 ? (double)(cal[k] + cal2[k]) : (double)cal[k]; };
+    const int chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int k0 = min(n, (int)threadIdx.x * chunk), k1 = min(n, k0 + chunk);
 
     double mc = -DBL_MAX, mo = -DBL_MAX;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = k0; k < k1; k++) {
         mc = fmax(mc, pred(k));
         mo = fmax(mo, (double)obs[k]);
     }
     const double cmax = block_max(mc, wsum), omax = block_max(mo, wsum);
     const double eps = 1e-3 * sigma * sigma;
-    auto pf = [&](double u) { return pw ? u * u + eps : exp((u - cmax) / sigma); };
-    auto pg = [&](double u) { return pw ? u * u + eps : exp((u - omax) / sigma); };
+    auto pf = [&](double u) { return pw ? u * u + eps : exp((u - cmax) * inv_sigma); };
+    auto pg = [&](double u) { return pw ? u * u + eps : exp((u - omax) * inv_sigma); };
 
     double sf = 0.0, sg = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = k0; k < k1; k++) {
         const double x = pf(pred(k)), y = pg((double)obs[k]);
-        F[k] = x;
-        G[k] = y;
+        P[k] = x;
+        g[k] = y;
         sf += x;
         sg += y;
     }
     const double Sf = block_reduce(sf, wsum), Sg = block_reduce(sg, wsum);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        F[k] /= Sf;
-        G[k] /= Sg;
+    const double inv_Sf = 1.0 / Sf, inv_Sg = 1.0 / Sg;
+    // densities, the chunk sums of both, and the CDF G of the observed trace
+    double cf = 0.0, cg = 0.0;
+    for (int k = k0; k < k1; k++) {
+        g[k] *= inv_Sg;
+        cg += g[k];
+        cf += P[k] * inv_Sf;
     }
-    __syncthreads();
-    block_scan_array(F, n, false, wsum);
-    block_scan_array(G, n, false, wsum);
-
-    double w = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double y = F[k];
-        int lo = 0, hi = n - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (G[mid] > y)
-                hi = mid;
-            else
-                lo = mid + 1;
+    const double offF = block_excl_scan(cf, wsum), offG = block_excl_scan(cg, wsum);
+    {
+        double run = offG;
+        for (int k = k0; k < k1; k++) {
+            run += g[k];
+            G[k] = run;
         }
-        const int m = lo;
-        const double gm = pg((double)obs[m]) / Sg;
-        const double Gm1 = m > 0 ? G[m - 1] : 0.0;
-        const double T = a.dt * (m + (y - Gm1) / gm);
-        const double r = (k + 1) * a.dt - T;
-        const double fk = pf(pred(k)) / Sf;
-        w += r * r * fk;
-        R[k] = r;
-        Q[k] = r * fk * a.dt / gm;
     }
     __syncthreads();
-    block_scan_array(Q, n, true, wsum);
-    double fa = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double A = R[k] * R[k] - 2.0 * Q[k];
-        fa += pf(pred(k)) / Sf * A;
+
+    // transport T_k = G^-1(F_k) and the misfit terms
+    double w = 0.0, sq = 0.0, Fk = offF;
+    double r_loc[OT_MAX_CHUNK];
+    int m = 0;
+    for (int i = 0; i < k1 - k0; i++) {
+        const int k = k0 + i;
+        const double fk = P[k] * inv_Sf;
+        Fk += fk;
+        m = first_above(G, n, Fk, m);
+        const double gm = g[m];
+        const double inv_gm = 1.0 / gm;
+        const double Gm1 = m > 0 ? G[m - 1] : 0.0;
+        const double T = a.dt * (m + (Fk - Gm1) * inv_gm);
+        const double r = (k + 1) * a.dt - T;
+        w += r * r * fk;
+        r_loc[i] = r;
+        const double q = r * fk * a.dt * inv_gm;
+        Q[k] = q;
+        sq += q;
+    }
+    // suffix sums of q, the adjoint weights A_k = r_k^2 - 2 sum_{j>=k} q_j and
+    // their f-weighted sum
+    const double offQ = block_excl_suffix(sq, cs, wsum);
+    double fa = 0.0, run = offQ;
+    for (int i = k1 - k0 - 1; i >= 0; i--) {
+        const int k = k0 + i;
+        run += Q[k];
+        const double A = r_loc[i] * r_loc[i] - 2.0 * run;
+        Q[k] = A;
+        fa += P[k] * inv_Sf * A;
     }
     const double FA = block_reduce(fa, wsum);
     const double W = block_reduce(w, wsum);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double A = R[k] * R[k] - 2.0 * Q[k];
-        const double u = pred(k);
-        const double dp = pw ? 2.0 * u : exp((u - cmax) / sigma) / sigma;
-        res[k] = (float)(0.5 * (A - FA) / Sf * dp);
+    for (int k = k0; k < k1; k++) {
+        const double dp = pw ? 2.0 * pred(k) : P[k] * inv_sigma;
+        res[k] = (float)(0.5 * (Q[k] - FA) * inv_Sf * dp);
     }
     if (threadIdx.x == 0) a.trace_misfit[2 * tr + comp] = W;
 }
 
 size_t ot_smem_bytes(int nt) { return (size_t)4 * nt * sizeof(double); }
+
+// longest trace k_ot takes: four FP64 arrays of nt samples next to the static
+// block-scan buffers within 227 KB, and at most OT_MAX_CHUNK samples a thread
+int ot_max_nt() {
+    const int by_smem = (int)((227 * 1024 - (OT_THREADS + 32) * sizeof(double) - 1024) / (4 * sizeof(double)));
+    return by_smem < OT_MAX_CHUNK * OT_THREADS ? by_smem : OT_MAX_CHUNK * OT_THREADS;
+}
 
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st) {
     const size_t sm = ot_smem_bytes(a.nt);
@@ -255,8 +335,8 @@ extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z,
     if (tracenum > OT_NOALLOC_MAX_TRACES)
         return record_error(-1, "sfwi_ot_noalloc: %d traces exceed the fixed scratch of %d traces", tracenum,
                             OT_NOALLOC_MAX_TRACES);
-    if (ot_smem_bytes(length) > 227 * 1024)
-        return record_error(-1, "sfwi_ot_noalloc: length %d exceeds %d samples", length, (int)(227 * 1024 / 32));
+    if (length > ot_max_nt())
+        return record_error(-1, "sfwi_ot_noalloc: length %d exceeds %d samples", length, ot_max_nt());
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return record_error(-2, "sfwi_ot_noalloc: %s", cudaGetErrorString(e));

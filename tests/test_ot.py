@@ -91,10 +91,15 @@ def test_oracle_ot_grows_with_the_time_shift():
 def test_gpu_ot_entry_points_match_oracle(kind):
     import sfwi_gb300 as sg
     fn = {1: sg.OT, 2: sg.OT_power, 3: sg.OT_alltrace}[kind]
-    for seed, ntr, nt in ((1, 5, 300), (2, 96, 3000), (3, 1, 7)):
+    # lengths: short, the 3000-sample gathers, one sample a thread past a
+    # block (257), the 6000-sample snapshot workload and the longest taken
+    for seed, ntr, nt in ((1, 5, 300), (2, 96, 3000), (3, 1, 7), (4, 3, 257), (5, 4, 6000), (6, 2, 7160)):
         obs_x, obs_z, cal_x, cal_z = _gather(seed, ntr, nt, shift=min(6, nt // 2))
         m_ref, rx_ref, rz_ref = po.ot_gather(kind, 1e-3, obs_x, obs_z, cal_x, cal_z)
         rx, rz, m = fn(obs_x, obs_z, cal_x, cal_z, 1e-3)
+        print("kind %d nt %d: rel err x %.2e z %.2e misfit %.2e" % (
+            kind, nt, np.linalg.norm(rx - rx_ref) / np.linalg.norm(rx_ref),
+            np.linalg.norm(rz - rz_ref) / np.linalg.norm(rz_ref), abs(m - m_ref) / abs(m_ref)))
         assert np.linalg.norm(rx_ref) > 0
         assert np.linalg.norm(rx - rx_ref) <= TOL * np.linalg.norm(rx_ref), (kind, seed, "x")
         assert np.linalg.norm(rz - rz_ref) <= TOL * np.linalg.norm(rz_ref), (kind, seed, "z")
@@ -149,3 +154,11 @@ def test_gpu_ot_trace_without_signal_matches_oracle(kind):
     assert np.linalg.norm(rz - rz_ref) <= TOL * np.linalg.norm(rz_ref)
     assert np.linalg.norm(rx - rx_ref) <= TOL * np.linalg.norm(rx_ref)
     assert abs(m - m_ref) <= TOL * abs(m_ref)
+
+
+@pytest.mark.gpu
+def test_gpu_ot_refuses_traces_longer_than_its_shared_memory():
+    import sfwi_gb300 as sg
+    obs_x, obs_z, cal_x, cal_z = _gather(7, 1, 7161)
+    with pytest.raises(sg.SfwiError):
+        sg.OT(obs_x, obs_z, cal_x, cal_z, 1e-3)

@@ -1,7 +1,9 @@
-"""Tile shapes of the step kernels (sfwi_set_tile_shape) and the autotuner
-(sfwi_autotune).  Every shape runs the same per-cell arithmetic in the same
-order, so its records, residuals and gradients equal the default shape's bit
-for bit, and each is within the 1e-4 relative L2 of the FP64 oracle."""
+"""Launch configurations of the step kernels: tile shapes
+(sfwi_set_tile_shape), the autotuner (sfwi_autotune) and programmatic
+dependent launch (sfwi_set_launch_overlap).  Every configuration runs the same
+per-cell arithmetic in the same order, so its records, residuals and gradients
+equal the default's bit for bit, and each is within the 1e-4 relative L2 of
+the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -23,7 +25,7 @@ def _run(case, shape, snap=None):
     shot, inputs, _ = load_case(case)
     fd = make_engine(shot, inputs)
     fd.set_tile_shape(shape)
-    assert fd.tile_shape() == tuple(shape)
+    assert fd.tile_shape() == shape
     if snap:
         fd.set_snapshots(*snap)
     out = run_ref_api(shot, inputs, fd=fd)
@@ -33,7 +35,7 @@ def _run(case, shape, snap=None):
 
 @pytest.mark.parametrize("case", ["s1_full", "s2_window", "s2_dx12p5"])
 def test_every_shape_matches_default_and_oracle(case):
-    shot, inputs, base = _run(case, (16, 32))
+    shot, inputs, base = _run(case, "16x32")
     ref = po.run_shot("f64", shot, inputs)
     for shape in _shapes()[1:]:
         _, _, out = _run(case, shape)
@@ -44,7 +46,7 @@ def test_every_shape_matches_default_and_oracle(case):
 
 
 def test_every_shape_with_compressed_snapshots():
-    _, _, base = _run("s1_full", (16, 32), snap=(4, "f16"))
+    _, _, base = _run("s1_full", "16x32", snap=(4, "f16"))
     for shape in _shapes()[1:]:
         _, _, out = _run("s1_full", shape, snap=(4, "f16"))
         for k in KEYS:
@@ -57,7 +59,7 @@ def test_autotune_picks_a_shape_and_keeps_results():
     first = run_ref_api(shot, inputs, fd=fd)
     choice, ms = fd.autotune(reps=3)
     print("autotune:", choice, ms)
-    assert choice in [tuple(s) for s in _shapes()]
+    assert choice in _shapes()
     assert fd.tile_shape() == choice
     assert all(v > 0 for v in ms.values()) and ms[choice] == min(ms.values())
     # the gradients of the run before were accumulated already
@@ -89,3 +91,18 @@ def test_bad_shape_is_refused():
     with pytest.raises(sg.SfwiError):
         fd.set_tile_shape(7)
     fd.close()
+
+
+@pytest.mark.parametrize("case", ["s1_full", "s2_window"])
+def test_launch_overlap_keeps_results(case):
+    shot, inputs, _ = load_case(case)
+    outs = []
+    for on in (True, False):
+        fd = make_engine(shot, inputs)
+        fd.set_launch_overlap(on)
+        outs.append(run_ref_api(shot, inputs, fd=fd))
+        ms = fd.time_kernels(reps=5)
+        print(case, "overlap" if on else "serial", {k: round(v * 1e3, 2) for k, v in ms.items()})
+        fd.close()
+    for k in KEYS:
+        assert np.array_equal(outs[0][k], outs[1][k]), k

@@ -74,6 +74,14 @@ struct Tile {
     int z0;
     int flags;
 };
+// tile table entry as the step kernels read it: the tile and its shot's
+// geometry in one 64-byte record, fetched in one round trip per tile
+struct alignas(16) TileRec {
+    Tile t;
+    ShotGeo g;
+    int pad[2];
+};
+static_assert(sizeof(TileRec) == 64, "TileRec is four 16-byte words");
 enum TileFlags : int {
     TILE_FRAME = 1,      // intersects the PML frame (damping != 0 somewhere)
     TILE_STRIP = 2,      // core or halo touches an edge strip
@@ -106,7 +114,7 @@ struct Params {
     float *glam, *gmu, *illum;  // per-cell imaging accumulators
     float *grho;                // density kernel accumulator, null unless requested
     const ShotGeo *geo;
-    const Tile *tiles;
+    const TileRec *tiles;
     const float *sou;           // [nt]
     float *tb, *lr;             // edge strips (layout below); null in modelling-only runs
     float *rrow;                // receiver-row records [nt][nrc][X]

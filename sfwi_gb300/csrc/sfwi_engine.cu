@@ -98,7 +98,6 @@ struct Batch {
     std::vector<std::vector<int>> rcols;  // per shot: recording and injection columns (tile flags)
     std::vector<int> trow;      // packed receiver row of each trace, -1 outside the update region
     std::vector<int> rtr;       // per packed row: the trace whose residual is injected there, or -1
-    std::vector<double> sigma;  // OT scale per trace/component
     int rsp = 0;                // row length of the residual source (2 nt rounded up to 4)
     // device
     DevBuf<float> grid;      // NGRID * X * P
@@ -112,7 +111,8 @@ struct Batch {
     DevBuf<double> tmis;     // 2 * ntr_tot
     DevBuf<double> dsigma;
     DevBuf<ShotGeo> dgeo;
-    DevBuf<Tile> dtiles;
+    std::vector<TileRec> trecs;  // tiles with their shot geometry, as uploaded
+    DevBuf<TileRec> dtiles;
     DevBuf<int> dtrow, drtr;
     size_t cells = 0;        // X * P
     DevBuf<int> derr;        // device-side error flag (bounded waits)
@@ -300,6 +300,21 @@ void build_tiles(sfwi_handle *h) {
     b.ntiles = (int)b.tiles.size();
 }
 
+// The tile table as the step kernels read it: each tile with its shot's
+// geometry (b.trecs stays alive until the copy has run)
+int upload_tiles(sfwi_handle *h) {
+    Batch &b = h->b;
+    b.trecs.resize(b.tiles.size());
+    for (size_t i = 0; i < b.tiles.size(); i++) {
+        b.trecs[i] = TileRec{};
+        b.trecs[i].t = b.tiles[i];
+        b.trecs[i].g = b.geo[b.tiles[i].shot];
+    }
+    CK(b.dtiles.ensure(b.trecs.size()));
+    CK(cudaMemcpyAsync(b.dtiles.p, b.trecs.data(), b.trecs.size() * sizeof(TileRec), cudaMemcpyHostToDevice, h->st));
+    return SFWI_OK;
+}
+
 // Tensor maps of the batch's arrays with the boxes of the handle's tile shape
 // (halo boxes BX x BZ, core tiles TX x TZ); the strip, residual-source and
 // snapshot maps only exist for gradient runs.
@@ -335,7 +350,6 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     b.rcols.clear();
     b.trow.clear();
     b.rtr.clear();
-    b.sigma.clear();
     int row = 0, tr0 = 0;
     b.max_nxpml = 0;
     for (int s = 0; s < b.nshots; s++) {
@@ -380,27 +394,6 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
             std::vector<int> cols(rix);
             cols.insert(cols.end(), iix.begin(), iix.end());
             b.rcols.push_back(std::move(cols));
-        }
-        // OT scales: max|obs| per trace and component (floored at a fraction of
-        // the gather's, so a trace without signal does not blow the transform
-        // up), or over the gather
-        {
-            std::vector<double> sz(in.ntr, 0.0), sx(in.ntr, 0.0);
-            double gz = 0.0, gx = 0.0;
-            for (int t = 0; t < in.ntr; t++)
-                for (int k = 0; k < nt; k++) {
-                    if (in.obs_z) sz[t] = std::max(sz[t], (double)std::fabs(in.obs_z[(size_t)t * nt + k]));
-                    if (in.obs_x) sx[t] = std::max(sx[t], (double)std::fabs(in.obs_x[(size_t)t * nt + k]));
-                }
-            for (int t = 0; t < in.ntr; t++) {
-                gz = std::max(gz, sz[t]);
-                gx = std::max(gx, sx[t]);
-            }
-            const bool all = h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE;
-            for (int t = 0; t < in.ntr; t++) {
-                b.sigma.push_back(all ? gz : std::max(sz[t], kOtSigmaFloor * gz));
-                b.sigma.push_back(all ? gx : std::max(sx[t], kOtSigmaFloor * gx));
-            }
         }
         row += nxpml;
         tr0 += in.ntr;
@@ -500,7 +493,6 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(b.tmis.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
     CK(b.dsigma.ensure(2 * (size_t)std::max(b.ntr_tot, 1)));
     CK(b.dgeo.ensure(b.geo.size()));
-    CK(b.dtiles.ensure(b.tiles.size()));
     CK(b.dtrow.ensure(std::max<size_t>(b.trow.size(), 1)));
     CK(b.drtr.ensure(b.rtr.size()));
     CK(b.derr.ensure(1));
@@ -512,12 +504,10 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 
     cudaStream_t st = h->st;
     CK(cudaMemcpyAsync(b.dgeo.p, b.geo.data(), b.geo.size() * sizeof(ShotGeo), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, st));
+    if (int rc = upload_tiles(h)) return rc;
     if (!b.trow.empty())
         CK(cudaMemcpyAsync(b.dtrow.p, b.trow.data(), b.trow.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(b.drtr.p, b.rtr.data(), b.rtr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    if (!b.sigma.empty())
-        CK(cudaMemcpyAsync(b.dsigma.p, b.sigma.data(), b.sigma.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     // zero the state (fields, memory variables, accumulators) and the records
     CK(cudaMemsetAsync(b.grid.p, 0, (size_t)NSTATE * b.cells * sizeof(float), st));
     CK(cudaMemsetAsync(b.recs.p, 0, recs * sizeof(float), st));
@@ -562,6 +552,14 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(cudaEventRecord(h->ev[4], st));
     launch_setup(a, b.nshots, b.max_nxpml, st);
     h->launches++;
+    // OT scales: max|obs| per trace and component, floored at a fraction of
+    // the shot's largest (a trace without signal must not blow the transform
+    // up), or the shot's largest for every trace
+    if (with_obs && h->misfit_kind != SFWI_MISFIT_L2 && b.ntr_tot) {
+        launch_ot_scales(b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), nt, b.ntr_tot, b.dgeo.p, b.nshots,
+                         h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE, b.dsigma.p, st);
+        h->launches += 2;
+    }
     CK(cudaGetLastError());
     return SFWI_OK;
 }
@@ -1454,9 +1452,8 @@ int sfwi_set_tile_shape(sfwi_handle *h, int shape) {
     // re-tile the resident batch and re-encode its maps for the new boxes
     CK(cudaSetDevice(h->device));
     build_tiles(h);
-    CK(b.dtiles.ensure(b.tiles.size()));
-    CK(cudaMemcpyAsync(b.dtiles.p, b.tiles.data(), b.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, h->st));
-    CK(cudaStreamSynchronize(h->st));  // b.tiles may change again before the copy ran
+    if (int rc = upload_tiles(h)) return rc;
+    CK(cudaStreamSynchronize(h->st));  // b.trecs may change again before the copy ran
     return encode_tile_maps(h, h->last_forward_only);
 }
 

@@ -468,8 +468,14 @@ struct TileCtx {
 };
 __device__ __forceinline__ TileCtx tile_ctx(const Params &p, int ti) {
     TileCtx c;
-    c.t = p.tiles[ti];
-    c.g = p.geo[c.t.shot];
+    // one 64-byte record: four independent 16-byte loads
+    const int4 *src = reinterpret_cast<const int4 *>(p.tiles + ti);
+    int4 w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) w[i] = __ldg(src + i);
+    const TileRec *r = reinterpret_cast<const TileRec *>(w);
+    c.t = r->t;
+    c.g = r->g;
     c.brow = c.g.row0 + c.t.x0 - HALO;
     c.bcol = c.t.z0 - HALO;
     c.crow = c.g.row0 + c.t.x0;
@@ -542,7 +548,10 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
         // for a free stage, so their global round trips overlap that wait
         // (the counters and the tile table are written before the time loop,
         // so these reads may also precede the wait for the previous kernel)
+        // tile indices are drawn one tile ahead, so each draw's round trip
+        // overlaps the staging of the tile before it
         int t = atomicAdd(counter, 1);
+        int t_next = atomicAdd(counter, 1);
         TileCtx ctx;
         if (t < p.ntiles) ctx = tile_ctx(p, t);
         griddep_wait();
@@ -559,8 +568,12 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
             }
             s_ctx[s] = ctx;
             issue(ctx, sm + s * STAGE_FLOATS, &full[s]);
-            t = atomicAdd(counter, 1);
-            if (t < p.ntiles) ctx = tile_ctx(p, t);
+            // indices only grow: once one is past the end, so are all later ones
+            t = t_next;
+            if (t < p.ntiles) {
+                ctx = tile_ctx(p, t);
+                t_next = atomicAdd(counter, 1);
+            }
         }
     }
     griddep_wait();

@@ -85,6 +85,10 @@ struct OtArgs {
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st);
 size_t ot_smem_bytes(int nt);
 int ot_max_nt();
+// OT scales of a batch on the device: max |obs| per (trace, component),
+// floored per shot (sigma: 2 doubles per trace; geo: the batch's shots)
+void launch_ot_scales(const float *obs_z, const float *obs_x, int nt, int ntr, const ShotGeo *geo, int nshots,
+                      int all, double *sigma, cudaStream_t st);
 
 // sfwi_engine.cu: set the calling thread's sfwi_last_error() message; returns code
 int record_error(int code, const char *fmt, ...);

@@ -307,6 +307,29 @@ __global__ void k_ot_gather_scale(double *sigma, int ntr, int all) {
         sigma[2 * t + comp] = all ? g : fmax(sigma[2 * t + comp], OT_SIGMA_FLOOR * g);
 }
 
+// per-shot floor of the trace scales (kinds 1, 2) or the shot's largest
+// scale for every trace (kind 3); block = (shot, component)
+__global__ void k_ot_shot_scale(double *sigma, const ShotGeo *geo, int all) {
+    __shared__ double wsum[32];
+    const int s = blockIdx.x >> 1, comp = blockIdx.x & 1;
+    const int t0 = geo[s].tr0, n = geo[s].ntr;
+    double m = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) m = fmax(m, sigma[2 * (t0 + t) + comp]);
+    const double g = block_max(m, wsum);
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        double &v = sigma[2 * (t0 + t) + comp];
+        v = all ? g : fmax(v, OT_SIGMA_FLOOR * g);
+    }
+}
+
+void launch_ot_scales(const float *obs_z, const float *obs_x, int nt, int ntr, const ShotGeo *geo, int nshots,
+                      int all, double *sigma, cudaStream_t st) {
+    if (ntr < 1) return;
+    k_ot_trace_scale<<<2 * ntr, 256, 0, st>>>(obs_z, obs_x, nt, sigma);
+    k_ot_shot_scale<<<2 * nshots, 256, 0, st>>>(sigma, geo, all);
+}
+
 // misfit = sum over traces of the two components, in trace order
 __global__ void k_ot_sum(const double *trace_misfit, int ntr, double *out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {

@@ -36,6 +36,13 @@ if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
+    # one plain stage-1 shot-gradient at 376x201: vertical-force source at
+    # node (188, 2), OT misfit, no Born term
+    "shot376": dict(name="plain-shot-376x201-stage1-vzforce-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
+                    dt=1e-3, f0=15.0, nshots=1, spacing=10, first=188, sy=2, gy=0, model="layered", aperture=None,
+                    misfit="OT", stage=1, source="vz",
+                    # forward 72 + adjoint 72 + reconstruction 72 + imaging 32
+                    pass_bytes=248),
     # one FWI iteration at 376x201 (the headline line)
     "fwi376": dict(name="fwi-iteration-376x201-38shots-born-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
                    dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0, model="layered", aperture=None, misfit="OT"),
@@ -59,6 +66,8 @@ METRIC = "shot-gradients/s"
 # array read once and written once per sweep, stencil neighbours reused on
 # chip, PML memory variables not counted)
 KERNEL_BYTES = {
+    "k_fwd_v": 32,         # read sigma(3) + 1/rho; RMW v(2)
+    "k_fwd_s": 40,         # read v(2) + lam, mu; RMW sigma(3)
     "k_fwd_v<born>": 60,   # read sigma(3) + sigma_s(3) + 1/rho; RMW v(2) + v_s(2)
     "k_fwd_s<born>": 80,   # read v(2) + v_s(2) + lam, mu, bp, bs; RMW sigma(3) + sigma_s(3)
     "k_bwd_s": 88,         # read v(2) + v_adj(2) + lam, mu; RMW sigma(3) + sigma_adj(3) + G_lam, G_mu
@@ -94,10 +103,27 @@ def build_workload(w):
     vp0 = synth.smooth_z(vp, 10)
     vs0 = (vp0 / 1.73).astype(np.float32)
     rho0 = (310.0 * vp0.astype(np.float64) ** 0.25).astype(np.float32)
-    shots = synth.config_shots(w["allnx"], w["dx"], w["pml"], w["nshots"], w["spacing"], aperture=w.get("aperture"))
+    shots = synth.config_shots(w["allnx"], w["dx"], w["pml"], w["nshots"], w["spacing"], first=w.get("first"),
+                               aperture=w.get("aperture"))
     sou = ricker(w["nt"], w["dt"], w["f0"])
     return dict(vp=vp, vs=vs, rho=rho, vp0=vp0, vs0=vs0, rho0=rho0, dvp=(vp - vp0).astype(np.float32),
                 dvs=(vs - vs0).astype(np.float32), shots=shots, sou=sou)
+
+
+L2_BYTES = 129e6  # GB300 L2
+
+
+def l2_note(cells, nt, nshots, w):
+    """How the timed steps relate to L2: a step is a whole pass of nt time
+    steps, each of which reads and writes the whole wavefield state once per
+    sweep; the state either exceeds L2 or stays in it across the sweeps."""
+    state = cells * 4 * 41
+    strips = 0 if w.get("snap") else 4 * nt * 2 * 8 * 4 * (cells / max(1, nshots)) ** 0.5 * nshots
+    if state > L2_BYTES:
+        return "inputs larger than L2: wavefield state %.2f GB per sweep" % (state / 1e9)
+    return ("wavefield state %.0f MB fits in L2 and stays there across the sweeps of a pass (a step is a whole "
+            "pass of %d time steps, no flush between steps); records and edge strips (~%.0f MB per pass) "
+            "stream through HBM" % (state / 1e6, nt, strips / 1e6))
 
 
 def ricker(nt, dt, fm):
@@ -177,16 +203,18 @@ def cpu_baseline_sample(w, data, nthreads, nt_sample, kind="port"):
     po.build()
     d = data["shots"][len(data["shots"]) // 2]
     nt = nt_sample
-    shot = dict(stage=2, allnx=w["allnx"], allnz=w["allnz"], nx=d["nx"], pml=w["pml"], nop=4, nt=nt, ntr=d["ntr"],
+    stage = w.get("stage", 2)
+    shot = dict(stage=stage, allnx=w["allnx"], allnz=w["allnz"], nx=d["nx"], pml=w["pml"], nop=4, nt=nt, ntr=d["ntr"],
                 dx=w["dx"], dz=w["dx"], dt=w["dt"], isx=d["isx"], isz=w["pml"] + w["sy"], igz=w["pml"] + w["gy"],
                 ngx_left=d["ngx_left"], delta_left=d["delta_left"], record_left_in_v=0, forward_only=0,
-                misfit_kind=0 if kind == "reference" else 1, nthreads=nthreads)
+                misfit_kind=0 if kind == "reference" else 1, nthreads=nthreads,
+                src_kind=1 if w.get("source") == "vz" and kind != "reference" else 0)
     rng = np.random.default_rng(0)
     model = dict(vp=data["vp0"], vs=data["vs0"], rho=data["rho0"], dvp=data["dvp"], dvs=data["dvs"],
                  sou=data["sou"][:nt], gc=d["gc"],
                  obs_z=(1e-9 * rng.standard_normal((d["ntr"], nt))).astype(np.float32),
                  obs_x=(1e-9 * rng.standard_normal((d["ntr"], nt))).astype(np.float32))
-    lib = {"port": "f32", "reference": "ref2"}[kind]
+    lib = {"port": "f32", "reference": "ref%d" % stage}[kind]
     t = time.perf_counter()
     po.run_shot(lib, shot, model)
     el = time.perf_counter() - t
@@ -220,10 +248,11 @@ def run_reference_arm(args, w):
     if rank != 0:
         return 0
     from oracle import pyoracle as po
-    kind = "reference" if po.available("ref2") else "port"
+    ref = "ref%d" % w.get("stage", 2)
+    kind = "reference" if po.available(ref) else "port"
     try:
         if kind == "reference":
-            po.load("ref2")
+            po.load(ref)
     except OSError:
         kind = "port"
     data = build_workload(w)
@@ -284,6 +313,7 @@ def main():
 
     import sfwi_gb300 as sg
     data = build_workload(w)
+    stage = w.get("stage", 2)
     nt, pml = w["nt"], w["pml"]
     nxpml, nzpml = w["allnx"] + 2 * pml, w["allnz"] + 2 * pml
     shots = data["shots"]
@@ -293,6 +323,8 @@ def main():
     fwd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml,
                              nt, 4, shots[0]["ntr"], stage=1)
     fwd.GPUbufferVPVS(data["vp"], data["vs"], data["rho"])
+    if w.get("source") == "vz":
+        fwd.set_source(sg.SOURCE_VZ_FORCE)
     for d in shots:
         fwd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"])
     fwd.run_forward()
@@ -306,9 +338,14 @@ def main():
     fwd.close()
 
     fd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml, nt,
-                            4, shots[0]["ntr"], stage=2)
-    fd.GPUbufferVPVS(data["vp0"], data["vs0"])
-    fd.GPUbufferM(data["dvp"], data["dvs"])
+                            4, shots[0]["ntr"], stage=stage)
+    if stage == 2:
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"])
+        fd.GPUbufferM(data["dvp"], data["dvs"])
+    else:
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])
+    if w.get("source") == "vz":
+        fd.set_source(sg.SOURCE_VZ_FORCE)
     if w["misfit"] == "OT":
         fd.set_misfit(sg.MISFIT_OT)
     if w.get("snap"):
@@ -445,11 +482,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
-                       "nt": nt, "misfit": w["misfit"], "born": True, "dx_m": w["dx"],
+                       "nt": nt, "misfit": w["misfit"], "born": stage == 2, "dx_m": w["dx"],
+                       "source": "vertical force" if w.get("source") == "vz" else "txx+tzz",
                        "tile": fd_tile, "autotune": tune,
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
                                    else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
-                       "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 41 / 1e9 + 0.0),
+                       "l2": l2_note(cells, nt, len(shots), w),
                        "alg_bytes_per_step_GB": round(alg_bytes_step / 1e9, 2),
                        "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,

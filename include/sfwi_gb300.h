@@ -214,6 +214,16 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
  * gradients, already read or accumulated, are untouched). */
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
 
+/* Source of the forward sweeps.  SFWI_SOURCE_TXX_TZZ (default) is the
+ * reference's: sou[it] added to txx and tzz at the source cell ahead of the
+ * velocity sweep (sfwi-stage1/FD2DGPU.cu:2104-2114).  SFWI_SOURCE_VZ_FORCE is
+ * a vertical force with no reference counterpart: sou[it] added to vz at the
+ * source cell after the velocity sweep.  Both go into the total field only,
+ * so the next sweep of that field rebuilds it from its split parts. */
+#define SFWI_SOURCE_TXX_TZZ 0
+#define SFWI_SOURCE_VZ_FORCE 1
+int sfwi_set_source(sfwi_handle *h, int kind);
+
 /* Tile shapes of the step kernels (cells of a tile's core, x by z, and the
  * CTAs per SM): each is compiled as its own set of kernels.  16x32 runs two
  * CTAs per SM with two pipeline stages each; 32x32 and 16x64 one CTA (two

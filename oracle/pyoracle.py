@@ -33,7 +33,7 @@ class Shot(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("stage", "allnx", "allnz", "nx", "pml", "nop", "nt", "ntr")] + \
                [(n, C.c_float) for n in ("dx", "dz", "dt")] + \
                [(n, C.c_int) for n in ("isx", "isz", "igz", "ngx_left", "delta_left", "record_left_in_v",
-                                       "forward_only", "misfit_kind", "nthreads", "snap_every")]
+                                       "forward_only", "misfit_kind", "nthreads", "snap_every", "src_kind")]
 
 
 _fp = C.POINTER(C.c_float)

@@ -563,10 +563,18 @@ int FN(image_singleshot)(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
     /* ---------------- forward ---------------- */
     for (int it = 0; it < nt; it++) {
         size_t si = IDX(isx, isz);
-        F_(TXX)[si] += io->sou[it]; /* GPUapplysource on txx and tzz, FD2DGPU.cu:2104-2114 */
-        F_(TZZ)[si] += io->sou[it];
+        if (s.src_kind == 0) {
+            F_(TXX)[si] += io->sou[it]; /* GPUapplysource on txx and tzz, FD2DGPU.cu:2104-2114 */
+            F_(TZZ)[si] += io->sou[it];
+        }
         update_v(g, F_(TXX), F_(TZZ), F_(TXZ), F_(VX), F_(VXX), F_(VXZ), F_(VZ), F_(VZX), F_(VZZ), F_(RHO), F_(DX_),
                  F_(DZ_), 1);
+        /* vertical force (no reference counterpart): like the reference's
+         * stress source it goes into the total field only, here vz after the
+         * velocity sweep, so the stress sweep, the records, the edge strips
+         * and the snapshots of this step see it and the next velocity sweep
+         * (which rebuilds vz from its split parts) does not */
+        if (s.src_kind == 1) F_(VZ)[si] += io->sou[it];
         update_s(g, F_(TXX), F_(TZZ), F_(TXXX), F_(TXXZ), F_(TZZX), F_(TZZZ), F_(TXZ), F_(TXZX), F_(TXZZ), F_(VX),
                  F_(VZ), F_(LAM), F_(MU), F_(DX_), F_(DZ_), 1, NULL, NULL, NULL, NULL);
         if (s.stage == 2) { /* born_modeling(+1, 1), sfwi-stage2/FD2DGPU.cu:1818-1843 */

@@ -36,6 +36,9 @@ typedef struct {
     int nthreads;         /* OpenMP threads for the emulated launches / loops (<=0: all) */
     int snap_every;       /* oracle only: 0 = reconstruction (as the reference); k > 0 = image
                              from exact forward snapshots of vx, vz every k-th step, weight k */
+    int src_kind;         /* oracle only: 0 = sou[it] added to txx and tzz before the velocity
+                             sweep (as the reference); 1 = vertical force, sou[it] added to vz
+                             after the velocity sweep */
 } sfwi_oracle_shot;
 
 typedef struct {

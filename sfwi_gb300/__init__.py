@@ -256,6 +256,11 @@ class FD2DGPU_ELASTIC:
             shape = TILE_SHAPES.index(shape)
         _lib.check(_lib.load().sfwi_set_tile_shape(self._h, int(shape)))
 
+    def set_source(self, kind):
+        """Source of the forward sweeps: SOURCE_TXX_TZZ (the reference's
+        stress source, default) or SOURCE_VZ_FORCE (vertical force)."""
+        _lib.check(_lib.load().sfwi_set_source(self._h, int(kind)))
+
     def set_launch_overlap(self, on=True):
         """Programmatic dependent launch of the time-step kernels (default on)."""
         _lib.check(_lib.load().sfwi_set_launch_overlap(self._h, int(bool(on))))
@@ -318,6 +323,7 @@ def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
 
 
 SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
+SOURCE_TXX_TZZ, SOURCE_VZ_FORCE = 0, 1
 # tile shapes of the step kernels in SFWI_TILE_* order: core cells x by z,
 # and "x3" for three one-stage CTAs per SM
 TILE_SHAPES = ["16x32", "32x32", "16x64", "16x32x3"]

@@ -82,6 +82,9 @@ struct alignas(16) TileRec {
     int pad[2];
 };
 static_assert(sizeof(TileRec) == 64, "TileRec is four 16-byte words");
+// source kinds: sou[it] into txx and tzz ahead of the velocity sweep (the
+// reference's), or a vertical force, sou[it] into vz after it
+enum SourceKind : int { SRC_TXX_TZZ = 0, SRC_VZ_FORCE = 1 };
 enum TileFlags : int {
     TILE_FRAME = 1,      // intersects the PML frame (damping != 0 somewhere)
     TILE_STRIP = 2,      // core or halo touches an edge strip
@@ -131,6 +134,7 @@ struct Params {
     int *err;                   // set to a nonzero code when a bounded device wait gives up
     int *counters;              // tile counters, one per (time step, kernel): counters[4*it + kernel]
     int overlap;                // host side: launch step kernels with programmatic dependent launch
+    int src_kind;               // SRC_TXX_TZZ (the reference's) or SRC_VZ_FORCE
 };
 
 // Edge strips of vx and vz saved each forward step and restored in the

@@ -161,6 +161,7 @@ struct sfwi_handle {
     float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
     bool use_graphs = true;
     bool launch_overlap = true;  // programmatic dependent launch of the step kernels
+    int src_kind = SRC_TXX_TZZ;  // source: the reference's txx+tzz, or a vertical force
     bool last_forward_only = false;
     const TileVariant *tv = nullptr;  // tile shape of the step kernels
     // trial models of a line search: while set, shots cut their windows from
@@ -417,6 +418,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     Params p{};
     p.overlap = h->launch_overlap ? 1 : 0;
+    p.src_kind = h->src_kind;
     p.X = b.X;
     p.P = b.P;
     p.nzpml = h->nzpml;
@@ -567,7 +569,7 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, h->snap_every, h->snap_fmt,
-                                (long long)(uintptr_t)h->tv, h->launch_overlap,
+                                (long long)(uintptr_t)h->tv, h->launch_overlap, h->src_kind,
                                 (long long)(uintptr_t)b.snap.p, (long long)(uintptr_t)b.sscale.p, b.nshots, b.ntiles,
                                 b.X, b.P,
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
@@ -1434,6 +1436,13 @@ int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     }
     if (choice) *choice = pick;
     return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_set_source(sfwi_handle *h, int kind) {
+    if (int rc = check(h)) return rc;
+    if (kind != SFWI_SOURCE_TXX_TZZ && kind != SFWI_SOURCE_VZ_FORCE) return fail(SFWI_E_ARG, "unknown source kind %d", kind);
+    h->src_kind = kind == SFWI_SOURCE_VZ_FORCE ? SRC_VZ_FORCE : SRC_TXX_TZZ;
+    return SFWI_OK;
 }
 
 int sfwi_set_launch_overlap(sfwi_handle *h, int on) {

@@ -668,7 +668,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
         const float *core = s + S::NB * BOX;
-        if ((c.t.flags & TILE_SOURCE) && threadIdx.x == 0) {
+        if (p.src_kind == SRC_TXX_TZZ && (c.t.flags & TILE_SOURCE) && threadIdx.x == 0) {
             // explosive source into the total txx and tzz (seen by this sweep only)
             const int r = c.g.isx - (c.t.x0 - HALO), cc = c.g.isz - c.bcol;
             const float sv = p.sou[it];
@@ -725,11 +725,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             // scale of this step's snapshot: max |v| over the shot (the bits of
             // non-negative floats order as unsigned integers)
             float mx = 0.f, mz = 0.f;
+            // a vertical force enters vz after this sweep: the source cell's
+            // snapshot value includes it
+            const bool fsrc = p.src_kind == SRC_VZ_FORCE && (c.t.flags & TILE_SOURCE) && m.lx == c.g.isx;
 #pragma unroll
             for (int j = 0; j < 4; j++)
                 if (m.ok[j]) {
                     mx = fmaxf(mx, fabsf(bg.vx[j]));
-                    mz = fmaxf(mz, fabsf(bg.vz[j]));
+                    mz = fmaxf(mz, fabsf(fsrc && m.lz + j == c.g.isz ? bg.vz[j] + p.sou[it] : bg.vz[j]));
                 }
             const unsigned am = __activemask();
             const unsigned rx = __reduce_max_sync(am, __float_as_uint(mx));
@@ -785,6 +788,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         const float *s_vx = s, *s_vz = s + BOX;
         const float *b_vx = s + 2 * BOX, *b_vz = s + 3 * BOX;
         const float *core = s + S::NB * BOX;
+        if (p.src_kind == SRC_VZ_FORCE && (c.t.flags & TILE_SOURCE)) {
+            // vertical force into the total vz: this sweep, the records, the
+            // strips and the snapshot of this step see it
+            if (threadIdx.x == 0) s[BOX + (c.g.isx - (c.t.x0 - HALO)) * BZ + (c.g.isz - c.bcol)] += p.sou[it];
+            consumer_sync();
+        }
         const CellMap m = cell_map(p, c.t, c.g);
         const bool frame = c.t.flags & TILE_FRAME;
         // receiver row: the velocities at column igz of this tile's core rows,

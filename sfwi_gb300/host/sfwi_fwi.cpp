@@ -1,7 +1,7 @@
 // sfwi_fwi.cpp — the stage-1 and stage-2 inversion drivers on one GPU.
 //
 //   sfwi_fwi <para_file> [--stage 1|2] [--iters N] [--misfit l2|ot|ot_power|ot_alltrace]
-//            [--snapshots K f32|f16|bf16] [--gradient-only]
+//            [--snapshots K f32|f16|bf16] [--source txx_tzz|vz] [--gradient-only]
 //
 // The reference runs these as MPI programs (sfwi-stage1/main.cpp,
 // sfwi-stage2/main.cpp): a master hands shots to one worker per GPU, each
@@ -110,8 +110,9 @@ struct Shot {
 
 int main(int argc, char **argv) {
     if (argc < 2) die("usage: sfwi_fwi <para_file> [--stage 1|2] [--iters N] [--misfit l2|ot|...] "
-                      "[--snapshots K f32|f16|bf16] [--gradient-only]");
+                      "[--snapshots K f32|f16|bf16] [--source txx_tzz|vz] [--gradient-only]");
     int stage = 1, iters = -1, misfit_kind = SFWI_MISFIT_L2, snap_k = 0, snap_fmt = SFWI_SNAP_F16;
+    int source = SFWI_SOURCE_TXX_TZZ;
     bool gradient_only = false;
     for (int i = 2; i < argc; i++) {
         if (!std::strcmp(argv[i], "--stage") && i + 1 < argc)
@@ -128,6 +129,14 @@ int main(int argc, char **argv) {
             snap_k = std::atoi(argv[++i]);
             const char *f = argv[++i];
             snap_fmt = !std::strcmp(f, "f32") ? SFWI_SNAP_F32 : !std::strcmp(f, "bf16") ? SFWI_SNAP_BF16 : SFWI_SNAP_F16;
+        } else if (!std::strcmp(argv[i], "--source") && i + 1 < argc) {
+            const char *k = argv[++i];
+            if (!std::strcmp(k, "vz"))
+                source = SFWI_SOURCE_VZ_FORCE;
+            else if (!std::strcmp(k, "txx_tzz"))
+                source = SFWI_SOURCE_TXX_TZZ;
+            else
+                die("--source must be txx_tzz or vz");
         } else if (!std::strcmp(argv[i], "--gradient-only"))
             gradient_only = true;
         else
@@ -191,6 +200,7 @@ int main(int argc, char **argv) {
           "sfwi_create");
     check(sfwi_set_misfit(h, misfit_kind), "misfit");
     if (snap_k > 0) check(sfwi_set_snapshots(h, snap_k, snap_fmt), "snapshots");
+    check(sfwi_set_source(h, source), "source");
 
     std::vector<float> grad_pp(n), grad_ps(n), illum(n), cg_pp(n), cg_ps(n), cg_pp_old(n, 0.f), cg_ps_old(n, 0.f);
     std::vector<float> image_pp(n, 0.f), image_ps(n, 0.f);  // stage 2: model perturbation

@@ -214,6 +214,15 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
  * gradients, already read or accumulated, are untouched). */
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
 
+/* Failure path of the device-side waits, without a fault: runs the tile
+ * pipeline of the last batch with a producer that stages nothing and a wait
+ * bound of `tries` (1..2^24) mbarrier tries, so the consumers' and the
+ * producer's waits run out.  The kernel sets the device error flag and
+ * returns, and the call reports it as a run does: SFWI_E_CUDA with "a
+ * device-side pipeline wait timed out".  The flag is cleared afterwards and
+ * the handle stays usable. */
+int sfwi_wait_selftest(sfwi_handle *h, unsigned tries);
+
 /* Source of the forward sweeps.  SFWI_SOURCE_TXX_TZZ (default) is the
  * reference's: sou[it] added to txx and tzz at the source cell ahead of the
  * velocity sweep (sfwi-stage1/FD2DGPU.cu:2104-2114).  SFWI_SOURCE_VZ_FORCE is

@@ -256,6 +256,12 @@ class FD2DGPU_ELASTIC:
             shape = TILE_SHAPES.index(shape)
         _lib.check(_lib.load().sfwi_set_tile_shape(self._h, int(shape)))
 
+    def wait_selftest(self, tries=4096):
+        """Make the device-side pipeline waits of the last batch's tile
+        pipeline run out (bounded, no fault); raises SfwiError carrying the
+        timeout report a real run would give."""
+        _lib.check(_lib.load().sfwi_wait_selftest(self._h, int(tries)))
+
     def set_source(self, kind):
         """Source of the forward sweeps: SOURCE_TXX_TZZ (the reference's
         stress source, default) or SOURCE_VZ_FORCE (vertical force)."""

@@ -135,7 +135,11 @@ struct Params {
     int *counters;              // tile counters, one per (time step, kernel): counters[4*it + kernel]
     int overlap;                // host side: launch step kernels with programmatic dependent launch
     int src_kind;               // SRC_TXX_TZZ (the reference's) or SRC_VZ_FORCE
+    unsigned wait_limit;        // tries of a pipeline mbarrier wait before it is declared lost
 };
+// tries of mbarrier.try_wait before a pipeline wait is declared lost (each try
+// may suspend the thread for a while; the bound is several seconds)
+constexpr unsigned PIPE_WAIT_LIMIT = 1u << 24;
 
 // Edge strips of vx and vz saved each forward step and restored in the
 // backward step (the reference's record_edge_wavefield/load_edge_wavefield,

@@ -418,6 +418,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     Params p{};
     p.overlap = h->launch_overlap ? 1 : 0;
+    p.wait_limit = PIPE_WAIT_LIMIT;
     p.src_kind = h->src_kind;
     p.X = b.X;
     p.P = b.P;
@@ -1436,6 +1437,28 @@ int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     }
     if (choice) *choice = pick;
     return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_wait_selftest(sfwi_handle *h, unsigned tries) {
+    if (int rc = check(h)) return rc;
+    if (tries < 1 || tries > PIPE_WAIT_LIMIT) return fail(SFWI_E_ARG, "tries must be in 1..%u", PIPE_WAIT_LIMIT);
+    Batch &b = h->b;
+    if (b.ntiles < 4 || !b.grid.p) return fail(SFWI_E_STATE, "run a batch of at least 4 tiles first");
+    CK(cudaSetDevice(h->device));
+    Params p = make_params(h, h->last_forward_only);
+    p.wait_limit = tries;
+    CK(cudaMemsetAsync(b.dctr.p, 0, sizeof(int), h->st));
+    CK(cudaMemsetAsync(b.derr.p, 0, sizeof(int), h->st));
+    h->tv->wait_probe(p, h->st);
+    h->launches++;
+    CK(cudaGetLastError());
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaMemsetAsync(b.derr.p, 0, sizeof(int), h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
+    return fail(SFWI_E_STATE, "the wait probe completed without a timeout");
 }
 
 int sfwi_set_source(sfwi_handle *h, int kind) {

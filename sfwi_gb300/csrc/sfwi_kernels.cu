@@ -69,9 +69,6 @@ constexpr float K4 = (float)(-5.0 / 7168.0);
 constexpr int NSTAGE = SFWI_STAGES;
 constexpr int CORE = TX * TZ;  // floats of a core tile
 constexpr uint32_t BOX_BYTES = BOX * 4u, CORE_BYTES = CORE * 4u;
-// iterations of mbarrier.try_wait before a wait is declared lost (each try
-// may suspend the thread for a while; the bound is several seconds)
-constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 // ----------------------------------------------------------------------------
 // TMA / mbarrier primitives
@@ -123,9 +120,9 @@ __device__ __forceinline__ bool consumer_any(bool v) {
         : "memory");
     return r != 0;
 }
-// bounded wait: false when the phase did not complete within WAIT_LIMIT tries
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++)
+// bounded wait: false when the phase did not complete within `limit` tries
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -557,7 +554,7 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
         griddep_wait();
         for (int k = 0;; k++) {
             const int s = k % NSTAGE;
-            if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1))) {
+            if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1), p.wait_limit)) {
                 atomicExch(p.err, 2);
                 return;  // consumers give up on full[s] the same way
             }
@@ -579,12 +576,12 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
     griddep_wait();
     for (int k = 0;; k++) {
         const int s = k % NSTAGE;
-        const bool ok = mbar_wait(&full[s], (uint32_t)((k / NSTAGE) & 1));
+        const bool ok = mbar_wait(&full[s], (uint32_t)((k / NSTAGE) & 1), p.wait_limit);
         if (consumer_any(!ok)) {
             if (threadIdx.x == 0) {
                 atomicExch(p.err, 1);
                 // the other stage may still be loading: let it land (bounded)
-                if (NSTAGE > 1) mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1));
+                if (NSTAGE > 1) mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1), p.wait_limit);
             }
             return;
         }
@@ -1520,6 +1517,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 }
 
 // ---------------------------------------------------------------------------
+// wait probe: the tile pipeline with a producer that stages nothing, so every
+// consumer's wait on its first stage runs out after p.wait_limit tries and the
+// producer's wait for a free stage does too.  Both set the error flag and
+// return (nothing is in flight); the host reads the flag as it does after a
+// real run.  It exercises the failure path of the bounded waits without a
+// fault, a trap or an unbounded spin.
+// ---------------------------------------------------------------------------
+constexpr int PROBE_STAGE = 32;
+__global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM) k_wait_probe(const Params p) {
+    auto issue = [&](const TileCtx &, float *, uint64_t *) {};
+    auto body = [&](const TileCtx &, float *, StageRelease &) {};
+    run_tiles<PROBE_STAGE>(p, p.counters, issue, body);
+}
+
+// ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
 constexpr size_t SMEM_ALIGN_SLACK = 1024;
@@ -1581,6 +1593,12 @@ static void launch_step(void (*k)(KArgs...), size_t smem, const Params &p, cudaS
     cudaLaunchKernelEx(&cfg, k, p, args...);
 }
 
+// one CTA; with p.ntiles >= 4 its producer draws real tiles (it reads their
+// records) until it waits for a free stage
+void launch_wait_probe(const Params &p, cudaStream_t st) {
+    k_wait_probe<<<1, BLOCK_THREADS, NSTAGE * PROBE_STAGE * sizeof(float) + SMEM_ALIGN_SLACK, st>>>(p);
+}
+
 void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
                         cudaStream_t st) {
     switch (which) {
@@ -1622,7 +1640,8 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
 #define SFWI_STR(x) SFWI_STR2(x)
 const TileVariant *SFWI_VARIANT_FN() {
     static const TileVariant v{TX, TZ, HALO, CTAS_PER_SM, SFWI_VARIANT_NS::NSTAGE, SFWI_STR(SFWI_VARIANT_NS),
-                               &SFWI_VARIANT_NS::configure_step_kernels, &SFWI_VARIANT_NS::launch_step_kernel};
+                               &SFWI_VARIANT_NS::configure_step_kernels, &SFWI_VARIANT_NS::launch_step_kernel,
+                               &SFWI_VARIANT_NS::launch_wait_probe};
     return &v;
 }
 

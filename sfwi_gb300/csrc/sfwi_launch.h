@@ -28,6 +28,7 @@ struct TileVariant {
     const char *name;
     cudaError_t (*configure)();
     void (*launch)(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir, cudaStream_t st);
+    void (*wait_probe)(const Params &p, cudaStream_t st);
 };
 const TileVariant *tile_variant_16x32();
 const TileVariant *tile_variant_32x32();

@@ -665,14 +665,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         float *s_xx = s, *s_zz = s + BOX, *s_xz = s + 2 * BOX;
         const float *core = s + S::NB * BOX;
-        if (p.src_kind == SRC_TXX_TZZ && (c.t.flags & TILE_SOURCE) && threadIdx.x == 0) {
-            // explosive source into the total txx and tzz (seen by this sweep only)
-            const int r = c.g.isx - (c.t.x0 - HALO), cc = c.g.isz - c.bcol;
-            const float sv = p.sou[it];
-            s_xx[r * BZ + cc] += sv;
-            s_zz[r * BZ + cc] += sv;
+        // (tile flags are the same for every consumer thread, so the barrier
+        // below is taken by all of them or by none)
+        if (p.src_kind == SRC_TXX_TZZ && (c.t.flags & TILE_SOURCE)) {
+            if (threadIdx.x == 0) {
+                // explosive source into the total txx and tzz (seen by this sweep only)
+                const int r = c.g.isx - (c.t.x0 - HALO), cc = c.g.isz - c.bcol;
+                const float sv = p.sou[it];
+                s_xx[r * BZ + cc] += sv;
+                s_zz[r * BZ + cc] += sv;
+            }
+            consumer_sync();
         }
-        consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
@@ -1152,7 +1156,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             }
         }
         if (c.t.flags & TILE_RECV) patch_residual(c, s + S::RS, it, a_vx, a_vz);
-        consumer_sync();
+        // the views were patched: every consumer thread (same flags) waits
+        if (c.t.flags & (TILE_STRIP | TILE_RECV)) consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
@@ -1405,7 +1410,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
             for (int i = threadIdx.x; i < 2 * BOX; i += NTHREADS) sv[i] = from16(raw[i], FMT) * sc[i >= BOX];
         }
-        consumer_sync();
+        // views written by other threads: every consumer thread (same flags) waits
+        if ((c.t.flags & TILE_RECV) || (FMT != SNAP_F32 && img)) consumer_sync();
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;

@@ -222,6 +222,45 @@ def cpu_baseline_sample(w, data, nthreads, nt_sample, kind="port"):
     return 1.0 / per_shot, el
 
 
+def reference_gpu_sample(w, data, nshots):
+    """The reference's own CUDA kernels (oracle/ref_gpu_harness.cpp) on this
+    GPU, one shot at a time as the reference runs them: `nshots` shots of the
+    workload at the full nt, wall-clock per shot including the per-shot
+    allocations and copies the reference makes.  Its misfit is L2 (the
+    reference has no OT)."""
+    from oracle import pyoracle as po
+    stage = w.get("stage", 2)
+    try:
+        if not po.build_refgpu() or not po.available("gpu%d" % stage):
+            return {"unavailable": "the reference's device-code modules are not in oracle/_ref"}
+        po.load("gpu%d" % stage)
+    except Exception as e:  # noqa: BLE001 - reported, not fatal
+        return {"unavailable": "reference GPU harness: %s" % e}
+    shots = data["shots"]
+    pick = shots[:: max(1, len(shots) // nshots)][:nshots]
+    rng = np.random.default_rng(0)
+    els = []
+    for j, d in enumerate(pick[:1] + pick):  # the first run is a warm-up
+        shot = dict(stage=stage, allnx=w["allnx"], allnz=w["allnz"], nx=d["nx"], pml=w["pml"], nop=4, nt=w["nt"],
+                    ntr=d["ntr"], dx=w["dx"], dz=w["dx"], dt=w["dt"], isx=d["isx"], isz=w["pml"] + w["sy"],
+                    igz=w["pml"] + w["gy"], ngx_left=d["ngx_left"], delta_left=d["delta_left"], record_left_in_v=0,
+                    forward_only=0, misfit_kind=0, nthreads=0)
+        model = dict(vp=data["vp0"], vs=data["vs0"], rho=data["rho0"], dvp=data["dvp"], dvs=data["dvs"],
+                     sou=data["sou"], gc=d["gc"],
+                     obs_z=(1e-9 * rng.standard_normal((d["ntr"], w["nt"]))).astype(np.float32),
+                     obs_x=(1e-9 * rng.standard_normal((d["ntr"], w["nt"]))).astype(np.float32))
+        t = time.perf_counter()
+        po.run_shot("gpu%d" % stage, shot, model)
+        if j > 0:
+            els.append(time.perf_counter() - t)
+    per = float(np.mean(els))
+    return {"value": round(1.0 / per, 3), "unit": "shot-gradients/s", "ms_per_shot": round(per * 1e3, 1),
+            "shots_sampled": len(els),
+            "sample": "the reference's CUDA kernels (its born.cu and FD2DGPU.cu kernels, nvcc -O3 for sm_103a, "
+                      "64-register cap) in IMAGE_SINGLESHOT's launch sequence, one shot at a time, L2 misfit, "
+                      "wall clock per shot"}
+
+
 def run_serving(n, budget_gb=64.0, slots=4):
     """Serving loop on a seeded Poisson stream (50 requests/s; grids, nt and
     shots drawn from the serving configuration's ranges, then scaled by 0.3 in
@@ -293,6 +332,8 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=48, help="requests of the serving-loop measurement")
     ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
+    ap.add_argument("--reference-gpu-shots", type=int, default=1,
+                    help="shots of the reference's own CUDA path timed on this GPU (0: skip)")
     ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or a name in sfwi_gb300.TILE_SHAPES")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
@@ -465,6 +506,11 @@ def main():
         for fmt in ("f16", "bf16"):
             snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
                              for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
+    ref_gpu = None
+    if rank == 0 and args.reference_gpu_shots > 0 and not w.get("snap"):
+        ref_gpu = reference_gpu_sample(w, data, args.reference_gpu_shots)
+        if "value" in ref_gpu:
+            ref_gpu["batched_over_reference_gpu"] = round(value / ref_gpu["value"], 1)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, el = cpu_baseline_sample(w, data, 1, min(nt, 1000), "port")
@@ -493,6 +539,7 @@ def main():
             "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving, "snapshot_error": snap_err,
+            "reference_gpu": ref_gpu,
             "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2),
                          "misfit": round(float(np.mean(mis_ms)), 2)}}
     print(json.dumps(line), flush=True)

@@ -9,6 +9,11 @@ oracle/_ref where the reference sources are mounted):
   "f32"  oracle/lib/liboracle32.so  FP32 transliteration (same source)
   "ref1" oracle/_ref/libsfwi_ref_s1.so  the reference's stage-1 kernels on the CPU
   "ref2" oracle/_ref/libsfwi_ref_s2.so  the reference's stage-2 kernels on the CPU
+  "gpu1" oracle/_ref/libsfwi_refgpu_s1.so  the reference's stage-1 kernels on the GPU
+  "gpu2" oracle/_ref/libsfwi_refgpu_s2.so  the reference's stage-2 kernels on the GPU
+The "gpu" libraries are built on the GPU machine by build_refgpu() from
+oracle/ref_gpu_harness.cpp and the device-code modules that oracle/ref_build.py
+left in oracle/_ref.
 """
 import ctypes as C
 import os
@@ -25,8 +30,36 @@ _PATHS = {
     "f32": os.path.join(LIBDIR, "liboracle32.so"),
     "ref1": os.path.join(REFDIR, "libsfwi_ref_s1.so"),
     "ref2": os.path.join(REFDIR, "libsfwi_ref_s2.so"),
+    "gpu1": os.path.join(REFDIR, "libsfwi_refgpu_s1.so"),
+    "gpu2": os.path.join(REFDIR, "libsfwi_refgpu_s2.so"),
 }
-_PREFIX = {"f64": "orc64_", "f32": "orc32_", "ref1": "sfwi_ref_", "ref2": "sfwi_ref_"}
+_PREFIX = {"f64": "orc64_", "f32": "orc32_", "ref1": "sfwi_ref_", "ref2": "sfwi_ref_", "gpu1": "sfwi_refgpu_",
+           "gpu2": "sfwi_refgpu_"}
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def refgpu_modules_present():
+    return all(os.path.exists(os.path.join(REFDIR, f % st)) for st in (1, 2)
+               for f in ("ref_born_s%d.cubin", "ref_fdk_s%d.cubin", "ref_kernels_s%d.txt"))
+
+
+def build_refgpu(force=False):
+    """Compile oracle/ref_gpu_harness.cpp into oracle/_ref/libsfwi_refgpu_s{1,2}.so
+    where the reference's device-code modules are present; returns whether
+    both libraries exist afterwards."""
+    if not refgpu_modules_present():
+        return False
+    src = os.path.join(HERE, "ref_gpu_harness.cpp")
+    deps = [src, os.path.join(HERE, "ref_sequence.inc"), os.path.join(HERE, "sfwi_oracle.h")]
+    for st in (1, 2):
+        out = _PATHS["gpu%d" % st]
+        if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+            continue
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-DSFWI_STAGE=%d" % st, "-I", HERE,
+                        "-I", os.path.join(CUDA_HOME, "include"), src, "-o", out,
+                        "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart_static", "-ldl", "-lpthread", "-lrt",
+                        "-L", os.path.join(CUDA_HOME, "lib64", "stubs"), "-lcuda"], check=True)
+    return all(os.path.exists(_PATHS["gpu%d" % st]) for st in (1, 2))
 
 
 class Shot(C.Structure):
@@ -74,6 +107,11 @@ def load(kind):
         f = getattr(lib, _PREFIX[kind] + "image_singleshot")
         f.argtypes = [C.POINTER(Shot), C.POINTER(IO)]
         f.restype = C.c_int
+        if kind.startswith("gpu"):
+            lib.sfwi_refgpu_error.restype = C.c_char_p
+            lib.sfwi_refgpu_init.argtypes = [C.c_char_p]
+            if lib.sfwi_refgpu_init(REFDIR.encode()) != 0:
+                raise RuntimeError("reference GPU kernels: %s" % lib.sfwi_refgpu_error().decode())
         _LIBS[kind] = lib
     return _LIBS[kind]
 
@@ -134,7 +172,8 @@ def run_shot(kind, shot, model, want_rho=False):
         setattr(io, k, _p(v, C.c_double))
     rc = getattr(lib, _PREFIX[kind] + "image_singleshot")(C.byref(s), C.byref(io))
     if rc != 0:
-        raise RuntimeError("%s image_singleshot returned %d" % (kind, rc))
+        why = lib.sfwi_refgpu_error().decode() if kind.startswith("gpu") else ""
+        raise RuntimeError("%s image_singleshot returned %d %s" % (kind, rc, why))
     out["misfit"] = float(misfit[0])
     return out
 

@@ -6,7 +6,8 @@
  * sfwi-stage{1,2}/FD2DGPU.cu), all built as host C++ through oracle/cuda_shim.
  * The result, oracle/_ref/libsfwi_ref_s{1,2}.so, runs the reference's
  * arithmetic on the CPU so the restatement in sfwi_oracle.c can be pinned to
- * it.  Only the launch sequence below is written here; every cell update is
+ * it.  Only the launch sequence (oracle/ref_sequence.inc, shared with the GPU
+ * build in oracle/ref_gpu_harness.cpp) is written here; every cell update is
  * the reference's own code.
  *
  * The sequence restates IMAGE_SINGLESHOT:
@@ -28,6 +29,7 @@
 #error "SFWI_STAGE must be 1 or 2"
 #endif
 
+#include <algorithm>
 #include <vector>
 #include <cstdint>
 #include "sfwi_oracle.h"
@@ -64,263 +66,32 @@ void launch(dim3 grid, dim3 block, F &&body) {
     }
 }
 
-struct Dev {
-    std::vector<float> v;
-    explicit Dev(size_t n = 0) : v(n, 0.0f) {}
-    float *p() { return v.data(); }
+// arrays of the emulated device (zero-filled, as the reference memsets them)
+template <class T>
+struct Arr {
+    std::vector<T> v;
+    explicit Arr(size_t n = 0) : v(n, T(0)) {}
+    T *p() { return v.data(); }
+    void upload(const T *h, size_t n) { std::copy(h, h + n, v.begin()); }
+    std::vector<T> host() const { return v; }
 };
+typedef Arr<float> Dev;
+typedef Arr<int> IDev;
 
 } // namespace
 
 extern "C" int sfwi_ref_stage(void) { return SFWI_STAGE; }
 
-extern "C" int sfwi_ref_image_singleshot(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
-    const sfwi_oracle_shot s = *sp;
-    if (s.stage != SFWI_STAGE) return -1;
-    if (s.misfit_kind != 0) return -2; /* the reference's live misfit is L2 only */
+#define REF_LAUNCH(grid, block, kernel, ...) launch(grid, block, [&] { kernel(__VA_ARGS__); })
 #ifdef _OPENMP
-    if (s.nthreads > 0) omp_set_num_threads(s.nthreads);
-#endif
-    const int pml = s.pml, nop = s.nop, nt = s.nt, ntr = s.ntr;
-    const int nx = s.nx, nz = s.allnz;
-    const int nxpml = nx + 2 * pml, nzpml = nz + 2 * pml;
-    const int allnx = s.allnx, allnz = s.allnz;
-    const float dx = s.dx, dz = s.dz, dt = s.dt;
-    const size_t nDim = (size_t)nxpml * nzpml, nxnz = (size_t)allnx * allnz;
-    const int N = nop;
-
-    const dim3 GB_grid((nzpml + 31) / 32, (nxpml + 31) / 32), GB_block(32, 32);
-    const dim3 IM_grid((nz + 31) / 32, (nx + 31) / 32), IM_block(32, 32);
-    const dim3 TR_grid((ntr + 31) / 32), TR_block(32);
-    const dim3 SB_grid((nt + 31) / 32, (ntr + 31) / 32), SB_block(32, 32);
-
-    /* global arrays */
-    Dev vel(nxnz), vel_s(nxnz), rho_all(nxnz), image_pp_m(nxnz), image_ps_m(nxnz);
-    Dev pp_gradient(nxnz), ps_gradient(nxnz), denom(nxnz);
-    /* window / material arrays */
-    Dev vp(nDim), vs(nDim), d_rho(nDim), lamda(nDim), miu(nDim), d_damp(nDim), d_dampz(nDim);
-    Dev s_image_pp_m(nDim), s_image_ps_m(nDim);
-    /* background */
-    Dev vx(nDim), vz(nDim), vx_x(nDim), vx_z(nDim), vz_x(nDim), vz_z(nDim);
-    Dev txx(nDim), tzz(nDim), txz(nDim), txx_x(nDim), txx_z(nDim), tzz_x(nDim), tzz_z(nDim), txz_x(nDim), txz_z(nDim);
-    /* scattered */
-    Dev b_vx(nDim), b_vz(nDim), b_vx_x(nDim), b_vx_z(nDim), b_vz_x(nDim), b_vz_z(nDim);
-    Dev b_txx(nDim), b_tzz(nDim), b_txz(nDim), b_txx_x(nDim), b_txx_z(nDim), b_tzz_x(nDim), b_tzz_z(nDim),
-        b_txz_x(nDim), b_txz_z(nDim);
-    /* adjoint */
-    Dev vx_bk(nDim), vz_bk(nDim), vx_x_bk(nDim), vx_z_bk(nDim), vz_x_bk(nDim), vz_z_bk(nDim);
-    Dev txx_bk(nDim), tzz_bk(nDim), txz_bk(nDim), txx_x_bk(nDim), txx_z_bk(nDim), tzz_x_bk(nDim), tzz_z_bk(nDim),
-        txz_x_bk(nDim), txz_z_bk(nDim);
-    /* strains */
-    Dev vx_gx(nDim), vz_gz(nDim), vx_gz(nDim), vz_gx(nDim);
-    /* records */
-    const size_t nrec = (size_t)ntr * nt;
-    Dev rec_z(nrec), rec_x(nrec), sc_z(nrec), sc_x(nrec), sc2_z(nrec), sc2_x(nrec);
-    std::vector<int> gc(ntr);
-    Dev source(nt);
-    /* edge strips (vx stands in for omega, vz for theta) */
-    const size_t nud = (size_t)2 * N * nx * nt, nlr = (size_t)2 * nz * N * nt;
-    Dev om_up(nud), th_up(nud), om_dn(nud), th_dn(nud), om_l(nlr), th_l(nlr), om_r(nlr), th_r(nlr);
-
-    /* host -> "device" copies (GPUbufferVPVS, GPUbufferM, record_copytoGPU, ctor source copy) */
-    for (size_t i = 0; i < nxnz; ++i) {
-        vel.v[i] = io->vp_all[i];
-        vel_s.v[i] = io->vs_all[i];
-        if (SFWI_STAGE == 1) rho_all.v[i] = io->rho_all[i];
-        if (SFWI_STAGE == 2) {
-            image_pp_m.v[i] = io->dvp_all ? io->dvp_all[i] : 0.0f;
-            image_ps_m.v[i] = io->dvs_all ? io->dvs_all[i] : 0.0f;
-        }
-    }
-    for (int i = 0; i < nt; ++i) source.v[i] = io->sou[i];
-    for (int i = 0; i < ntr; ++i) gc[i] = io->gc[i];
-    if (!s.forward_only) {
-        for (size_t i = 0; i < nrec; ++i) {
-            rec_z.v[i] = io->obs_z[i];
-            rec_x.v[i] = io->obs_x[i];
-        }
-    }
-
-    /* bufferVpVsHtoD(delta_left + record_left_in_v) */
-    const int ngx_min = s.delta_left + s.record_left_in_v;
-    launch(GB_grid, GB_block, [&] { copyvelocityHtoD(vel.p(), vp.p(), pml, nzpml, ngx_min, allnz, nx, nz); });
-    launch(GB_grid, GB_block, [&] { copyvelocityHtoD(vel_s.p(), vs.p(), pml, nzpml, ngx_min, allnz, nx, nz); });
-#if SFWI_STAGE == 1
-    launch(GB_grid, GB_block, [&] { copyvelocityHtoD(rho_all.p(), d_rho.p(), pml, nzpml, ngx_min, allnz, nx, nz); });
-#endif
-    launch(GB_grid, GB_block, [&] { copypmlVz(vp.p(), pml, nxpml, nzpml); });
-    launch(GB_grid, GB_block, [&] { copypmlVx(vp.p(), pml, nxpml, nzpml); });
-    launch(GB_grid, GB_block, [&] { copypmlVz(vs.p(), pml, nxpml, nzpml); });
-    launch(GB_grid, GB_block, [&] { copypmlVx(vs.p(), pml, nxpml, nzpml); });
-#if SFWI_STAGE == 1
-    launch(GB_grid, GB_block, [&] { copypmlVz(d_rho.p(), pml, nxpml, nzpml); });
-    launch(GB_grid, GB_block, [&] { copypmlVx(d_rho.p(), pml, nxpml, nzpml); });
-#endif
-
-    const int isx = s.isx, isz = s.isz, igz = s.igz, ngx_left = s.ngx_left;
-    const int delta_left = s.delta_left, record_left_in_v = s.record_left_in_v;
-
-#if SFWI_STAGE == 2
-    /* buffer_image_extrapolation(cmin), cmin = delta_left + record_left_in_v */
-    {
-        const int cmin = (int)(float)(delta_left + record_left_in_v);
-        launch(GB_grid, GB_block, [&] { copyvelocityHtoD(image_pp_m.p(), s_image_pp_m.p(), pml, nzpml, cmin, allnz, nx, nz); });
-        launch(GB_grid, GB_block, [&] { copyvelocityHtoD(image_ps_m.p(), s_image_ps_m.p(), pml, nzpml, cmin, allnz, nx, nz); });
-        launch(GB_grid, GB_block, [&] { copypmlVz(s_image_pp_m.p(), pml, nxpml, nzpml); });
-        launch(GB_grid, GB_block, [&] { copypmlVx(s_image_pp_m.p(), pml, nxpml, nzpml); });
-        launch(GB_grid, GB_block, [&] { copypmlVz(s_image_ps_m.p(), pml, nxpml, nzpml); });
-        launch(GB_grid, GB_block, [&] { copypmlVx(s_image_ps_m.p(), pml, nxpml, nzpml); });
-    }
-#endif
-
-    /* calculate_elastic_damp_C: the cuBLAS Isamin result only feeds the unused
-     * vmin argument, so a valid pointer is passed in its place. */
-    const float rr = 0.001f;
-    launch(GB_grid, GB_block, [&] { dampX(d_damp.p(), pml, vp.p(), vp.p(), nxpml, nzpml, dx, rr); });
-    launch(GB_grid, GB_block, [&] { dampZ(d_dampz.p(), pml, vp.p(), vp.p(), nxpml, nzpml, dz, rr); });
-    launch(GB_grid, GB_block, [&] { GPUcalculate_elastic_rho_C(d_rho.p(), vp.p(), vs.p(), lamda.p(), miu.p(), nxpml, nzpml); });
-
-    const int direction = 1, direction_rec = -1;
-#if SFWI_STAGE == 1
-    const int adj_dir = direction;     /* born_modeling(direction,8) */
+#define REF_SET_THREADS(n) \
+    do {                   \
+        if ((n) > 0) omp_set_num_threads(n); \
+    } while (0)
 #else
-    const int adj_dir = direction_rec; /* born_modeling(direction_rec,8) */
+#define REF_SET_THREADS(n) (void)(n)
 #endif
 
-    /* ---------------- forward ---------------- */
-    for (int it = 0; it < nt; ++it) {
-        launch(dim3(1), dim3(1), [&] { GPUapplysource(txx.p(), source.p(), isx, isz, nzpml, it); });
-        launch(dim3(1), dim3(1), [&] { GPUapplysource(tzz.p(), source.p(), isx, isz, nzpml, it); });
-        launch(GB_grid, GB_block, [&] {
-            update_vx_vz(txx.p(), tzz.p(), txz.p(), vx.p(), vx_x.p(), vx_z.p(), vz.p(), vz_x.p(), vz_z.p(), nxpml,
-                         nzpml, dt, dx, dz, nop, d_rho.p(), d_damp.p(), d_dampz.p(), direction);
-        });
-        launch(GB_grid, GB_block, [&] {
-            update_txx_tzz_txz(txx.p(), tzz.p(), txx_x.p(), txx_z.p(), tzz_x.p(), tzz_z.p(), txz.p(), txz_x.p(),
-                               txz_z.p(), vx.p(), vz.p(), nxpml, nzpml, dt, dx, dz, nop, lamda.p(), miu.p(),
-                               d_damp.p(), d_dampz.p(), direction);
-        });
-#if SFWI_STAGE == 2
-        launch(GB_grid, GB_block, [&] {
-            update_vx_vz(b_txx.p(), b_tzz.p(), b_txz.p(), b_vx.p(), b_vx_x.p(), b_vx_z.p(), b_vz.p(), b_vz_x.p(),
-                         b_vz_z.p(), nxpml, nzpml, dt, dx, dz, nop, d_rho.p(), d_damp.p(), d_dampz.p(), direction);
-        });
-        launch(GB_grid, GB_block, [&] {
-            add_born_source_components(vx.p(), vz.p(), b_txx_x.p(), b_txx_z.p(), b_tzz_x.p(), b_tzz_z.p(),
-                                       b_txz_x.p(), b_txz_z.p(), s_image_pp_m.p(), s_image_ps_m.p(), nxpml, nzpml,
-                                       pml, dx, dz, dt, nop, lamda.p(), miu.p(), d_rho.p(), vp.p(), vs.p(), direction);
-        });
-        launch(GB_grid, GB_block, [&] {
-            update_txx_tzz_txz(b_txx.p(), b_tzz.p(), b_txx_x.p(), b_txx_z.p(), b_tzz_x.p(), b_tzz_z.p(), b_txz.p(),
-                               b_txz_x.p(), b_txz_z.p(), b_vx.p(), b_vz.p(), nxpml, nzpml, dt, dx, dz, nop,
-                               lamda.p(), miu.p(), d_damp.p(), d_dampz.p(), direction);
-        });
-        /* record_scatter(it, true): scattered into scatter, background into scatter2 */
-        launch(TR_grid, TR_block, [&] {
-            GPUrecord_scatterwavefield(b_vz.p(), b_vx.p(), sc_z.p(), sc_x.p(), gc.data(), it, ngx_left, pml, nzpml,
-                                       ntr, (int)dx, nt, igz);
-        });
-        launch(TR_grid, TR_block, [&] {
-            GPUrecord_scatterwavefield(vz.p(), vx.p(), sc2_z.p(), sc2_x.p(), gc.data(), it, ngx_left, pml, nzpml,
-                                       ntr, (int)dx, nt, igz);
-        });
-#else
-        /* record_background_wave(it) */
-        launch(TR_grid, TR_block, [&] {
-            GPUrecord_scatterwavefield(vz.p(), vx.p(), sc_z.p(), sc_x.p(), gc.data(), it, ngx_left, pml, nzpml, ntr,
-                                       dx, nt, igz);
-        });
-#endif
-        if (!s.forward_only)
-            launch(GB_grid, GB_block, [&] {
-                record_edge_wavefield(vx.p(), vz.p(), om_up.p(), th_up.p(), om_dn.p(), th_dn.p(), om_l.p(), th_l.p(),
-                                      om_r.p(), th_r.p(), pml, nzpml, nxpml, nx, nz, N, it);
-            });
-    }
-
-    auto out_rec = [&](double *dst, Dev &src) {
-        if (dst)
-            for (size_t i = 0; i < nrec; ++i) dst[i] = src.v[i];
-    };
-    out_rec(io->syn_z, sc_z);
-    out_rec(io->syn_x, sc_x);
-#if SFWI_STAGE == 2
-    out_rec(io->syn2_z, sc2_z);
-    out_rec(io->syn2_x, sc2_x);
-#endif
-    if (s.forward_only) return 0;
-
-    /* ---------------- residual and misfit ---------------- */
-    const float scale_size = 1.0f;
-    launch(SB_grid, SB_block, [&] { GPU_subtract(sc_z.p(), sc_x.p(), rec_z.p(), rec_x.p(), nt, ntr, scale_size); });
-#if SFWI_STAGE == 2
-    launch(SB_grid, SB_block, [&] { GPU_add(sc_z.p(), sc_x.p(), sc2_z.p(), sc2_x.p(), nt, ntr, scale_size); });
-#endif
-    out_rec(io->res_z, sc_z);
-    out_rec(io->res_x, sc_x);
-    if (io->misfit) {
-        double misfit = 0.0;
-        for (int i = 0; i < ntr; i++)
-            for (int j = 0; j < nt; j++)
-                misfit += (sc_z.v[i * nt + j] * sc_z.v[i * nt + j] + sc_x.v[i * nt + j] * sc_x.v[i * nt + j]);
-        *io->misfit += misfit;
-    }
-
-    /* ---------------- backward ---------------- */
-    const bool stack = false;
-    for (int it = nt - 1; it >= 0; --it) {
-        launch(GB_grid, GB_block, [&] {
-            load_edge_wavefield(vx.p(), vz.p(), om_up.p(), th_up.p(), om_dn.p(), th_dn.p(), om_l.p(), th_l.p(),
-                                om_r.p(), th_r.p(), pml, nzpml, nxpml, nx, nz, N, it);
-        });
-        /* born_modeling(direction_rec, 6) */
-        launch(GB_grid, GB_block, [&] {
-            update_txx_tzz_txz_grad(txx.p(), tzz.p(), txx_x.p(), txx_z.p(), tzz_x.p(), tzz_z.p(), txz.p(), txz_x.p(),
-                                    txz_z.p(), vx.p(), vz.p(), vx_gx.p(), vz_gz.p(), vx_gz.p(), vz_gx.p(), nxpml,
-                                    nzpml, dt, dx, dz, nop, lamda.p(), miu.p(), d_damp.p(), d_dampz.p(),
-                                    direction_rec, pml);
-        });
-        launch(GB_grid, GB_block, [&] {
-            update_vx_vz(txx.p(), tzz.p(), txz.p(), vx.p(), vx_x.p(), vx_z.p(), vz.p(), vz_x.p(), vz_z.p(), nxpml,
-                         nzpml, dt, dx, dz, nop, d_rho.p(), d_damp.p(), d_dampz.p(), direction_rec);
-        });
-        /* elastic_rotation_addS_bac(it, 0, stack) */
-        launch(TR_grid, TR_block, [&] {
-#if SFWI_STAGE == 2
-            GPUapplysource_backward_from_record(vz_bk.p(), vx_bk.p(), sc_z.p(), sc_x.p(), gc.data(), it,
-                                                (float)ngx_left, pml, nzpml, ntr, dx, nt, dt, stack, igz);
-#else
-            GPUapplysource_backward_from_record(vz_bk.p(), vx_bk.p(), sc_z.p(), sc_x.p(), gc.data(), it,
-                                                (float)ngx_left, pml, nzpml, ntr, dx, nt, stack, igz);
-#endif
-        });
-        /* born_modeling(adj_dir, 8) */
-        launch(GB_grid, GB_block, [&] {
-            GPUcalculate_elastic_txx_tzz_txz_back(txx_bk.p(), tzz_bk.p(), txx_x_bk.p(), txx_z_bk.p(), tzz_x_bk.p(),
-                                                  tzz_z_bk.p(), txz_bk.p(), txz_x_bk.p(), txz_z_bk.p(), vx_bk.p(),
-                                                  vz_bk.p(), nxpml, nzpml, dt, dx, dz, nop, lamda.p(), miu.p(),
-                                                  d_damp.p(), d_dampz.p(), adj_dir);
-        });
-        launch(GB_grid, GB_block, [&] {
-            GPUcalculate_elastic_vx_vz_back(txx_bk.p(), tzz_bk.p(), txz_bk.p(), vx_bk.p(), vx_x_bk.p(), vx_z_bk.p(),
-                                            vz_bk.p(), vz_x_bk.p(), vz_z_bk.p(), lamda.p(), miu.p(), nxpml, nzpml,
-                                            dt, dx, dz, nop, d_rho.p(), d_damp.p(), d_dampz.p(), adj_dir);
-        });
-        /* image_gradient */
-        launch(IM_grid, IM_block, [&] {
-            doimage_gradient(pp_gradient.p(), ps_gradient.p(), vx_gx.p(), vz_gz.p(), vx_gz.p(), vz_gx.p(),
-                             txx_bk.p(), tzz_bk.p(), txz_bk.p(), vp.p(), vs.p(), d_rho.p(), nx, nz, delta_left,
-                             record_left_in_v, pml, nzpml);
-        });
-        launch(IM_grid, IM_block, [&] {
-            doimage_illum(denom.p(), vx.p(), vz.p(), nx, nz, delta_left, record_left_in_v, pml, nzpml);
-        });
-    }
-
-    for (size_t i = 0; i < nxnz; ++i) {
-        if (io->grad_pp) io->grad_pp[i] += pp_gradient.v[i];
-        if (io->grad_ps) io->grad_ps[i] += ps_gradient.v[i];
-        if (io->illum) io->illum[i] += denom.v[i];
-    }
-    return 0;
+extern "C" int sfwi_ref_image_singleshot(const sfwi_oracle_shot *sp, const sfwi_oracle_io *io) {
+#include "ref_sequence.inc"
 }

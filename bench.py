@@ -222,7 +222,7 @@ def cpu_baseline_sample(w, data, nthreads, nt_sample, kind="port"):
     return 1.0 / per_shot, el
 
 
-def reference_gpu_sample(w, data, nshots):
+def reference_gpu_sample(w, data, nshots, warm=True):
     """The reference's own CUDA kernels (oracle/ref_gpu_harness.cpp) on this
     GPU, one shot at a time as the reference runs them: `nshots` shots of the
     workload at the full nt, wall-clock per shot including the per-shot
@@ -240,7 +240,7 @@ def reference_gpu_sample(w, data, nshots):
     pick = shots[:: max(1, len(shots) // nshots)][:nshots]
     rng = np.random.default_rng(0)
     els = []
-    for j, d in enumerate(pick[:1] + pick):  # the first run is a warm-up
+    for j, d in enumerate((pick[:1] if warm else []) + pick):  # the first run is a warm-up
         shot = dict(stage=stage, allnx=w["allnx"], allnz=w["allnz"], nx=d["nx"], pml=w["pml"], nop=4, nt=w["nt"],
                     ntr=d["ntr"], dx=w["dx"], dz=w["dx"], dt=w["dt"], isx=d["isx"], isz=w["pml"] + w["sy"],
                     igz=w["pml"] + w["gy"], ngx_left=d["ngx_left"], delta_left=d["delta_left"], record_left_in_v=0,
@@ -251,7 +251,7 @@ def reference_gpu_sample(w, data, nshots):
                      obs_x=(1e-9 * rng.standard_normal((d["ntr"], w["nt"]))).astype(np.float32))
         t = time.perf_counter()
         po.run_shot("gpu%d" % stage, shot, model)
-        if j > 0:
+        if j > 0 or not warm:
             els.append(time.perf_counter() - t)
     per = float(np.mean(els))
     return {"value": round(1.0 / per, 3), "unit": "shot-gradients/s", "ms_per_shot": round(per * 1e3, 1),
@@ -334,6 +334,8 @@ def main():
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     ap.add_argument("--reference-gpu-shots", type=int, default=1,
                     help="shots of the reference's own CUDA path timed on this GPU (0: skip)")
+    ap.add_argument("--profile-reference-gpu", action="store_true",
+                    help="only run the reference's CUDA path on one shot of the workload (for ncu captures)")
     ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or a name in sfwi_gb300.TILE_SHAPES")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
@@ -344,6 +346,10 @@ def main():
         w["spacing"] = max(1, min(w["spacing"], (w["allnx"] - 1) // max(1, args.shots)))
     if args.impl == "reference":
         return run_reference_arm(args, w)
+    if args.profile_reference_gpu:
+        r = reference_gpu_sample(w, build_workload(w), 1, warm=False)
+        log("reference GPU: %s" % r)
+        return 0 if "value" in r else 1
 
     ws, rank = dist_info()
     pg = None

@@ -473,21 +473,30 @@ def main():
     alg_bytes_step = w.get("pass_bytes", PASS_BYTES_PER_CELL_STEP) * cells * nt
 
     # plain form: the same engine, one shot per run (the reference's per-shot
-    # call pattern), device-timed on an evenly spread sample of the shots
+    # call pattern), device-timed on an evenly spread sample of the shots,
+    # with the tile shape the autotuner picks for a one-shot batch
     plain = None
     if args.plain_shots > 0:
         pick = shots[:: max(1, len(shots) // args.plain_shots)][: args.plain_shots]
         plain_ms = []
+        batch_tile = fd.tile_shape()
+        plain_tile = None
         for j, d in enumerate(pick[:1] + pick):  # the first run warms the one-shot graph shape
             i = shots.index(d)
             fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[i][0].array,
                             obs[i][1].array)
             fd.run()
-            if j > 0:
+            if j == 0:
+                plain_tile = fd.autotune(reps=5)[0] if args.tile == "auto" else batch_tile
+                fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"],
+                                obs[i][0].array, obs[i][1].array)
+                fd.run()  # captures the graphs of the chosen shape
+            else:
                 plain_ms.append(fd.last_timing()["total_ms"])
         fd.imagebuffer_resettozero()
+        fd.set_tile_shape(batch_tile)
         pv = len(pick) / (sum(plain_ms) / 1000.0)
-        plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick),
+        plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick), "tile": plain_tile,
                  "ms_per_shot": round(float(np.mean(plain_ms)), 2), "batched_over_plain": round(value / pv, 2)}
     # compressed snapshots against FP32 snapshots at full size, on a few shots
     snap_err = None

@@ -237,17 +237,21 @@ int sfwi_set_source(sfwi_handle *h, int kind);
  * CTAs per SM): each is compiled as its own set of kernels.  16x32 runs two
  * CTAs per SM with two pipeline stages each; 32x32 and 16x64 one CTA (two
  * stages fill the shared memory) and re-read less halo; 16x32_3CTA three
- * CTAs with one stage each (more warps in flight, fewer registers each). */
+ * CTAs with one stage each (more warps in flight, fewer registers each);
+ * 8x32_3CTA three CTAs of half-height tiles (more tiles for small batches). */
 #define SFWI_TILE_16x32 0
 #define SFWI_TILE_32x32 1
 #define SFWI_TILE_16x64 2
 #define SFWI_TILE_16x32_3CTA 3
-#define SFWI_NUM_TILE_SHAPES 4
+#define SFWI_TILE_8x32_3CTA 4
+#define SFWI_NUM_TILE_SHAPES 5
 
-/* Select the tile shape for this handle's runs (default SFWI_TILE_16x32).
- * A batch already on the device is re-tiled; results do not depend on the
- * shape beyond FP32 rounding of the same arithmetic (they are bit-identical:
- * every cell's update reads the same values in the same order). */
+/* Select the tile shape for this handle's runs.  Until one is selected (here
+ * or by sfwi_autotune) each batch gets SFWI_TILE_16x32, or SFWI_TILE_8x32_3CTA
+ * when its 16x32 tiles would give fewer than four to each of the device's
+ * CTA slots (small batches).  A batch already on the device is re-tiled.
+ * Results do not depend on the shape: they are bit-identical, since every
+ * cell's update reads the same values in the same order. */
 int sfwi_set_tile_shape(sfwi_handle *h, int shape);
 /* Launch the time-step kernels with programmatic dependent launch (default
  * on): each may be scheduled while the previous one drains and waits for its

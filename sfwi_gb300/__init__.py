@@ -332,7 +332,7 @@ SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
 SOURCE_TXX_TZZ, SOURCE_VZ_FORCE = 0, 1
 # tile shapes of the step kernels in SFWI_TILE_* order: core cells x by z,
 # and "x3" for three one-stage CTAs per SM
-TILE_SHAPES = ["16x32", "32x32", "16x64", "16x32x3"]
+TILE_SHAPES = ["16x32", "32x32", "16x64", "16x32x3", "8x32x3"]
 
 
 class PinnedArray:

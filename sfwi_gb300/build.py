@@ -23,7 +23,7 @@ OBJDIR = os.path.join(ROOT, "_build", "obj")
 # (source, object, defines): the step kernels once per tile shape (core
 # TX x TZ cells, CTAs per SM, pipeline stages per CTA, name), then the rest
 TILE_SHAPES = [(16, 32, 2, 2, "16x32"), (32, 32, 1, 2, "32x32"), (16, 64, 1, 2, "16x64"),
-               (16, 32, 3, 1, "16x32x3")]
+               (16, 32, 3, 1, "16x32x3"), (8, 32, 3, 2, "8x32x3")]
 UNITS = [("sfwi_kernels.cu", "sfwi_kernels_%s.o" % n,
           ["-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c, "-DSFWI_STAGES=%d" % ns,
            "-DSFWI_VARIANT_NS=v%s" % n, "-DSFWI_VARIANT_FN=tile_variant_%s" % n])

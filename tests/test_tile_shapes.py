@@ -106,3 +106,23 @@ def test_launch_overlap_keeps_results(case):
         fd.close()
     for k in KEYS:
         assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_default_shape_follows_the_batch_size():
+    """Without an explicit choice a one-shot batch gets the 8x32 tiles and a
+    batch with at least four 16x32 tiles per CTA slot gets 16x32."""
+    import bench
+    import sfwi_gb300 as sg
+    w = dict(bench.WORKLOADS["fwi376"], nt=20)
+    data = bench.build_workload(w)
+    pml, nxpml, nzpml = w["pml"], w["allnx"] + 2 * w["pml"], w["allnz"] + 2 * w["pml"]
+    isz, igz = pml + w["sy"], pml + w["gy"]
+    for nshots, want in ((1, "8x32x3"), (len(data["shots"]), "16x32")):
+        fd = sg.FD2DGPU_ELASTIC(data["sou"][:20], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1,
+                                pml, 20, 4, data["shots"][0]["ntr"], stage=1)
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])
+        for d in data["shots"][:nshots]:
+            fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"])
+        fd.run_forward()
+        assert fd.tile_shape() == want, (nshots, fd.tile_shape())
+        fd.close()

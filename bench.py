@@ -45,7 +45,8 @@ WORKLOADS = {
                     pass_bytes=248),
     # one FWI iteration at 376x201 (the headline line)
     "fwi376": dict(name="fwi-iteration-376x201-38shots-born-ot", allnx=376, allnz=201, dx=10.0, pml=20, nt=3000,
-                   dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0, model="layered", aperture=None, misfit="OT"),
+                   dt=1e-3, f0=15.0, nshots=38, spacing=10, sy=2, gy=0, model="layered", aperture=None, misfit="OT",
+                   rho_grad=True),
     # stage-2 batch at 401x301, 12.5 m: salt body, 80 shots with seeded
     # window widths of 150-401 nodes
     "salt401": dict(name="stage2-salt-401x301-80shots-uneven-apertures", allnx=401, allnz=301, dx=12.5, pml=20,
@@ -397,14 +398,18 @@ def main():
         fd.set_misfit(sg.MISFIT_OT)
     if w.get("snap"):
         fd.set_snapshots(*w["snap"])
+    if w.get("rho_grad"):
+        fd.set_density_gradient(True)
+        KERNEL_BYTES["k_bwd_v"] += 8  # the density kernel's accumulator, read and written
 
     def step():
         for d, (pz, px) in zip(shots, obs):
             fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], pz.array,
                             px.array)
         m, _ = fd.run()
+        grho = fd.read_density_gradient_f64() if w.get("rho_grad") else None
         g = fd.imagebuffer_resettozero()
-        return m, g
+        return m, (g, grho)
 
     tune = None
     if args.tile != "auto":
@@ -452,7 +457,7 @@ def main():
     value = nsh * args.steps / total_dev_s
     e2e = nsh * args.steps / wall
     h2d = sum(2 * d["ntr"] * nt * 4 for d in shots)
-    d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots)
+    d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots) + (8 * w["allnx"] * w["allnz"] if w.get("rho_grad") else 0)
 
     # per-kernel average launch durations (CUDA events on the engine stream)
     kt = fd.time_kernels(reps=20)
@@ -545,6 +550,7 @@ def main():
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
                        "nt": nt, "misfit": w["misfit"], "born": stage == 2, "dx_m": w["dx"],
                        "source": "vertical force" if w.get("source") == "vz" else "txx+tzz",
+                       "gradients": "vp, vs, rho" if w.get("rho_grad") else "vp, vs",
                        "tile": fd_tile, "autotune": tune,
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
                                    else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",

@@ -1280,6 +1280,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
+        // the density accumulator (when requested) is read from global memory
+        // here, so that its round trip overlaps the stencils below (it does
+        // not alias the arrays they store to)
+        const bool rho_img = p.grho != nullptr && image;
+        float4 gr4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (rho_img) gr4 = ld4(p.grho + m.gi);
         // everything this thread needs from the stage, then release it
         float ib[4], ex[4], ez[4], il[4];
         core4(core, 0, m.ci, ib);
@@ -1317,7 +1323,6 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // where the reconstruction (direction -1) subtracts dt (1/rho) D sigma,
         // so the step is formed from that increment directly rather than as a
         // difference of two nearly equal velocities.
-        const bool rho_img = p.grho != nullptr && image;
         float gvx[4], gvz[4];
         if (rho_img) {
 #pragma unroll
@@ -1343,7 +1348,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (rho_img) {
             // G_rho -= v_adj . (v(it) - v(it-1)) / dt
             float gr[4];
-            f4_to(ld4(p.grho + m.gi), gr);
+            f4_to(gr4, gr);
 #pragma unroll
             for (int j = 0; j < 4; j++)
                 if (m.image[j]) gr[j] -= ad.vx[j] * gvx[j] + ad.vz[j] * gvz[j];

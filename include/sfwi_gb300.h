@@ -233,23 +233,26 @@ int sfwi_wait_selftest(sfwi_handle *h, unsigned tries);
 #define SFWI_SOURCE_VZ_FORCE 1
 int sfwi_set_source(sfwi_handle *h, int kind);
 
-/* Tile shapes of the step kernels (cells of a tile's core, x by z, and the
- * CTAs per SM): each is compiled as its own set of kernels.  16x32 runs two
- * CTAs per SM with two pipeline stages each; 32x32 and 16x64 one CTA (two
- * stages fill the shared memory) and re-read less halo; 16x32_3CTA three
- * CTAs with one stage each (more warps in flight, fewer registers each);
- * 8x32_3CTA three CTAs of half-height tiles (more tiles for small batches). */
+/* Tile shapes of the step kernels (cells of a tile's core, x by z; CTAs per
+ * SM; cells per compute thread): each is compiled as its own set of kernels.
+ *   16x32           two CTAs per SM, two pipeline stages each, 4 cells a thread
+ *   32x32, 16x64    one CTA (two stages fill the shared memory), less halo
+ *   8x32_3CTA       three CTAs of half-height tiles
+ *   16x32_2CELL     16x32 with 2 cells a thread: twice the warps, fewer registers
+ *   8x32_2CELL_3STAGE  half-height tiles, 2 cells a thread, three stages: the
+ *                   most tiles in flight, for small batches */
 #define SFWI_TILE_16x32 0
 #define SFWI_TILE_32x32 1
 #define SFWI_TILE_16x64 2
-#define SFWI_TILE_16x32_3CTA 3
-#define SFWI_TILE_8x32_3CTA 4
-#define SFWI_NUM_TILE_SHAPES 5
+#define SFWI_TILE_8x32_3CTA 3
+#define SFWI_TILE_16x32_2CELL 4
+#define SFWI_TILE_8x32_2CELL_3STAGE 5
+#define SFWI_NUM_TILE_SHAPES 6
 
 /* Select the tile shape for this handle's runs.  Until one is selected (here
- * or by sfwi_autotune) each batch gets SFWI_TILE_16x32, or SFWI_TILE_8x32_3CTA
- * when its 16x32 tiles would give fewer than four to each of the device's
- * CTA slots (small batches).  A batch already on the device is re-tiled.
+ * or by sfwi_autotune) each batch gets SFWI_TILE_16x32, or
+ * SFWI_TILE_8x32_2CELL_3STAGE when its 16x32 tiles would give fewer than four
+ * to each of the device's CTA slots (small batches).  A batch already on the device is re-tiled.
  * Results do not depend on the shape: they are bit-identical, since every
  * cell's update reads the same values in the same order. */
 int sfwi_set_tile_shape(sfwi_handle *h, int shape);

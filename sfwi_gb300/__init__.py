@@ -331,8 +331,9 @@ def OT_alltrace(obs_x, obs_z, cal_x, cal_z, dt):
 SNAP_F32, SNAP_F16, SNAP_BF16 = 1, 2, 3
 SOURCE_TXX_TZZ, SOURCE_VZ_FORCE = 0, 1
 # tile shapes of the step kernels in SFWI_TILE_* order: core cells x by z,
-# and "x3" for three one-stage CTAs per SM
-TILE_SHAPES = ["16x32", "32x32", "16x64", "16x32x3", "8x32x3"]
+# "x3" for three CTAs per SM, "c2" for two cells per compute thread, "s3"
+# for three pipeline stages
+TILE_SHAPES = ["16x32", "32x32", "16x64", "8x32x3", "16x32c2", "8x32c2s3"]
 
 
 class PinnedArray:

@@ -21,13 +21,14 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libsfwi_gb300.so")
 OBJDIR = os.path.join(ROOT, "_build", "obj")
 # (source, object, defines): the step kernels once per tile shape (core
-# TX x TZ cells, CTAs per SM, pipeline stages per CTA, name), then the rest
-TILE_SHAPES = [(16, 32, 2, 2, "16x32"), (32, 32, 1, 2, "32x32"), (16, 64, 1, 2, "16x64"),
-               (16, 32, 3, 1, "16x32x3"), (8, 32, 3, 2, "8x32x3")]
+# TX x TZ cells, CTAs per SM, pipeline stages per CTA, cells per compute
+# thread, name), then the rest
+TILE_SHAPES = [(16, 32, 2, 2, 4, "16x32"), (32, 32, 1, 2, 4, "32x32"), (16, 64, 1, 2, 4, "16x64"),
+               (8, 32, 3, 2, 4, "8x32x3"), (16, 32, 2, 2, 2, "16x32c2"), (8, 32, 2, 3, 2, "8x32c2s3")]
 UNITS = [("sfwi_kernels.cu", "sfwi_kernels_%s.o" % n,
           ["-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c, "-DSFWI_STAGES=%d" % ns,
-           "-DSFWI_VARIANT_NS=v%s" % n, "-DSFWI_VARIANT_FN=tile_variant_%s" % n])
-         for tx, tz, c, ns, n in TILE_SHAPES]
+           "-DSFWI_CPT=%d" % cpt, "-DSFWI_VARIANT_NS=v%s" % n, "-DSFWI_VARIANT_FN=tile_variant_%s" % n])
+         for tx, tz, c, ns, cpt, n in TILE_SHAPES]
 UNITS += [(f, f.replace(".cu", ".o"), []) for f in ("sfwi_aux.cu", "sfwi_ot.cu", "sfwi_engine.cu")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]

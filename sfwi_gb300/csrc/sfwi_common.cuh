@@ -34,7 +34,14 @@ constexpr int HALO = 4;
 constexpr int BX = TX + 2 * HALO;  // staged box rows
 constexpr int BZ = TZ + 2 * HALO;  // staged box columns (multiple of 4)
 constexpr int BOX = BX * BZ;       // floats per staged box
-constexpr int NTHREADS = TX * TZ / 4;  // compute threads of a tile: one float4 of cells each
+#ifndef SFWI_CPT
+#define SFWI_CPT 4
+#endif
+// cells per compute thread, consecutive in z (4: one float4, 2: one float2)
+constexpr int CPT = SFWI_CPT;
+static_assert(CPT == 2 || CPT == 4, "2 or 4 cells per thread");
+constexpr int NP = CPT / 2;            // FP32x2 pairs per thread
+constexpr int NTHREADS = TX * TZ / CPT;  // compute threads of a tile
 constexpr int CTAS_PER_SM = SFWI_CTAS;  // persistent CTAs per SM (independent tile pipelines)
 
 // Arrays of the packed batch grid, in allocation order: one [X][P] array each,

@@ -260,23 +260,24 @@ const TileVariant *tile_variant(int shape) {
     switch (shape) {
     case SFWI_TILE_32x32: return tile_variant_32x32();
     case SFWI_TILE_16x64: return tile_variant_16x64();
-    case SFWI_TILE_16x32_3CTA: return tile_variant_16x32x3();
     case SFWI_TILE_8x32_3CTA: return tile_variant_8x32x3();
+    case SFWI_TILE_16x32_2CELL: return tile_variant_16x32c2();
+    case SFWI_TILE_8x32_2CELL_3STAGE: return tile_variant_8x32c2s3();
     default: return tile_variant_16x32();
     }
 }
 
 // Default tile shape for a batch: the 16x32 tiles when they give every CTA
-// slot (2 per SM) at least four tiles, else the 8x32 tiles of the three-CTA
-// build, which double the tiles of a small batch (one 376x201 shot: 196
-// 16x32 tiles for 304 slots; its pass is 8 % faster on 8x32; a 38-shot
-// batch is 3.5 % faster on 16x32).  sfwi_set_tile_shape or sfwi_autotune
-// replace the rule.
+// slot (2 per SM) at least four tiles, else 8x32 tiles with two cells per
+// thread and three pipeline stages, which double the tiles of a small batch
+// and keep more of them in flight (one 376x201 shot: 196 16x32 tiles for 304
+// slots; a step is 20 % faster on those tiles; a 38-shot batch is 14 %
+// faster on 16x32).  sfwi_set_tile_shape or sfwi_autotune replace the rule.
 void pick_tile_shape(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     long long tiles = 0;
     const int zt = (h->nzpml - 2 * NOP + 31) / 32;
     for (const ShotIn &in : shots) tiles += (long long)((in.nx + 2 * h->pml - 2 * NOP + 15) / 16) * zt;
-    h->tv = tile_variant(tiles < 4LL * 2 * std::max(h->nsm, 1) ? SFWI_TILE_8x32_3CTA : SFWI_TILE_16x32);
+    h->tv = tile_variant(tiles < 4LL * 2 * std::max(h->nsm, 1) ? SFWI_TILE_8x32_2CELL_3STAGE : SFWI_TILE_16x32);
 }
 
 // The tile table of the batch for the handle's tile shape: tiles over each

@@ -148,63 +148,107 @@ __device__ __forceinline__ void tma_load_2d(float *dst, const CUtensorMap *map, 
 // ----------------------------------------------------------------------------
 // stencils on staged boxes (row pitch BZ)
 // ----------------------------------------------------------------------------
-struct V4 {
-    float v[4];
+struct VC {
+    float v[CPT];
 };
 
-// a += k*(p - m) on four cells as two packed FP32x2 pairs (cells 0-1, 2-3);
-// p - m is formed as fma(m, -1, p), which rounds exactly like a subtraction
-__device__ __forceinline__ void acc4(V4 &a, float k, float4 p, float4 m) {
+// this thread's CPT consecutive cells of a staged row or core tile (one
+// float4 or float2 shared-memory access) and of a global array (one vector
+// store); `p` is 4*CPT-byte aligned
+__device__ __forceinline__ void ldc(const float *p, float o[CPT]) {
+    if constexpr (CPT == 4) {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        o[0] = a.x, o[1] = a.y, o[2] = a.z, o[3] = a.w;
+    } else {
+        const float2 a = *reinterpret_cast<const float2 *>(p);
+        o[0] = a.x, o[1] = a.y;
+    }
+}
+__device__ __forceinline__ void stc(float *p, const float o[CPT]) {
+    if constexpr (CPT == 4)
+        *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+    else
+        *reinterpret_cast<float2 *>(p) = make_float2(o[0], o[1]);
+}
+
+// a += k*(p - m) on this thread's cells as packed FP32x2 pairs; p - m is
+// formed as fma(m, -1, p), which rounds exactly like a subtraction
+__device__ __forceinline__ void accc(VC &a, float k, const float *pp, const float *mp) {
+    float pv[CPT], mv[CPT];
+    ldc(pp, pv);
+    ldc(mp, mv);
     const float2 kk = make_float2(k, k), neg = make_float2(-1.f, -1.f);
-    const float2 d0 = __ffma2_rn(make_float2(m.x, m.y), neg, make_float2(p.x, p.y));
-    const float2 d1 = __ffma2_rn(make_float2(m.z, m.w), neg, make_float2(p.z, p.w));
-    const float2 r0 = __ffma2_rn(kk, d0, make_float2(a.v[0], a.v[1]));
-    const float2 r1 = __ffma2_rn(kk, d1, make_float2(a.v[2], a.v[3]));
-    a.v[0] = r0.x;
-    a.v[1] = r0.y;
-    a.v[2] = r1.x;
-    a.v[3] = r1.y;
+#pragma unroll
+    for (int h = 0; h < NP; h++) {
+        const float2 d = __ffma2_rn(make_float2(mv[2 * h], mv[2 * h + 1]), neg, make_float2(pv[2 * h], pv[2 * h + 1]));
+        const float2 r = __ffma2_rn(kk, d, make_float2(a.v[2 * h], a.v[2 * h + 1]));
+        a.v[2 * h] = r.x;
+        a.v[2 * h + 1] = r.y;
+    }
+}
+__device__ __forceinline__ VC zero_cells() {
+    VC a;
+#pragma unroll
+    for (int j = 0; j < CPT; j++) a.v[j] = 0.f;
+    return a;
 }
 // D+x: sum_k K_k (f[r+k] - f[r-k+1])   (txx in update_vx, vz in txz update)
-__device__ __forceinline__ V4 dxp(const float *f, int r, int c) {
+__device__ __forceinline__ VC dxp(const float *f, int r, int c) {
     const float *q = f + r * BZ + c;
-    V4 a = {{0.f, 0.f, 0.f, 0.f}};
-    acc4(a, K1, ld4(q + 1 * BZ), ld4(q));
-    acc4(a, K2, ld4(q + 2 * BZ), ld4(q - 1 * BZ));
-    acc4(a, K3, ld4(q + 3 * BZ), ld4(q - 2 * BZ));
-    acc4(a, K4, ld4(q + 4 * BZ), ld4(q - 3 * BZ));
+    VC a = zero_cells();
+    accc(a, K1, q + 1 * BZ, q);
+    accc(a, K2, q + 2 * BZ, q - 1 * BZ);
+    accc(a, K3, q + 3 * BZ, q - 2 * BZ);
+    accc(a, K4, q + 4 * BZ, q - 3 * BZ);
     return a;
 }
 // D-x: sum_k K_k (f[r+k-1] - f[r-k])   (txz in update_vz, vx in txx update)
-__device__ __forceinline__ V4 dxm(const float *f, int r, int c) {
+__device__ __forceinline__ VC dxm(const float *f, int r, int c) {
     const float *q = f + r * BZ + c;
-    V4 a = {{0.f, 0.f, 0.f, 0.f}};
-    acc4(a, K1, ld4(q), ld4(q - 1 * BZ));
-    acc4(a, K2, ld4(q + 1 * BZ), ld4(q - 2 * BZ));
-    acc4(a, K3, ld4(q + 2 * BZ), ld4(q - 3 * BZ));
-    acc4(a, K4, ld4(q + 3 * BZ), ld4(q - 4 * BZ));
+    VC a = zero_cells();
+    accc(a, K1, q, q - 1 * BZ);
+    accc(a, K2, q + 1 * BZ, q - 2 * BZ);
+    accc(a, K3, q + 2 * BZ, q - 3 * BZ);
+    accc(a, K4, q + 3 * BZ, q - 4 * BZ);
     return a;
 }
-struct W12 {
-    float w[12];
+// the row window of the z stencils: this thread's cells and 4 on each side
+struct WC {
+    float w[CPT + 8];
 };
-__device__ __forceinline__ W12 loadw(const float *f, int r, int c) {
+__device__ __forceinline__ WC loadw(const float *f, int r, int c) {
     const float *q = f + r * BZ + c;
-    float4 a = ld4(q - 4), b = ld4(q), d = ld4(q + 4);
-    W12 o = {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, d.x, d.y, d.z, d.w}};
+    WC o;
+    if constexpr (CPT == 4) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float4 v = ld4(q - 4 + 4 * i);
+            o.w[4 * i] = v.x;
+            o.w[4 * i + 1] = v.y;
+            o.w[4 * i + 2] = v.z;
+            o.w[4 * i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < (CPT + 8) / 2; i++) {
+            const float2 v = *reinterpret_cast<const float2 *>(q - 4 + 2 * i);
+            o.w[2 * i] = v.x;
+            o.w[2 * i + 1] = v.y;
+        }
+    }
     return o;
 }
-__device__ __forceinline__ float2 pr(const W12 &s, int i) { return make_float2(s.w[i], s.w[i + 1]); }
+__device__ __forceinline__ float2 pr(const WC &s, int i) { return make_float2(s.w[i], s.w[i + 1]); }
 // k*(p - q) + a on a pair
 __device__ __forceinline__ float2 kdiff2(float k, float2 p, float2 q, float2 a) {
     const float2 d = __ffma2_rn(q, make_float2(-1.f, -1.f), p);
     return __ffma2_rn(make_float2(k, k), d, a);
 }
-// D+z: sum_k K_k (f[c+k] - f[c-k+1]) on cells (0,1) and (2,3) as FP32x2 pairs
-__device__ __forceinline__ V4 dzp(const W12 &s) {
-    V4 a;
+// D+z: sum_k K_k (f[c+k] - f[c-k+1]) on the cell pairs as FP32x2
+__device__ __forceinline__ VC dzp(const WC &s) {
+    VC a;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < NP; h++) {
         const int c = 4 + 2 * h;  // first cell of the pair
         float2 t = make_float2(0.f, 0.f);
         t = kdiff2(K1, pr(s, c + 1), pr(s, c), t);
@@ -217,10 +261,10 @@ __device__ __forceinline__ V4 dzp(const W12 &s) {
     return a;
 }
 // D-z: sum_k K_k (f[c+k-1] - f[c-k])
-__device__ __forceinline__ V4 dzm(const W12 &s) {
-    V4 a;
+__device__ __forceinline__ VC dzm(const WC &s) {
+    VC a;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < NP; h++) {
         const int c = 4 + 2 * h;
         float2 t = make_float2(0.f, 0.f);
         t = kdiff2(K1, pr(s, c), pr(s, c - 1), t);
@@ -241,32 +285,32 @@ __device__ __forceinline__ void f4_to(const float4 &a, float o[4]) {
 }
 __device__ __forceinline__ float4 to_f4(const float o[4]) { return make_float4(o[0], o[1], o[2], o[3]); }
 
-// thread -> cells: TZ/4 float4 columns x TX rows per tile
+// thread -> cells: TZ/CPT groups of CPT consecutive cells per row x TX rows
 struct CellMap {
-    int r, c;     // box coordinates of the first of the four cells
+    int r, c;     // box coordinates of the first of the thread's cells
     int ci;       // core-tile index of the first cell
     int lx, lz;   // local row / column of the first cell
     size_t gi;    // packed index of the first cell
     bool live;    // the row is updated and the first cell's column < nzpml-NOP
-    bool ok[4];   // cell inside the update region
-    bool image[4];  // inside the imaging interior [pml, n-pml)
+    bool ok[CPT];     // cell inside the update region
+    bool image[CPT];  // inside the imaging interior [pml, n-pml)
 };
 
 __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, const ShotGeo &g) {
     CellMap m;
-    const int tz = threadIdx.x % (TZ / 4), tr = threadIdx.x / (TZ / 4);
+    const int tz = threadIdx.x % (TZ / CPT), tr = threadIdx.x / (TZ / CPT);
     m.r = tr + HALO;
-    m.c = 4 * tz + HALO;
-    m.ci = tr * TZ + 4 * tz;
+    m.c = CPT * tz + HALO;
+    m.ci = tr * TZ + CPT * tz;
     m.lx = t.x0 + tr;
-    m.lz = t.z0 + 4 * tz;
+    m.lz = t.z0 + CPT * tz;
     m.gi = (size_t)(g.row0 + m.lx) * p.P + m.lz;
     const bool row_ok = m.lx >= NOP && m.lx < g.nxpml - NOP;
-    m.live = row_ok && m.lz < p.nzpml - NOP;  // lz, P are multiples of 4, so lz+3 < P
+    m.live = row_ok && m.lz < p.nzpml - NOP;  // lz is a multiple of CPT and P of 4, so lz+CPT-1 < P
     const int pml = p.pml, nzpml = p.nzpml, nxpml = g.nxpml;
     const bool xi = m.lx >= pml && m.lx < nxpml - pml;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < CPT; j++) {
         const int z = m.lz + j;
         m.ok[j] = row_ok && z >= NOP && z < nzpml - NOP;
         m.image[j] = m.ok[j] && xi && z >= pml && z < nzpml - pml;
@@ -274,20 +318,18 @@ __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, cons
     return m;
 }
 
-__device__ __forceinline__ void core4(const float *core, int slot, int ci, float o[4]) {
-    f4_to(ld4(core + slot * CORE + ci), o);
-}
+__device__ __forceinline__ void core4(const float *core, int slot, int ci, float o[CPT]) { ldc(core + slot * CORE + ci, o); }
 
 // PML factors of a frame cell: the split update (d1*m + c*D)/d2 is evaluated
 // as (d1*m + c*D) * (1/d2) with a correctly rounded reciprocal, one rounding
 // more than a division
 struct Damp {
-    float d1[4], r2[4], d3[4], r4[4];
+    float d1[CPT], r2[CPT], d3[CPT], r4[CPT];
 };
-__device__ __forceinline__ Damp make_damp(const Params &p, const float x[4], const float z[4]) {
+__device__ __forceinline__ Damp make_damp(const Params &p, const float x[CPT], const float z[CPT]) {
     Damp d;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < CPT; j++) {
         d.d1[j] = 1.f - p.dt * x[j] / 2;
         d.r2[j] = __frcp_rn(1.f + p.dt * x[j] / 2);
         d.d3[j] = 1.f - p.dt * z[j] / 2;
@@ -297,21 +339,21 @@ __device__ __forceinline__ Damp make_damp(const Params &p, const float x[4], con
 }
 
 struct VState {
-    float vx[4], vz[4], mx[4], mz[4];
+    float vx[CPT], vz[CPT], mx[CPT], mz[CPT];
 };
 struct SState {
-    float xx[4], zz[4], xz[4], mxx[4], mzz[4], mxz[4];
+    float xx[CPT], zz[CPT], xz[CPT], mxx[CPT], mzz[CPT], mxz[CPT];
 };
 
 // FP32x2 helpers on the cells (2h, 2h+1) of a four-cell group
-__device__ __forceinline__ float2 P2(const float v[4], int h) { return make_float2(v[2 * h], v[2 * h + 1]); }
-__device__ __forceinline__ void S2(float v[4], int h, float2 x) {
+__device__ __forceinline__ float2 P2(const float v[CPT], int h) { return make_float2(v[2 * h], v[2 * h + 1]); }
+__device__ __forceinline__ void S2(float v[CPT], int h, float2 x) {
     v[2 * h] = x.x;
     v[2 * h + 1] = x.y;
 }
 __device__ __forceinline__ float2 B2(float x) { return make_float2(x, x); }
 // store a packed pair into cells 2h, 2h+1 of v where the cell is updated
-__device__ __forceinline__ void sel2(float v[4], int h, float2 x, const bool ok[4]) {
+__device__ __forceinline__ void sel2(float v[CPT], int h, float2 x, const bool ok[CPT]) {
     if (ok[2 * h]) v[2 * h] = x.x;
     if (ok[2 * h + 1]) v[2 * h + 1] = x.y;
 }
@@ -324,20 +366,20 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 // with the split form in frame cells; stores the new state.
 template <bool FRAME>
 __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const FieldSet &f, VState &s,
-                                        const float ib[4], const Damp &d, float dir, const V4 &ax, const V4 &bz,
-                                        const V4 &dx_, const V4 &cz) {
+                                        const float ib[CPT], const Damp &d, float dir, const VC &ax, const VC &bz,
+                                        const VC &dx_, const VC &cz) {
     if (!FRAME) {
         // tile without PML cells: all four cells are updated (FP32x2)
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             const float2 i2 = P2(ib, h);
             const float2 cx = mul2(i2, tx), cz2 = mul2(i2, tz);
             S2(s.vx, h, add2(P2(s.vx, h), fma2(cx, P2(ax.v, h), mul2(cz2, P2(bz.v, h)))));
             S2(s.vz, h, add2(P2(s.vz, h), fma2(cx, P2(dx_.v, h), mul2(cz2, P2(cz.v, h)))));
         }
-        st4(f.vx + m.gi, to_f4(s.vx));
-        st4(f.vz + m.gi, to_f4(s.vz));
+        stc(f.vx + m.gi, s.vx);
+        stc(f.vz + m.gi, s.vz);
         return;
     }
     // tile with PML cells: the split update of the reference for every cell,
@@ -347,7 +389,7 @@ __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const
     {
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             const float2 i2 = P2(ib, h);
             const float2 cx = mul2(i2, tx), cz2 = mul2(i2, tz);
             const float2 d1 = P2(d.d1, h), r2 = P2(d.r2, h), d3 = P2(d.d3, h), r4 = P2(d.r4, h);
@@ -362,11 +404,11 @@ __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const
             sel2(s.vz, h, add2(zx, zz), m.ok);
         }
     }
-    st4(f.vx + m.gi, to_f4(s.vx));
-    st4(f.vz + m.gi, to_f4(s.vz));
+    stc(f.vx + m.gi, s.vx);
+    stc(f.vz + m.gi, s.vz);
     if (FRAME) {
-        st4(f.mvx + m.gi, to_f4(s.mx));
-        st4(f.mvz + m.gi, to_f4(s.mz));
+        stc(f.mvx + m.gi, s.mx);
+        stc(f.mvz + m.gi, s.mz);
     }
 }
 
@@ -375,13 +417,13 @@ __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const
 // with optional Born terms added to the split parts first (born != nullptr).
 template <bool FRAME>
 __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const FieldSet &f, SState &s,
-                                        const float lam[4], const float mu[4], const Damp &dm, float dir, const V4 &a,
-                                        const V4 &b, const V4 &c, const V4 &d, const float (*born)[4]) {
+                                        const float lam[CPT], const float mu[CPT], const Damp &dm, float dir, const VC &a,
+                                        const VC &b, const VC &c, const VC &d, const float (*born)[CPT]) {
     if (!FRAME) {
         // tile without PML cells: all four cells are updated (FP32x2)
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             const float2 l = P2(lam, h), u = P2(mu, h);
             const float2 l2m = fma2(u, B2(2.f), l);
             const float2 ax = mul2(tx, P2(a.v, h)), bz = mul2(tz, P2(b.v, h));
@@ -396,9 +438,9 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             S2(s.zz, h, add2(zz, fma2(l, ax, mul2(l2m, bz))));
             S2(s.xz, h, add2(xz, mul2(u, add2(dx_, cz))));
         }
-        st4(f.txx + m.gi, to_f4(s.xx));
-        st4(f.tzz + m.gi, to_f4(s.zz));
-        st4(f.txz + m.gi, to_f4(s.xz));
+        stc(f.txx + m.gi, s.xx);
+        stc(f.tzz + m.gi, s.zz);
+        stc(f.txz + m.gi, s.xz);
         return;
     }
     // tile with PML cells: the split updates of the reference for every cell
@@ -407,7 +449,7 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
     {
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             const float2 l = P2(lam, h), u = P2(mu, h);
             const float2 l2m = fma2(u, B2(2.f), l);
             const float2 ax = mul2(tx, P2(a.v, h)), bz = mul2(tz, P2(b.v, h));
@@ -438,13 +480,13 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             sel2(s.xz, h, add2(nxz_x, nxz_z), m.ok);
         }
     }
-    st4(f.txx + m.gi, to_f4(s.xx));
-    st4(f.tzz + m.gi, to_f4(s.zz));
-    st4(f.txz + m.gi, to_f4(s.xz));
+    stc(f.txx + m.gi, s.xx);
+    stc(f.tzz + m.gi, s.zz);
+    stc(f.txz + m.gi, s.xz);
     if (FRAME) {
-        st4(f.mtxx + m.gi, to_f4(s.mxx));
-        st4(f.mtzz + m.gi, to_f4(s.mzz));
-        st4(f.mtxz + m.gi, to_f4(s.mxz));
+        stc(f.mtxx + m.gi, s.mxx);
+        stc(f.mtzz + m.gi, s.mzz);
+        stc(f.mtxz + m.gi, s.mxz);
     }
 }
 
@@ -614,17 +656,26 @@ __device__ __forceinline__ uint32_t to16(float v, int fmt) {
 __device__ __forceinline__ float from16(uint16_t u, int fmt) {
     return fmt == SNAP_F16 ? __half2float(__ushort_as_half(u)) : __bfloat162float(__ushort_as_bfloat16(u));
 }
-// four consecutive cells of one component of snapshot k
-__device__ __forceinline__ void store_snap4(const Params &p, int k, int comp, size_t cell, float4 v, float scale) {
+// this thread's consecutive cells (read from the staged box at `src`) of
+// one component of snapshot k
+__device__ __forceinline__ void store_snapc(const Params &p, int k, int comp, size_t cell, const float *src,
+                                            float scale) {
     const size_t o = ((size_t)(2 * k + comp) * p.X) * p.PS + cell;
+    float v[CPT];
+    ldc(src, v);
     if (p.snap_fmt == SNAP_F32) {
-        st4(reinterpret_cast<float *>(p.snap) + o, v);
+        stc(reinterpret_cast<float *>(p.snap) + o, v);
     } else {
         const float inv = scale > 0.f ? 1.0f / scale : 0.f;
-        uint2 w;
-        w.x = to16(v.x * inv, p.snap_fmt) | (to16(v.y * inv, p.snap_fmt) << 16);
-        w.y = to16(v.z * inv, p.snap_fmt) | (to16(v.w * inv, p.snap_fmt) << 16);
-        *reinterpret_cast<uint2 *>(reinterpret_cast<uint16_t *>(p.snap) + o) = w;
+        uint32_t w[NP];
+#pragma unroll
+        for (int h = 0; h < NP; h++)
+            w[h] = to16(v[2 * h] * inv, p.snap_fmt) | (to16(v[2 * h + 1] * inv, p.snap_fmt) << 16);
+        uint16_t *dst = reinterpret_cast<uint16_t *>(p.snap) + o;
+        if constexpr (CPT == 4)
+            *reinterpret_cast<uint2 *>(dst) = make_uint2(w[0], w[1]);
+        else
+            *reinterpret_cast<uint32_t *>(dst) = w[0];
     }
 }
 
@@ -681,7 +732,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
         // everything this thread needs from the stage, then release it
-        float ib[4], ex[4], ez[4];
+        float ib[CPT], ex[CPT], ez[CPT];
         core4(core, 0, m.ci, ib);
         if (frame) {
             core4(core, 3, m.ci, ex);
@@ -694,11 +745,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 5, m.ci, bg.mx);
             core4(core, 6, m.ci, bg.mz);
         }
-        const V4 ax = dxp(s_xx, m.r, m.c);
-        const V4 bz = dzm(loadw(s_xz, m.r, m.c));
-        const V4 dx_ = dxm(s_xz, m.r, m.c);
-        const V4 cz = dzp(loadw(s_zz, m.r, m.c));
-        V4 sax, sbz, sdx, scz;
+        const VC ax = dxp(s_xx, m.r, m.c);
+        const VC bz = dzm(loadw(s_xz, m.r, m.c));
+        const VC dx_ = dxm(s_xz, m.r, m.c);
+        const VC cz = dzp(loadw(s_zz, m.r, m.c));
+        VC sax, sbz, sdx, scz;
         if (BORN) {
             const float *b_xx = s + 3 * BOX, *b_zz = s + 4 * BOX, *b_xz = s + 5 * BOX;
             core4(core, 7, m.ci, sc.vx);
@@ -730,7 +781,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             // snapshot value includes it
             const bool fsrc = p.src_kind == SRC_VZ_FORCE && (c.t.flags & TILE_SOURCE) && m.lx == c.g.isx;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < CPT; j++)
                 if (m.ok[j]) {
                     mx = fmaxf(mx, fabsf(bg.vx[j]));
                     mz = fmaxf(mz, fabsf(fsrc && m.lz + j == c.g.isz ? bg.vz[j] + p.sou[it] : bg.vz[j]));
@@ -858,22 +909,22 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             const int k = it / p.snap_every;
             const size_t cell = (size_t)(c.g.row0 + m.lx) * p.PS + m.lz;
             const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
-            store_snap4(p, k, 0, cell, ld4(s_vx + m.r * BZ + m.c), sc[0]);
-            store_snap4(p, k, 1, cell, ld4(s_vz + m.r * BZ + m.c), sc[1]);
+            store_snapc(p, k, 0, cell, s_vx + m.r * BZ + m.c, sc[0]);
+            store_snapc(p, k, 1, cell, s_vz + m.r * BZ + m.c, sc[1]);
         }
         if (!m.live) return;
         // everything this thread needs from the stage, then release it
-        float lam[4], mu[4], ex[4], ez[4];
+        float lam[CPT], mu[CPT], ex[CPT], ez[CPT];
         core4(core, 0, m.ci, lam);
         core4(core, 1, m.ci, mu);
         if (frame) {
             core4(core, 5, m.ci, ex);
             core4(core, 6, m.ci, ez);
         }
-        const V4 a = dxm(s_vx, m.r, m.c);
-        const V4 cc = dzp(loadw(s_vx, m.r, m.c));
-        const V4 b = dzm(loadw(s_vz, m.r, m.c));
-        const V4 d = dxp(s_vz, m.r, m.c);
+        const VC a = dxm(s_vx, m.r, m.c);
+        const VC cc = dzp(loadw(s_vx, m.r, m.c));
+        const VC b = dzm(loadw(s_vz, m.r, m.c));
+        const VC d = dxp(s_vz, m.r, m.c);
         SState bg, sc;
         core4(core, 2, m.ci, bg.xx);
         core4(core, 3, m.ci, bg.zz);
@@ -883,8 +934,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 8, m.ci, bg.mzz);
             core4(core, 9, m.ci, bg.mxz);
         }
-        float bp[4], bs[4];
-        V4 as, cs, bs_, ds;
+        float bp[CPT], bs[CPT];
+        VC as, cs, bs_, ds;
         if (BORN) {
             core4(core, 10, m.ci, bp);
             core4(core, 11, m.ci, bs);
@@ -912,9 +963,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             // Born virtual source from the updated background velocity
             // (add_born_source_components, sfwi-stage2/born.cu:788-798); bp/bs
             // are zero outside the Born region
-            float born[6][4];
+            float born[6][CPT];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+            for (int h = 0; h < NP; h++) {
                 const float2 bp2 = P2(bp, h), bs2 = P2(bs, h);
                 const float2 mix = fma2(bs2, B2(-2.f), bp2);
                 const float2 ax = mul2(P2(a.v, h), B2(p.idx)), bz = mul2(P2(b.v, h), B2(p.idz));
@@ -946,12 +997,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 // adjoint stress update of the four cells (txx' keeps only an x-part and
 // tzz' only a z-part; txz' is split, its x-part in amxz) and its stores
 __device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m, bool frame, const Damp &dm,
-                                               float adj_dir, const V4 &aa, const V4 &ba, const V4 &ca, const V4 &da,
-                                               float axx[4], float azz[4], float axz[4], float amxz[4]) {
+                                               float adj_dir, const VC &aa, const VC &ba, const VC &ca, const VC &da,
+                                               float axx[CPT], float azz[CPT], float axz[CPT], float amxz[CPT]) {
     if (!frame) {
         const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             S2(axx, h, fma2(tx, P2(aa.v, h), P2(axx, h)));
             S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
             S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
@@ -960,7 +1011,7 @@ __device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m
         // PML tile: damping factors are 1 away from the PML
         const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NP; h++) {
             const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
             const float2 nxx = mul2(fma2(d1, P2(axx, h), mul2(tx, P2(aa.v, h))), r2);
             const float2 nzz = mul2(fma2(d3, P2(azz, h), mul2(tz, P2(ba.v, h))), r4);
@@ -972,10 +1023,10 @@ __device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m
             sel2(axz, h, add2(nx_, nz_), m.ok);
         }
     }
-    st4(p.ad.txx + m.gi, to_f4(axx));
-    st4(p.ad.tzz + m.gi, to_f4(azz));
-    st4(p.ad.txz + m.gi, to_f4(axz));
-    if (frame) st4(p.ad.mtxz + m.gi, to_f4(amxz));
+    stc(p.ad.txx + m.gi, axx);
+    stc(p.ad.tzz + m.gi, azz);
+    stc(p.ad.txz + m.gi, axz);
+    if (frame) stc(p.ad.mtxz + m.gi, amxz);
 }
 
 // zero-lag imaging of the lambda and mu kernels (doimage_gradient,
@@ -983,11 +1034,11 @@ __device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m
 //   G_lam += w * -(gxx + gzz)(txx' + tzz')
 //   G_mu  += w * (-2 (gxx txx' + gzz tzz') - (gxz + gzx) txz')
 // with the forward strains gxx = a/dx, gzz = b/dz, gxz = c/dz, gzx = d/dx
-__device__ __forceinline__ void image_lam_mu(const Params &p, const CellMap &m, float w, const V4 &a, const V4 &b,
-                                             const V4 &cc, const V4 &d, const float axx[4], const float azz[4],
-                                             const float axz[4], float gl[4], float gm[4]) {
+__device__ __forceinline__ void image_lam_mu(const Params &p, const CellMap &m, float w, const VC &a, const VC &b,
+                                             const VC &cc, const VC &d, const float axx[CPT], const float azz[CPT],
+                                             const float axz[CPT], float gl[CPT], float gm[CPT]) {
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < NP; h++) {
         const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
         const float2 gxz = mul2(P2(cc.v, h), B2(p.idz)), gzx = mul2(P2(d.v, h), B2(p.idx));
         const float2 x2 = P2(axx, h), z2 = P2(azz, h);
@@ -1162,7 +1213,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
         // everything this thread needs from the stage, then release it
-        float lam[4], mu[4], ex[4], ez[4];
+        float lam[CPT], mu[CPT], ex[CPT], ez[CPT];
         core4(core, 0, m.ci, lam);
         core4(core, 1, m.ci, mu);
         if (frame) {
@@ -1170,10 +1221,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 9, m.ci, ez);
         }
         // reconstruction (direction -1) with strains
-        const V4 a = dxm(s_vx, m.r, m.c);
-        const V4 cc = dzp(loadw(s_vx, m.r, m.c));
-        const V4 b = dzm(loadw(s_vz, m.r, m.c));
-        const V4 d = dxp(s_vz, m.r, m.c);
+        const VC a = dxm(s_vx, m.r, m.c);
+        const VC cc = dzp(loadw(s_vx, m.r, m.c));
+        const VC b = dzm(loadw(s_vz, m.r, m.c));
+        const VC d = dxp(s_vz, m.r, m.c);
         SState st;
         core4(core, 2, m.ci, st.xx);
         core4(core, 3, m.ci, st.zz);
@@ -1184,16 +1235,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 12, m.ci, st.mxz);
         }
         // adjoint stresses: txx' = x-part only, tzz' = z-part only, txz split
-        float axx[4], azz[4], axz[4], amxz[4];
+        float axx[CPT], azz[CPT], axz[CPT], amxz[CPT];
         core4(core, 5, m.ci, axx);
         core4(core, 6, m.ci, azz);
         core4(core, 7, m.ci, axz);
         if (frame) core4(core, 13, m.ci, amxz);
-        const V4 aa = dxm(a_vx, m.r, m.c);
-        const V4 ca = dzp(loadw(a_vx, m.r, m.c));
-        const V4 ba = dzm(loadw(a_vz, m.r, m.c));
-        const V4 da = dxp(a_vz, m.r, m.c);
-        float gl[4], gm[4];
+        const VC aa = dxm(a_vx, m.r, m.c);
+        const VC ca = dzp(loadw(a_vx, m.r, m.c));
+        const VC ba = dzm(loadw(a_vz, m.r, m.c));
+        const VC da = dxp(a_vz, m.r, m.c);
+        float gl[CPT], gm[CPT];
         if (image) {
             core4(core, 14, m.ci, gl);
             core4(core, 15, m.ci, gm);
@@ -1209,8 +1260,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // zero-lag imaging of the lambda and mu kernels (interior cells)
         if (image) {
             image_lam_mu(p, m, 1.f, a, b, cc, d, axx, azz, axz, gl, gm);
-            st4(p.glam + m.gi, to_f4(gl));
-            st4(p.gmu + m.gi, to_f4(gm));
+            stc(p.glam + m.gi, gl);
+            stc(p.gmu + m.gi, gm);
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
@@ -1220,6 +1271,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 //   P = (l+2m) txx + l tzz,  Q = l txx + (l+2m) tzz,  R = m txz
 __device__ __forceinline__ void lame_weight(float *s_P, float *s_Q, float *s_R, const float *s_l, const float *s_u) {
     for (int i = threadIdx.x; i < BOX / 4; i += NTHREADS) {
+        // four box cells per iteration whatever the cells per thread
         float xx[4], zz[4], xz[4], l[4], u[4], P_[4], Q_[4], R_[4];
         f4_to(ld4(s_P + 4 * i), xx);
         f4_to(ld4(s_Q + 4 * i), zz);
@@ -1284,10 +1336,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // here, so that its round trip overlaps the stencils below (it does
         // not alias the arrays they store to)
         const bool rho_img = p.grho != nullptr && image;
-        float4 gr4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (rho_img) gr4 = ld4(p.grho + m.gi);
+        float gr[CPT];
+        if (rho_img) ldc(p.grho + m.gi, gr);
         // everything this thread needs from the stage, then release it
-        float ib[4], ex[4], ez[4], il[4];
+        float ib[CPT], ex[CPT], ez[CPT], il[CPT];
         core4(core, 0, m.ci, ib);
         if (frame) {
             core4(core, 5, m.ci, ex);
@@ -1300,10 +1352,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 7, m.ci, bg.mx);
             core4(core, 8, m.ci, bg.mz);
         }
-        const V4 ax = dxp(s_xx, m.r, m.c);
-        const V4 bz = dzm(loadw(s_xz, m.r, m.c));
-        const V4 dx_ = dxm(s_xz, m.r, m.c);
-        const V4 cz = dzp(loadw(s_zz, m.r, m.c));
+        const VC ax = dxp(s_xx, m.r, m.c);
+        const VC bz = dzm(loadw(s_xz, m.r, m.c));
+        const VC dx_ = dxm(s_xz, m.r, m.c);
+        const VC cz = dzp(loadw(s_zz, m.r, m.c));
         if (image) core4(core, 11, m.ci, il);
         core4(core, 3, m.ci, ad.vx);
         core4(core, 4, m.ci, ad.vz);
@@ -1311,10 +1363,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 9, m.ci, ad.mx);
             core4(core, 10, m.ci, ad.mz);
         }
-        const V4 aax = dxp(s_P, m.r, m.c);
-        const V4 abz = dzm(loadw(s_R, m.r, m.c));
-        const V4 adx = dxm(s_R, m.r, m.c);
-        const V4 acz = dzp(loadw(s_Q, m.r, m.c));
+        const VC aax = dxp(s_P, m.r, m.c);
+        const VC abz = dzm(loadw(s_R, m.r, m.c));
+        const VC adx = dxm(s_R, m.r, m.c);
+        const VC acz = dzp(loadw(s_Q, m.r, m.c));
         release();
         Damp dm{};
         if (frame) dm = make_damp(p, ex, ez);
@@ -1323,10 +1375,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // where the reconstruction (direction -1) subtracts dt (1/rho) D sigma,
         // so the step is formed from that increment directly rather than as a
         // difference of two nearly equal velocities.
-        float gvx[4], gvz[4];
+        float gvx[CPT], gvz[CPT];
         if (rho_img) {
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < CPT; j++) {
                 gvx[j] = ib[j] * (ax.v[j] * p.idx + bz.v[j] * p.idz);
                 gvz[j] = ib[j] * (dx_.v[j] * p.idx + cz.v[j] * p.idz);
             }
@@ -1337,9 +1389,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.bg, bg, ib, dm, -1.f, ax, bz, dx_, cz);
         if (image) {
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < CPT; j++)
                 if (m.image[j]) il[j] += bg.vx[j] * bg.vx[j] + bg.vz[j] * bg.vz[j];
-            st4(p.illum + m.gi, to_f4(il));
+            stc(p.illum + m.gi, il);
         }
         if (frame)
             v_apply<true>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
@@ -1347,12 +1399,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
         if (rho_img) {
             // G_rho -= v_adj . (v(it) - v(it-1)) / dt
-            float gr[4];
-            f4_to(gr4, gr);
+
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < CPT; j++)
                 if (m.image[j]) gr[j] -= ad.vx[j] * gvx[j] + ad.vz[j] * gvz[j];
-            st4(p.grho + m.gi, to_f4(gr));
+            stc(p.grho + m.gi, gr);
         }
     };
     run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
@@ -1421,7 +1472,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
         // everything this thread needs from the stage, then release it
-        float ex[4], ez[4], axx[4], azz[4], axz[4], amxz[4], gl[4], gm[4], il[4], vx[4], vz[4];
+        float ex[CPT], ez[CPT], axx[CPT], azz[CPT], axz[CPT], amxz[CPT], gl[CPT], gm[CPT], il[CPT], vx[CPT], vz[CPT];
         core4(core, 0, m.ci, axx);
         core4(core, 1, m.ci, azz);
         core4(core, 2, m.ci, axz);
@@ -1430,11 +1481,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 4, m.ci, ez);
             core4(core, 5, m.ci, amxz);
         }
-        const V4 aa = dxm(a_vx, m.r, m.c);
-        const V4 ca = dzp(loadw(a_vx, m.r, m.c));
-        const V4 ba = dzm(loadw(a_vz, m.r, m.c));
-        const V4 da = dxp(a_vz, m.r, m.c);
-        V4 a{}, b{}, cc{}, d{};
+        const VC aa = dxm(a_vx, m.r, m.c);
+        const VC ca = dzp(loadw(a_vx, m.r, m.c));
+        const VC ba = dzm(loadw(a_vz, m.r, m.c));
+        const VC da = dxp(a_vz, m.r, m.c);
+        VC a{}, b{}, cc{}, d{};
         if (img) {
             core4(core, 6, m.ci, gl);
             core4(core, 7, m.ci, gm);
@@ -1443,8 +1494,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             cc = dzp(loadw(sv, m.r, m.c));
             b = dzm(loadw(sv + BOX, m.r, m.c));
             d = dxp(sv + BOX, m.r, m.c);
-            f4_to(ld4(sv + m.r * BZ + m.c), vx);
-            f4_to(ld4(sv + BOX + m.r * BZ + m.c), vz);
+            ldc(sv + m.r * BZ + m.c, vx);
+            ldc(sv + BOX + m.r * BZ + m.c, vz);
         }
         release();
         Damp dm{};
@@ -1453,11 +1504,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (img) {
             image_lam_mu(p, m, w, a, b, cc, d, axx, azz, axz, gl, gm);
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < CPT; j++)
                 if (m.image[j]) il[j] += w * (vx[j] * vx[j] + vz[j] * vz[j]);
-            st4(p.glam + m.gi, to_f4(gl));
-            st4(p.gmu + m.gi, to_f4(gm));
-            st4(p.illum + m.gi, to_f4(il));
+            stc(p.glam + m.gi, gl);
+            stc(p.gmu + m.gi, gm);
+            stc(p.illum + m.gi, il);
         }
     };
     if (sstep && FMT != SNAP_F32) {
@@ -1498,7 +1549,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         const CellMap m = cell_map(p, c.t, c.g);
         if (!m.live) return;
         const bool frame = c.t.flags & TILE_FRAME;
-        float ib[4], ex[4], ez[4];
+        float ib[CPT], ex[CPT], ez[CPT];
         core4(core, 0, m.ci, ib);
         if (frame) {
             core4(core, 3, m.ci, ex);
@@ -1511,10 +1562,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             core4(core, 5, m.ci, ad.mx);
             core4(core, 6, m.ci, ad.mz);
         }
-        const V4 aax = dxp(s_P, m.r, m.c);
-        const V4 abz = dzm(loadw(s_R, m.r, m.c));
-        const V4 adx = dxm(s_R, m.r, m.c);
-        const V4 acz = dzp(loadw(s_Q, m.r, m.c));
+        const VC aax = dxp(s_P, m.r, m.c);
+        const VC abz = dzm(loadw(s_R, m.r, m.c));
+        const VC adx = dxm(s_R, m.r, m.c);
+        const VC acz = dzp(loadw(s_Q, m.r, m.c));
         release();
         if (frame) {
             const Damp dm = make_damp(p, ex, ez);

@@ -33,8 +33,9 @@ struct TileVariant {
 const TileVariant *tile_variant_16x32();
 const TileVariant *tile_variant_32x32();
 const TileVariant *tile_variant_16x64();
-const TileVariant *tile_variant_16x32x3();
 const TileVariant *tile_variant_8x32x3();
+const TileVariant *tile_variant_16x32c2();
+const TileVariant *tile_variant_8x32c2s3();
 
 // sfwi_aux.cu
 struct SetupArgs {

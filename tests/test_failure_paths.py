@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 KEYS = ("syn_z", "syn_x", "res_z", "res_x", "grad_pp", "grad_ps", "illum")
 
 
-@pytest.mark.parametrize("shape", ["16x32", "16x32x3"])
+@pytest.mark.parametrize("shape", ["16x32", "8x32c2s3"])
 def test_pipeline_wait_timeout_is_reported_and_the_handle_stays_usable(shape):
     import sfwi_gb300 as sg
     shot, inputs, _ = load_case("s1_full")

@@ -117,7 +117,7 @@ def test_default_shape_follows_the_batch_size():
     data = bench.build_workload(w)
     pml, nxpml, nzpml = w["pml"], w["allnx"] + 2 * w["pml"], w["allnz"] + 2 * w["pml"]
     isz, igz = pml + w["sy"], pml + w["gy"]
-    for nshots, want in ((1, "8x32x3"), (len(data["shots"]), "16x32")):
+    for nshots, want in ((1, "8x32c2s3"), (len(data["shots"]), "16x32")):
         fd = sg.FD2DGPU_ELASTIC(data["sou"][:20], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1,
                                 pml, 20, 4, data["shots"][0]["ntr"], stage=1)
         fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])

@@ -93,6 +93,7 @@ enum RecArr { R_SYN_Z, R_SYN_X, R_SYN2_Z, R_SYN2_X, R_OBS_Z, R_OBS_X, R_RES_Z, R
 
 struct Batch {
     int nshots = 0, ntiles = 0, X = 0, P = 0, ntr_tot = 0, max_nxpml = 0;
+    bool ready = false;  // the batch described here is the one on the device (its upload completed)
     std::vector<ShotGeo> geo;
     std::vector<Tile> tiles;
     std::vector<std::vector<int>> rcols;  // per shot: recording and injection columns (tile flags)
@@ -695,6 +696,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     h->last_forward_only = forward_only;
     CK(cudaSetDevice(h->device));
     if (h->tile_auto) pick_tile_shape(h, shots);
+    h->b.ready = false;  // until this batch is on the device
     int rc = build_batch(h, shots);
     if (rc) return rc;
     if (mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2 && h->nt > ot_max_nt())
@@ -702,6 +704,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     rc = upload_batch(h, shots, forward_only, mode != RUN_FORWARD);
     if (rc) return rc;
     Batch &b = h->b;
+    b.ready = true;
     const Params p = make_params(h, forward_only);
     const int nt = h->nt;
     cudaStream_t st = h->st;
@@ -1274,6 +1277,7 @@ int sfwi_read_gradients_f64(sfwi_handle *h, double *grad_pp, double *grad_ps, do
 int sfwi_read_records(sfwi_handle *h, int i, float *syn_z, float *syn_x, float *syn2_z, float *syn2_x, float *res_z,
                       float *res_x) {
     if (int rc = check(h)) return rc;
+    if (!h->b.ready) return fail(SFWI_E_STATE, "no records: the last run did not complete");
     if (i < 0 || i >= (int)h->last_ntr.size()) return fail(SFWI_E_ARG, "shot %d not in the last run", i);
     const int nt = h->nt;
     const size_t off = (size_t)h->last_tr0[i] * nt, n = (size_t)h->last_ntr[i] * nt;
@@ -1408,7 +1412,7 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
     if (int rc = check(h)) return rc;
     if (!out_ms || reps < 1) return fail(SFWI_E_ARG, "bad argument");
-    if (h->b.ntiles == 0 || !h->b.grid.p) return fail(SFWI_E_STATE, "no batch has been run");
+    if (!h->b.ready || h->b.ntiles == 0) return fail(SFWI_E_STATE, "no batch on the device (none run, or the last run failed)");
     CK(cudaSetDevice(h->device));
     const Params p = make_params(h, false);
     const bool born = h->stage == 2;
@@ -1438,7 +1442,7 @@ int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
 int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     if (int rc = check(h)) return rc;
     if (reps < 1) return fail(SFWI_E_ARG, "bad argument");
-    if (h->b.ntiles == 0 || !h->b.grid.p) return fail(SFWI_E_STATE, "no batch has been run");
+    if (!h->b.ready || h->b.ntiles == 0) return fail(SFWI_E_STATE, "no batch on the device (none run, or the last run failed)");
     if (h->last_forward_only) return fail(SFWI_E_STATE, "the last run was forward-only (no edge strips)");
     CK(cudaSetDevice(h->device));
     // one gradient step of the batch (the four step kernels) per tile shape;
@@ -1462,7 +1466,7 @@ int sfwi_wait_selftest(sfwi_handle *h, unsigned tries) {
     if (int rc = check(h)) return rc;
     if (tries < 1 || tries > PIPE_WAIT_LIMIT) return fail(SFWI_E_ARG, "tries must be in 1..%u", PIPE_WAIT_LIMIT);
     Batch &b = h->b;
-    if (b.ntiles < 4 || !b.grid.p) return fail(SFWI_E_STATE, "run a batch of at least 4 tiles first");
+    if (!b.ready || b.ntiles < 4) return fail(SFWI_E_STATE, "run a batch of at least 4 tiles first");
     CK(cudaSetDevice(h->device));
     Params p = make_params(h, h->last_forward_only);
     p.wait_limit = tries;
@@ -1500,7 +1504,7 @@ int sfwi_set_tile_shape(sfwi_handle *h, int shape) {
     if (h->tv == tile_variant(shape)) return SFWI_OK;
     h->tv = tile_variant(shape);
     Batch &b = h->b;
-    if (b.nshots == 0 || !b.grid.p) return SFWI_OK;  // applies to the next batch
+    if (!b.ready || b.nshots == 0) return SFWI_OK;  // applies to the next batch
     // re-tile the resident batch and re-encode its maps for the new boxes
     CK(cudaSetDevice(h->device));
     build_tiles(h);

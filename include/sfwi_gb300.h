@@ -214,6 +214,14 @@ int sfwi_last_timing(sfwi_handle *h, float *fwd_ms, float *bwd_ms, float *other_
  * gradients, already read or accumulated, are untouched). */
 int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
 
+/* Debugging: the packed [X][P] arrays of the batch on the device (X packed
+ * rows: the shots' padded widths in enqueue order; P the padded depth
+ * rounded up to 4).  Arrays 0 .. nstate-1 are the wavefields, PML memory
+ * variables and imaging accumulators (zeroed per run), the rest the
+ * coefficients.  sfwi_debug_read_grid copies X*P floats of one array. */
+int sfwi_debug_grid_shape(sfwi_handle *h, int *X, int *P, int *narrays, int *nstate);
+int sfwi_debug_read_grid(sfwi_handle *h, int array, float *dst);
+
 /* Failure path of the device-side waits, without a fault: runs the tile
  * pipeline of the last batch with a producer that stages nothing and a wait
  * bound of `tries` (1..2^24) mbarrier tries, so the consumers' and the

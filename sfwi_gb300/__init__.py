@@ -256,6 +256,17 @@ class FD2DGPU_ELASTIC:
             shape = TILE_SHAPES.index(shape)
         _lib.check(_lib.load().sfwi_set_tile_shape(self._h, int(shape)))
 
+    def debug_grid(self):
+        """(arrays [narrays, X, P] float32 of the batch on the device, number
+        of state arrays): wavefields, PML memory variables and accumulators
+        first, coefficients after."""
+        X, P, na, ns = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(_lib.load().sfwi_debug_grid_shape(self._h, C.byref(X), C.byref(P), C.byref(na), C.byref(ns)))
+        out = np.zeros((na.value, X.value, P.value), np.float32)
+        for a in range(na.value):
+            _lib.check(_lib.load().sfwi_debug_read_grid(self._h, a, _fp(out[a])))
+        return out, ns.value
+
     def wait_selftest(self, tries=4096):
         """Make the device-side pipeline waits of the last batch's tile
         pipeline run out (bounded, no fault); raises SfwiError carrying the

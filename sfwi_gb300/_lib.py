@@ -59,6 +59,9 @@ SIGNATURES = {
     "sfwi_set_launch_overlap": (C.c_int, [_h, C.c_int]),
     "sfwi_set_source": (C.c_int, [_h, C.c_int]),
     "sfwi_wait_selftest": (C.c_int, [_h, C.c_uint]),
+    "sfwi_debug_grid_shape": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int)]),
+    "sfwi_debug_read_grid": (C.c_int, [_h, C.c_int, _fp]),
     "sfwi_get_tile_shape": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sfwi_autotune": (C.c_int, [_h, C.c_int, C.POINTER(C.c_int), _fp]),
     "sfwi_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),

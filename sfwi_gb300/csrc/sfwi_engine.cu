@@ -18,6 +18,7 @@
 #include "../../include/sfwi_gb300.h"
 #include <cudaTypedefs.h>
 
+#include <nvtx3/nvToolsExt.h>
 #include "sfwi_launch.h"
 
 
@@ -62,10 +63,12 @@ struct DevBuf {
         const size_t bytes = std::max<size_t>(m, 1) * sizeof(T);
         cudaError_t e = st ? cudaMallocAsync(reinterpret_cast<void **>(&p), bytes, st)
                            : cudaMalloc(reinterpret_cast<void **>(&p), bytes);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess) {
             n = m;
-        else
+        } else {
             p = nullptr;
+            cudaGetLastError();  // the failure is returned here; later launch checks must not see it again
+        }
         return e;
     }
     void release() {
@@ -695,6 +698,11 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     const int misfit_kind = h->force_l2 ? SFWI_MISFIT_L2 : h->misfit_kind;
     h->last_forward_only = forward_only;
     CK(cudaSetDevice(h->device));
+    // NVTX ranges mark the host side of each phase for timeline profilers
+    struct NvtxRange {
+        explicit NvtxRange(const char *n) { nvtxRangePushA(n); }
+        ~NvtxRange() { nvtxRangePop(); }
+    } nvtx_run("sfwi run_batch");
     if (h->tile_auto) pick_tile_shape(h, shots);
     h->b.ready = false;  // until this batch is on the device
     int rc = build_batch(h, shots);
@@ -719,6 +727,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
         }
         b.gsig = sig;
     }
+    nvtxMarkA("sfwi forward sweeps");
     CK(cudaEventRecord(h->ev[0], st));
     if (h->use_graphs)
         CK(cudaGraphLaunch(b.gfwd, st));
@@ -747,6 +756,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
         return SFWI_OK;
     }
     // adjoint source and misfit
+    nvtxMarkA("sfwi misfit");
     if (misfit_kind == SFWI_MISFIT_L2) {
         launch_residual_l2(h->stage, nt, b.ntr_tot, b.r(R_SYN_Z, nt), b.r(R_SYN_X, nt), b.r(R_SYN2_Z, nt),
                            b.r(R_SYN2_X, nt), b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), b.r(R_RES_Z, nt), b.r(R_RES_X, nt),
@@ -776,6 +786,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     h->launches++;
     h->launches++;
     CK(cudaGetLastError());
+    nvtxMarkA("sfwi backward sweeps");
     CK(cudaEventRecord(h->ev[2], st));
     if (h->use_graphs)
         CK(cudaGraphLaunch(b.gbwd, st));
@@ -1460,6 +1471,27 @@ int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     }
     if (choice) *choice = pick;
     return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_debug_grid_shape(sfwi_handle *h, int *X, int *P, int *narrays, int *nstate) {
+    if (int rc = check(h)) return rc;
+    if (!h->b.ready) return fail(SFWI_E_STATE, "no batch on the device");
+    if (X) *X = h->b.X;
+    if (P) *P = h->b.P;
+    if (narrays) *narrays = NGRID;
+    if (nstate) *nstate = NSTATE;
+    return SFWI_OK;
+}
+
+int sfwi_debug_read_grid(sfwi_handle *h, int array, float *dst) {
+    if (int rc = check(h)) return rc;
+    if (!dst || array < 0 || array >= NGRID) return fail(SFWI_E_ARG, "bad array %d", array);
+    Batch &b = h->b;
+    if (!b.ready) return fail(SFWI_E_STATE, "no batch on the device");
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync(dst, b.g(array), b.cells * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return SFWI_OK;
 }
 
 int sfwi_wait_selftest(sfwi_handle *h, unsigned tries) {

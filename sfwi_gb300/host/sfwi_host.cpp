@@ -46,7 +46,12 @@ int sfwi_su_index(const char *path, int *nt, float *dt, sfwi_su_shot *shots, int
     if (std::fread(h, kHeader, 1, fp.f) != 1) return -1;
     *nt = get_u16(h, kNs);
     *dt = get_u16(h, kDt) / 1000000.0f;
+    if (*nt < 1) return -1;  // no samples: not a record file
     const long long trace_bytes = (long long)*nt * 4;
+    // a file that is not a whole number of traces is truncated or corrupt
+    if (std::fseek(fp.f, 0, SEEK_END) != 0) return -1;
+    const long long size = std::ftell(fp.f);
+    if (size < 0 || size % (kHeader + trace_bytes) != 0) return -1;
     std::fseek(fp.f, 0, SEEK_SET);
     int ns = 0;
     long long pos = 0;

@@ -62,3 +62,27 @@ def test_para_file(tmp_path):
     bad.write_text("10 10\n")
     with pytest.raises(OSError):
         su.read_para(str(bad))
+
+
+def test_corrupt_record_files_are_refused(tmp_path):
+    """A truncated file, a header without samples and a read past the end
+    are reported (OSError from the host library's -1), never crashed on."""
+    path = str(tmp_path / "rec.su")
+    su.write(path, 1000, np.arange(0, 100, 10), np.ones((10, 64), np.float32), 1e-3)
+    good = open(path, "rb").read()
+    trunc = str(tmp_path / "trunc.su")
+    open(trunc, "wb").write(good[:-17])
+    with pytest.raises(OSError):
+        su.index(trunc)
+    with pytest.raises(OSError):
+        su.read(trunc, 9, 1, 64)
+    nosamples = bytearray(good)
+    nosamples[114:116] = b"\x00\x00"
+    bad = str(tmp_path / "ns0.su")
+    open(bad, "wb").write(bytes(nosamples))
+    with pytest.raises(OSError):
+        su.index(bad)
+    with pytest.raises(OSError):
+        su.read(path, 5, 10, 64)  # traces 5..14 of a 10-trace file
+    with pytest.raises(OSError):
+        su.index(str(tmp_path / "missing.su"))

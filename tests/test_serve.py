@@ -89,3 +89,30 @@ def test_request_gives_the_same_result_alone_and_in_the_mix():
         assert a[0] == r.misfit
         for x, y in zip(a[1:], (r.grad_pp, r.grad_ps, r.illum)):
             assert np.array_equal(x, y)
+
+
+def test_a_budget_of_zero_refuses_every_request():
+    reqs = _fake_requests([1, 2], [0.0, 0.0])
+    srv = serve.Server(0, max_active=4, runner=Recorder(), sizer=lambda r: r.size)
+    with pytest.raises(ValueError, match="more than the whole budget"):
+        srv.run(reqs)
+
+
+def test_a_failing_request_is_reported_and_frees_its_slot():
+    """A runner that dies in one request (its worker thread ends with an
+    exception): the others still run to completion or are not started, the
+    failure reaches the caller, and no slot or budget stays taken."""
+    rec = Recorder(dur=0.02)
+
+    def runner(r):
+        if r.rid == 1:
+            raise RuntimeError("request 1 failed")
+        return rec(r)
+
+    reqs = _fake_requests([10, 10, 10, 10], [0.0, 0.0, 0.01, 0.02])
+    srv = serve.Server(20, max_active=2, runner=runner, sizer=lambda r: r.size)
+    t = time.perf_counter()
+    with pytest.raises(RuntimeError, match="request 1 failed"):
+        srv.run(reqs)
+    assert time.perf_counter() - t < 5.0
+    assert rec.active == 0 and rec.bytes == 0

@@ -1,16 +1,20 @@
 // sfwi_kernels.cu — the time-step kernels of the shot-gradient path.
 //
 // One launch advances every shot of a batch by one sweep.  The work is cut
-// into TX x TZ tiles (32 x 32 cells of one shot).  Each kernel is persistent:
-// one CTA per SM walks the tile list, and a two-stage TMA pipeline
-// (cp.async.bulk.tensor into shared memory, completion on an mbarrier) loads
-// tile k+1 while tile k is computed.  Per tile the pipeline stages
+// into TX x TZ tiles of one shot; this file is compiled once per tile shape
+// (SFWI_TILE_X, SFWI_TILE_Z, SFWI_CTAS, SFWI_STAGES, SFWI_CPT) into its own
+// namespace, and the engine picks a shape per batch.  Each kernel is
+// persistent: CTAS_PER_SM CTAs per SM walk the tile list (dynamic draws from
+// a per-launch counter), and an NSTAGE-stage TMA pipeline (cp.async.bulk.tensor
+// into shared memory, completion on an mbarrier) loads the next tiles while
+// one is computed.  Per tile the pipeline stages
 //   - the fields read by the stencils as (TX+8) x (TZ+8) boxes (4-cell halo;
 //     cells outside the packed arrays arrive as zeros), and
 //   - the cell's own state and coefficients as TX x TZ core tiles,
-// and the threads write their updated cells with float4 stores.  A single
-// 3-D tensor map [array][row][column] over the packed grid addresses every
-// array (sfwi_common.cuh).
+// and each compute thread updates CPT consecutive cells (float4 or float2
+// accesses, FP32x2 arithmetic) and writes them with one vector store.  A
+// single 3-D tensor map [array][row][column] over the packed grid addresses
+// every array (sfwi_common.cuh).
 //
 //   k_fwd_v   forward velocity sweep  (update_vx_vz, sfwi-stage1/born.cu:355-394)
 //             of the background and, for the Born forward, the scattered field

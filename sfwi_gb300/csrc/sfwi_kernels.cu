@@ -538,13 +538,14 @@ __device__ __forceinline__ void load_cores(float *dst, const TmaMaps &tm, const 
 }
 
 // Warp-specialised tile pipeline.  Warp NTHREADS/32 is the producer: its lane
-// 0 takes the next tile index from this launch's counter (atomicAdd; SMs that
-// drew cheap tiles take more of them), stores the tile's context in shared
-// memory, and starts the tile's TMA loads on full[stage] once the consumers
-// have released that stage (empty[stage]).  The NTHREADS consumer threads
-// wait on full[stage], run body(ctx, stage_ptr), and release the stage one
-// arrival per warp.  Every wait is bounded; a wait that gives up sets the
-// error flag and the CTA winds down without leaving a copy in flight.
+// 0 draws tile indices from this launch's counter (atomicAdd, one tile ahead;
+// SMs that drew cheap tiles take more of them), reads each tile's 64-byte
+// record, stores the tile's context in shared memory, and starts the tile's
+// TMA loads on full[stage] once the consumers have released that stage
+// (empty[stage]).  The NTHREADS consumer threads wait on full[stage], run
+// body(ctx, stage_ptr), and release the stage one arrival per thread.  Every
+// wait is bounded by p.wait_limit tries; a wait that gives up sets the error
+// flag and the CTA winds down without leaving a copy in flight.
 //   issue(ctx, stage_ptr, bar):    producer lane 0, arms `bar` with expect_tx first
 //   body(ctx, stage_ptr, release): consumers; may use consumer_sync(); calls
 //                                  release() once its reads of the stage are

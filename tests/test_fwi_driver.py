@@ -87,3 +87,25 @@ def test_stage1_and_stage2_drivers(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     img = np.fromfile(os.path.join(s["out"] + "2", "sum_image_pp_1_%d_%d.dat" % shape), np.float32)
     assert np.all(np.isfinite(img)) and np.abs(img).max() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opts", [["--misfit", "ot"], ["--snapshots", "4", "f16"], ["--source", "vz"],
+                                  ["--misfit", "ot_alltrace", "--snapshots", "2", "bf16"]])
+def test_driver_options(tmp_path, opts):
+    """The driver's misfit, snapshot and source options: two stage-1
+    iterations run and write finite, updated models; with the L2 misfit and
+    the source the observed data were modelled with, the misfit decreases."""
+    from sfwi_gb300 import su
+    s = _survey(tmp_path)
+    r = subprocess.run([su.DRIVER, s["para"], "--stage", "1", "--iters", "2"] + opts, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    log = open(os.path.join(s["out"], "misfit.txt")).read()
+    m = [float(l.split("misfit = ")[1].split(",")[0]) for l in log.splitlines() if "misfit =" in l]
+    assert len(m) == 2 and all(np.isfinite(m)), log
+    if "--misfit" not in opts and "--source" not in opts:
+        assert m[1] < m[0], log
+    shape = (s["allnx"], s["allnz"])
+    v1 = np.fromfile(os.path.join(s["out"], "vel_p_1_%d_%d.dat" % shape), np.float32).reshape(shape)
+    assert np.all(np.isfinite(v1)) and not np.array_equal(v1, s["vp0"])

@@ -25,8 +25,15 @@ OBJDIR = os.path.join(ROOT, "_build", "obj")
 # thread, name), then the rest
 TILE_SHAPES = [(16, 32, 2, 2, 4, "16x32"), (32, 32, 1, 2, 4, "32x32"), (16, 64, 1, 2, 4, "16x64"),
                (8, 32, 3, 2, 4, "8x32x3"), (16, 32, 2, 2, 2, "16x32c2"), (8, 32, 2, 3, 2, "8x32c2s3")]
+# The step kernels build with -fmad=false: the compiler would otherwise fuse a
+# multiply into a following add where the product has no other use, so one
+# cell's update could round differently in a tile with PML cells (where the
+# products also feed the split update) than in an interior tile.  Every fused
+# multiply-add in them is written out (fma intrinsics), so results do not
+# depend on the tile shape.
 UNITS = [("sfwi_kernels.cu", "sfwi_kernels_%s.o" % n,
-          ["-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c, "-DSFWI_STAGES=%d" % ns,
+          ["-fmad=false",
+           "-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c, "-DSFWI_STAGES=%d" % ns,
            "-DSFWI_CPT=%d" % cpt, "-DSFWI_VARIANT_NS=v%s" % n, "-DSFWI_VARIANT_FN=tile_variant_%s" % n])
          for tx, tz, c, ns, cpt, n in TILE_SHAPES]
 UNITS += [(f, f.replace(".cu", ".o"), []) for f in ("sfwi_aux.cu", "sfwi_ot.cu", "sfwi_engine.cu")]
@@ -53,6 +60,7 @@ def build(force=False, verbose=False):
     os.makedirs(OBJDIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "sfwi_gb300.h"))
+    headers.append(os.path.abspath(__file__))  # the flags and the unit list
     nv = nvcc()
 
     def compile_one(unit):

@@ -284,26 +284,83 @@ void pick_tile_shape(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     h->tv = tile_variant(tiles < 4LL * 2 * std::max(h->nsm, 1) ? SFWI_TILE_8x32_2CELL_3STAGE : SFWI_TILE_16x32);
 }
 
+// Tiles of one axis of length n (with PML width pml) that start at `start`
+// and cover the updated cells [NOP, n-NOP): how many, and how many of them
+// hold a damped cell (index < pml or > n-pml).
+struct AxisTiling {
+    int start, count, frame;
+};
+AxisTiling axis_tiling(int n, int pml, int t, int start) {
+    AxisTiling a{start, (n - NOP - start + t - 1) / t, 0};
+    for (int k = 0; k < a.count; k++) {
+        const int lo = std::max(start + k * t, NOP), hi = std::min(start + (k + 1) * t, n - NOP) - 1;
+        if (lo < pml || hi > n - pml) a.frame++;
+    }
+    return a;
+}
+// Relative step cost of a shot's tiles: a tile holding PML cells also stages
+// damping and x-parts and runs the split update, about twice an interior
+// tile.
+double tiling_cost(const AxisTiling &x, const AxisTiling &z) {
+    const double all = (double)x.count * z.count;
+    return all + (all - (double)(x.count - x.frame) * (z.count - z.frame));
+}
+// The best start of the x tiles of a shot for a given z tiling: any row at or
+// before NOP whose first tile still holds an updated row.
+AxisTiling best_x_tiling(int nxpml, int pml, int tx, const AxisTiling &z) {
+    AxisTiling best = axis_tiling(nxpml, pml, tx, NOP);
+    for (int st = NOP - 1; st > NOP - tx; st--) {
+        const AxisTiling a = axis_tiling(nxpml, pml, tx, st);
+        if (tiling_cost(a, z) < tiling_cost(best, z)) best = a;
+    }
+    return best;
+}
+
 // The tile table of the batch for the handle's tile shape: tiles over each
 // shot's update region [NOP, n-NOP), flagged by what their core or halo box
 // touches (PML frame, edge-strip bands, receiver cells, imaging interior,
 // source cell).
+//
+// The tile grid may start before NOP so that fewer tiles hold PML cells: the
+// z start is one for the batch, the x start one per shot, a function of the
+// shot's width alone.  A TMA copy's first column times the element size must
+// be a multiple of 16 bytes: the boxes start HALO = 4 columns before a tile,
+// so z starts are NOP - 8k, which keeps box columns multiples of 8 (16-bit
+// snapshot boxes) and core columns multiples of 4 (FP32).
+// Cells before the grid are loaded as zeros by TMA and never updated, rows
+// before a shot's first row belong to the shot before it and are only read,
+// and every cell takes the same arithmetic in any tile, so the choice changes
+// no result.
 void build_tiles(sfwi_handle *h) {
     Batch &b = h->b;
     const int pml = h->pml, nzpml = h->nzpml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
+    AxisTiling zt = axis_tiling(nzpml, pml, tz, NOP);
+    double best = 0;
+    static_assert(NOP % 8 == HALO % 8, "box columns NOP - HALO - 8k stay multiples of 8");
+    for (int st = NOP; st > NOP - tz; st -= 8) {
+        const AxisTiling z = axis_tiling(nzpml, pml, tz, st);
+        double cost = 0;
+        for (int s = 0; s < b.nshots; s++) cost += tiling_cost(best_x_tiling(b.geo[s].nxpml, pml, tx, z), z);
+        if (st == NOP || cost < best) {
+            best = cost;
+            zt = z;
+        }
+    }
     b.tiles.clear();
     for (int s = 0; s < b.nshots; s++) {
         const ShotGeo &g = b.geo[s];
         const int nxpml = g.nxpml;
         const std::vector<int> &cols = b.rcols[s];
-        for (int x0 = NOP; x0 < nxpml - NOP; x0 += tx)
-            for (int z0 = NOP; z0 < nzpml - NOP; z0 += tz) {
+        const AxisTiling xt = best_x_tiling(nxpml, pml, tx, zt);
+        for (int x0 = xt.start; x0 < nxpml - NOP; x0 += tx)
+            for (int z0 = zt.start; z0 < nzpml - NOP; z0 += tz) {
                 const int cx1 = std::min(x0 + tx, nxpml - NOP), cz1 = std::min(z0 + tz, nzpml - NOP);
+                const int cx0 = std::max(x0, NOP), cz0 = std::max(z0, NOP);
                 const int bx0 = x0 - halo, bx1 = x0 + tx + halo, bz0 = z0 - halo, bz1 = z0 + tz + halo;
                 int f = 0;
-                // frame: cells with lx < pml, lx > nxpml-pml, lz < pml or lz > nzpml-pml
-                if (x0 < pml || cx1 - 1 > nxpml - pml || z0 < pml || cz1 - 1 > nzpml - pml) f |= TILE_FRAME;
-                if (box_hits(x0, cx1, z0, cz1, pml, nxpml - pml, pml, nzpml - pml)) f |= TILE_IMAGE;
+                // frame: updated cells with lx < pml, lx > nxpml-pml, lz < pml or lz > nzpml-pml
+                if (cx0 < pml || cx1 - 1 > nxpml - pml || cz0 < pml || cz1 - 1 > nzpml - pml) f |= TILE_FRAME;
+                if (box_hits(cx0, cx1, cz0, cz1, pml, nxpml - pml, pml, nzpml - pml)) f |= TILE_IMAGE;
                 if (box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, pml - NOP, pml + NOP) ||
                     box_hits(bx0, bx1, bz0, bz1, pml, nxpml - pml, nzpml - pml - NOP, nzpml - pml + NOP) ||
                     box_hits(bx0, bx1, bz0, bz1, pml - NOP, pml + NOP, pml, nzpml - pml) ||

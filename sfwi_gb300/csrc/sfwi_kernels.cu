@@ -298,6 +298,8 @@ struct CellMap {
     bool live;    // the row is updated and the first cell's column < nzpml-NOP
     bool ok[CPT];     // cell inside the update region
     bool image[CPT];  // inside the imaging interior [pml, n-pml)
+    bool split[CPT];  // updated cell with PML damping: the split update
+    bool any_split;   // one of the thread's cells has the split update
 };
 
 __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, const ShotGeo &g) {
@@ -310,14 +312,24 @@ __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, cons
     m.lz = t.z0 + CPT * tz;
     m.gi = (size_t)(g.row0 + m.lx) * p.P + m.lz;
     const bool row_ok = m.lx >= NOP && m.lx < g.nxpml - NOP;
-    m.live = row_ok && m.lz < p.nzpml - NOP;  // lz is a multiple of CPT and P of 4, so lz+CPT-1 < P
+    // lz is a multiple of CPT, as are NOP and P: the thread's cells lie wholly
+    // before NOP (a tile grid may start there; not live) or at or after it,
+    // and lz+CPT-1 < P
+    m.live = row_ok && m.lz >= NOP && m.lz < p.nzpml - NOP;
     const int pml = p.pml, nzpml = p.nzpml, nxpml = g.nxpml;
     const bool xi = m.lx >= pml && m.lx < nxpml - pml;
+    // damping is non-zero exactly for lx < pml, lx > nxpml-pml, lz < pml or
+    // lz > nzpml-pml (k_setup); every other cell takes the plain update in
+    // any tile, so results do not depend on how the grid is tiled
+    const bool xd = m.lx < pml || m.lx > nxpml - pml;
+    m.any_split = false;
 #pragma unroll
     for (int j = 0; j < CPT; j++) {
         const int z = m.lz + j;
         m.ok[j] = row_ok && z >= NOP && z < nzpml - NOP;
         m.image[j] = m.ok[j] && xi && z >= pml && z < nzpml - pml;
+        m.split[j] = m.ok[j] && (xd || z < pml || z > nzpml - pml);
+        m.any_split |= m.split[j];
     }
     return m;
 }
@@ -361,6 +373,12 @@ __device__ __forceinline__ void sel2(float v[CPT], int h, float2 x, const bool o
     if (ok[2 * h]) v[2 * h] = x.x;
     if (ok[2 * h + 1]) v[2 * h + 1] = x.y;
 }
+// in a tile with PML cells: the split result where the cell is damped, the
+// plain one in the other updated cells
+__device__ __forceinline__ void pick2(float v[CPT], int h, float2 split, float2 plain, const CellMap &m) {
+    if (m.ok[2 * h]) v[2 * h] = m.split[2 * h] ? split.x : plain.x;
+    if (m.ok[2 * h + 1]) v[2 * h + 1] = m.split[2 * h + 1] ? split.y : plain.y;
+}
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
@@ -386,31 +404,34 @@ __device__ __forceinline__ void v_apply(const Params &p, const CellMap &m, const
         stc(f.vz + m.gi, s.vz);
         return;
     }
-    // tile with PML cells: the split update of the reference for every cell,
+    // tile with PML cells: the split update of the reference in damped cells,
     //   v_x = (d1 v_x + c_x D_x) r2,  v_z = (d3 v_z + c_z D_z) r4,  v = v_x + v_z,
-    // with the x-part kept in mx and the z-part = v - mx (damping factors are
-    // 1 away from the PML); cells outside the update region keep their values
+    // with the x-part kept in mx and the z-part = v - mx; the plain update
+    // above in the tile's other cells; cells outside the update region keep
+    // their values
     {
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
         for (int h = 0; h < NP; h++) {
             const float2 i2 = P2(ib, h);
             const float2 cx = mul2(i2, tx), cz2 = mul2(i2, tz);
+            const float2 px = add2(P2(s.vx, h), fma2(cx, P2(ax.v, h), mul2(cz2, P2(bz.v, h))));
+            const float2 pz = add2(P2(s.vz, h), fma2(cx, P2(dx_.v, h), mul2(cz2, P2(cz.v, h))));
             const float2 d1 = P2(d.d1, h), r2 = P2(d.r2, h), d3 = P2(d.d3, h), r4 = P2(d.r4, h);
             const float2 mx = P2(s.mx, h), mz = P2(s.mz, h);
             const float2 xx = mul2(fma2(d1, mx, mul2(cx, P2(ax.v, h))), r2);
             const float2 xz = mul2(fma2(d3, fma2(mx, neg, P2(s.vx, h)), mul2(cz2, P2(bz.v, h))), r4);
             const float2 zx = mul2(fma2(d1, mz, mul2(cx, P2(dx_.v, h))), r2);
             const float2 zz = mul2(fma2(d3, fma2(mz, neg, P2(s.vz, h)), mul2(cz2, P2(cz.v, h))), r4);
-            sel2(s.mx, h, xx, m.ok);
-            sel2(s.mz, h, zx, m.ok);
-            sel2(s.vx, h, add2(xx, xz), m.ok);
-            sel2(s.vz, h, add2(zx, zz), m.ok);
+            sel2(s.mx, h, xx, m.split);
+            sel2(s.mz, h, zx, m.split);
+            pick2(s.vx, h, add2(xx, xz), px, m);
+            pick2(s.vz, h, add2(zx, zz), pz, m);
         }
     }
     stc(f.vx + m.gi, s.vx);
     stc(f.vz + m.gi, s.vz);
-    if (FRAME) {
+    if (m.any_split) {
         stc(f.mvx + m.gi, s.mx);
         stc(f.mvz + m.gi, s.mz);
     }
@@ -440,16 +461,17 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             }
             S2(s.xx, h, add2(xx, fma2(l2m, ax, mul2(l, bz))));
             S2(s.zz, h, add2(zz, fma2(l, ax, mul2(l2m, bz))));
-            S2(s.xz, h, add2(xz, mul2(u, add2(dx_, cz))));
+            S2(s.xz, h, fma2(u, fma2(tz, P2(c.v, h), dx_), xz));
         }
         stc(f.txx + m.gi, s.xx);
         stc(f.tzz + m.gi, s.zz);
         stc(f.txz + m.gi, s.xz);
         return;
     }
-    // tile with PML cells: the split updates of the reference for every cell
+    // tile with PML cells: the split updates of the reference in damped cells
     // (x-parts in mxx, mzz, mxz; z-part = total - x-part), Born increments
-    // added to the split parts before the damping
+    // added to the split parts before the damping; the plain update above in
+    // the tile's other cells
     {
         const float2 tx = B2(dir * p.dtdx), tz = B2(dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
@@ -458,6 +480,15 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             const float2 l2m = fma2(u, B2(2.f), l);
             const float2 ax = mul2(tx, P2(a.v, h)), bz = mul2(tz, P2(b.v, h));
             const float2 cz = mul2(tz, P2(c.v, h)), dx_ = mul2(tx, P2(d.v, h));
+            float2 pxx = P2(s.xx, h), pzz = P2(s.zz, h), pxz = P2(s.xz, h);
+            if (born) {
+                pxx = add2(pxx, add2(P2(born[0], h), P2(born[1], h)));
+                pzz = add2(pzz, add2(P2(born[2], h), P2(born[3], h)));
+                pxz = add2(pxz, add2(P2(born[4], h), P2(born[5], h)));
+            }
+            pxx = add2(pxx, fma2(l2m, ax, mul2(l, bz)));
+            pzz = add2(pzz, fma2(l, ax, mul2(l2m, bz)));
+            pxz = fma2(u, fma2(tz, P2(c.v, h), dx_), pxz);
             const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
             float2 mxx = P2(s.mxx, h), mzz = P2(s.mzz, h), mxz = P2(s.mxz, h);
             float2 zxx = fma2(mxx, neg, P2(s.xx, h)), zzz = fma2(mzz, neg, P2(s.zz, h));
@@ -476,18 +507,18 @@ __device__ __forceinline__ void s_apply(const Params &p, const CellMap &m, const
             const float2 nzz_z = mul2(fma2(d3, zzz, mul2(l2m, bz)), r4);
             const float2 nxz_x = mul2(fma2(d1, mxz, mul2(u, dx_)), r2);
             const float2 nxz_z = mul2(fma2(d3, zxz, mul2(u, cz)), r4);
-            sel2(s.mxx, h, nxx_x, m.ok);
-            sel2(s.mzz, h, nzz_x, m.ok);
-            sel2(s.mxz, h, nxz_x, m.ok);
-            sel2(s.xx, h, add2(nxx_x, nxx_z), m.ok);
-            sel2(s.zz, h, add2(nzz_x, nzz_z), m.ok);
-            sel2(s.xz, h, add2(nxz_x, nxz_z), m.ok);
+            sel2(s.mxx, h, nxx_x, m.split);
+            sel2(s.mzz, h, nzz_x, m.split);
+            sel2(s.mxz, h, nxz_x, m.split);
+            pick2(s.xx, h, add2(nxx_x, nxx_z), pxx, m);
+            pick2(s.zz, h, add2(nzz_x, nzz_z), pzz, m);
+            pick2(s.xz, h, add2(nxz_x, nxz_z), pxz, m);
         }
     }
     stc(f.txx + m.gi, s.xx);
     stc(f.tzz + m.gi, s.zz);
     stc(f.txz + m.gi, s.xz);
-    if (FRAME) {
+    if (m.any_split) {
         stc(f.mtxx + m.gi, s.mxx);
         stc(f.mtzz + m.gi, s.mzz);
         stc(f.mtxz + m.gi, s.mxz);
@@ -910,7 +941,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // snapshot of the background velocity after this step (the staged box
         // holds it): the tile's core cells of this shot's rows and of the
         // row pitch (a tile's last columns can reach past it)
-        if (snap_step(p, it) && m.lx < c.g.nxpml && m.lz < p.PS) {
+        if (snap_step(p, it) && m.lx >= 0 && m.lx < c.g.nxpml && m.lz >= 0 && m.lz < p.PS) {
             const int k = it / p.snap_every;
             const size_t cell = (size_t)(c.g.row0 + m.lx) * p.PS + m.lz;
             const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
@@ -1010,28 +1041,32 @@ __device__ __forceinline__ void adjoint_stress(const Params &p, const CellMap &m
         for (int h = 0; h < NP; h++) {
             S2(axx, h, fma2(tx, P2(aa.v, h), P2(axx, h)));
             S2(azz, h, fma2(tz, P2(ba.v, h), P2(azz, h)));
-            S2(axz, h, add2(P2(axz, h), add2(mul2(tx, P2(da.v, h)), mul2(tz, P2(ca.v, h)))));
+            S2(axz, h, add2(P2(axz, h), fma2(tx, P2(da.v, h), mul2(tz, P2(ca.v, h)))));
         }
     } else {
-        // PML tile: damping factors are 1 away from the PML
+        // tile with PML cells: the split update in damped cells, the plain
+        // one above in the others
         const float2 tx = B2(adj_dir * p.dtdx), tz = B2(adj_dir * p.dtdz), neg = B2(-1.f);
 #pragma unroll
         for (int h = 0; h < NP; h++) {
+            const float2 pxx = fma2(tx, P2(aa.v, h), P2(axx, h));
+            const float2 pzz = fma2(tz, P2(ba.v, h), P2(azz, h));
+            const float2 pxz = add2(P2(axz, h), fma2(tx, P2(da.v, h), mul2(tz, P2(ca.v, h))));
             const float2 d1 = P2(dm.d1, h), r2 = P2(dm.r2, h), d3 = P2(dm.d3, h), r4 = P2(dm.r4, h);
             const float2 nxx = mul2(fma2(d1, P2(axx, h), mul2(tx, P2(aa.v, h))), r2);
             const float2 nzz = mul2(fma2(d3, P2(azz, h), mul2(tz, P2(ba.v, h))), r4);
             const float2 nx_ = mul2(fma2(d1, P2(amxz, h), mul2(tx, P2(da.v, h))), r2);
             const float2 nz_ = mul2(fma2(d3, fma2(P2(amxz, h), neg, P2(axz, h)), mul2(tz, P2(ca.v, h))), r4);
-            sel2(axx, h, nxx, m.ok);
-            sel2(azz, h, nzz, m.ok);
-            sel2(amxz, h, nx_, m.ok);
-            sel2(axz, h, add2(nx_, nz_), m.ok);
+            pick2(axx, h, nxx, pxx, m);
+            pick2(azz, h, nzz, pzz, m);
+            sel2(amxz, h, nx_, m.split);
+            pick2(axz, h, add2(nx_, nz_), pxz, m);
         }
     }
     stc(p.ad.txx + m.gi, axx);
     stc(p.ad.tzz + m.gi, azz);
     stc(p.ad.txz + m.gi, axz);
-    if (frame) stc(p.ad.mtxz + m.gi, amxz);
+    if (frame && m.any_split) stc(p.ad.mtxz + m.gi, amxz);
 }
 
 // zero-lag imaging of the lambda and mu kernels (doimage_gradient,
@@ -1285,9 +1320,9 @@ __device__ __forceinline__ void lame_weight(float *s_P, float *s_Q, float *s_R, 
         f4_to(ld4(s_u + 4 * i), u);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            const float l2m = l[j] + 2 * u[j];
-            P_[j] = l2m * xx[j] + l[j] * zz[j];
-            Q_[j] = l[j] * xx[j] + l2m * zz[j];
+            const float l2m = fmaf(2.f, u[j], l[j]);
+            P_[j] = fmaf(l2m, xx[j], l[j] * zz[j]);
+            Q_[j] = fmaf(l[j], xx[j], l2m * zz[j]);
             R_[j] = u[j] * xz[j];
         }
         st4(s_P + 4 * i, to_f4(P_));
@@ -1384,8 +1419,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (rho_img) {
 #pragma unroll
             for (int j = 0; j < CPT; j++) {
-                gvx[j] = ib[j] * (ax.v[j] * p.idx + bz.v[j] * p.idz);
-                gvz[j] = ib[j] * (dx_.v[j] * p.idx + cz.v[j] * p.idz);
+                gvx[j] = ib[j] * fmaf(ax.v[j], p.idx, bz.v[j] * p.idz);
+                gvz[j] = ib[j] * fmaf(dx_.v[j], p.idx, cz.v[j] * p.idz);
             }
         }
         if (frame)
@@ -1395,7 +1430,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         if (image) {
 #pragma unroll
             for (int j = 0; j < CPT; j++)
-                if (m.image[j]) il[j] += bg.vx[j] * bg.vx[j] + bg.vz[j] * bg.vz[j];
+                if (m.image[j]) il[j] += fmaf(bg.vx[j], bg.vx[j], bg.vz[j] * bg.vz[j]);
             stc(p.illum + m.gi, il);
         }
         if (frame)
@@ -1407,7 +1442,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 
 #pragma unroll
             for (int j = 0; j < CPT; j++)
-                if (m.image[j]) gr[j] -= ad.vx[j] * gvx[j] + ad.vz[j] * gvz[j];
+                if (m.image[j]) gr[j] -= fmaf(ad.vx[j], gvx[j], ad.vz[j] * gvz[j]);
             stc(p.grho + m.gi, gr);
         }
     };
@@ -1510,7 +1545,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             image_lam_mu(p, m, w, a, b, cc, d, axx, azz, axz, gl, gm);
 #pragma unroll
             for (int j = 0; j < CPT; j++)
-                if (m.image[j]) il[j] += w * (vx[j] * vx[j] + vz[j] * vz[j]);
+                if (m.image[j]) il[j] += w * fmaf(vx[j], vx[j], vz[j] * vz[j]);
             stc(p.glam + m.gi, gl);
             stc(p.gmu + m.gi, gm);
             stc(p.illum + m.gi, il);

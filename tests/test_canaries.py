@@ -23,9 +23,9 @@ pytestmark = pytest.mark.gpu
 NOP = 4
 
 
-def _run(stage, tile, snap=None, source=0, uneven=True):
+def _run(stage, tile, snap=None, source=0, uneven=True, grid=None):
     import sfwi_gb300 as sg
-    cfg, model, shots = _batch_inputs(stage, nshots=3, uneven=uneven)
+    cfg, model, shots = _batch_inputs(stage, nshots=3, uneven=uneven, **(grid or {}))
     pml, allnx, allnz, nt = cfg["pml"], cfg["allnx"], cfg["allnz"], cfg["nt"]
     maxnx = max(d["nx"] for d in shots)
     fd = sg.FD2DGPU_ELASTIC(model["sou"], cfg["dx"], cfg["dx"], cfg["dt"], maxnx + 2 * pml, allnz + 2 * pml, allnx,
@@ -73,6 +73,14 @@ def test_no_writes_outside_the_update_region_for_every_tile_shape(tile):
                                                (2, (1, "f32"), 0)])
 def test_no_writes_outside_the_update_region_in_every_mode(stage, snap, source):
     _check(*_run(stage, "16x32", snap=snap, source=source))
+
+
+@pytest.mark.parametrize("tile", ["16x32", "32x32", "8x32c2s3"])
+def test_no_writes_outside_the_update_region_with_tile_grids_starting_early(tile):
+    """On this grid the tile grids start before the first updated row and
+    column (fewer tiles hold PML cells): the cells there are loaded as zeros
+    or from the shot before and must not be written."""
+    _check(*_run(2, tile, grid=dict(allnx=150, allnz=83, pml=11, nt=120)))
 
 
 def test_batch_larger_than_the_gpu_is_refused_and_the_handle_keeps_working():

@@ -346,10 +346,12 @@ __device__ __forceinline__ Damp make_damp(const Params &p, const float x[CPT], c
     Damp d;
 #pragma unroll
     for (int j = 0; j < CPT; j++) {
-        d.d1[j] = 1.f - p.dt * x[j] / 2;
-        d.r2[j] = __frcp_rn(1.f + p.dt * x[j] / 2);
-        d.d3[j] = 1.f - p.dt * z[j] / 2;
-        d.r4[j] = __frcp_rn(1.f + p.dt * z[j] / 2);
+        // 1 -+ (dt d)/2: halving is exact, so one fused step rounds once
+        const float tx = p.dt * x[j], tz = p.dt * z[j];
+        d.d1[j] = fmaf(tx, -0.5f, 1.f);
+        d.r2[j] = __frcp_rn(fmaf(tx, 0.5f, 1.f));
+        d.d3[j] = fmaf(tz, -0.5f, 1.f);
+        d.r4[j] = __frcp_rn(fmaf(tz, 0.5f, 1.f));
     }
     return d;
 }
@@ -1082,13 +1084,17 @@ __device__ __forceinline__ void image_lam_mu(const Params &p, const CellMap &m, 
         const float2 gxx = mul2(P2(a.v, h), B2(p.idx)), gzz = mul2(P2(b.v, h), B2(p.idz));
         const float2 gxz = mul2(P2(cc.v, h), B2(p.idz)), gzx = mul2(P2(d.v, h), B2(p.idx));
         const float2 x2 = P2(axx, h), z2 = P2(azz, h);
-        float2 lg = mul2(B2(-1.f), mul2(add2(gxx, gzz), add2(x2, z2)));
-        float2 mg = fma2(B2(-2.f), fma2(gxx, x2, mul2(gzz, z2)), mul2(B2(-1.f), mul2(add2(gxz, gzx), P2(axz, h))));
-        if (w != 1.f) {
-            lg = mul2(B2(w), lg);
-            mg = mul2(B2(w), mg);
+        // the increments are -lg and -mg (negation is exact)
+        const float2 lg = mul2(add2(gxx, gzz), add2(x2, z2));
+        const float2 mg = fma2(B2(2.f), fma2(gxx, x2, mul2(gzz, z2)), mul2(add2(gxz, gzx), P2(axz, h)));
+        float2 ngl, ngm;
+        if (w == 1.f) {
+            ngl = fma2(B2(-1.f), lg, P2(gl, h));
+            ngm = fma2(B2(-1.f), mg, P2(gm, h));
+        } else {
+            ngl = add2(P2(gl, h), mul2(B2(-w), lg));
+            ngm = add2(P2(gm, h), mul2(B2(-w), mg));
         }
-        const float2 ngl = add2(P2(gl, h), lg), ngm = add2(P2(gm, h), mg);
         if (m.image[2 * h]) {
             gl[2 * h] = ngl.x;
             gm[2 * h] = ngm.x;
@@ -1545,7 +1551,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             image_lam_mu(p, m, w, a, b, cc, d, axx, azz, axz, gl, gm);
 #pragma unroll
             for (int j = 0; j < CPT; j++)
-                if (m.image[j]) il[j] += w * fmaf(vx[j], vx[j], vz[j] * vz[j]);
+                if (m.image[j]) il[j] = fmaf(w, fmaf(vx[j], vx[j], vz[j] * vz[j]), il[j]);
             stc(p.glam + m.gi, gl);
             stc(p.gmu + m.gi, gm);
             stc(p.illum + m.gi, il);

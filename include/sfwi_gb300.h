@@ -260,9 +260,11 @@ int sfwi_set_source(sfwi_handle *h, int kind);
 /* Select the tile shape for this handle's runs.  Until one is selected (here
  * or by sfwi_autotune) each batch gets SFWI_TILE_16x32, or
  * SFWI_TILE_8x32_2CELL_3STAGE when its 16x32 tiles would give fewer than four
- * to each of the device's CTA slots (small batches).  A batch already on the device is re-tiled.
- * Results do not depend on the shape: they are bit-identical, since every
- * cell's update reads the same values in the same order. */
+ * to each of the device's CTA slots (small batches).  A batch already on
+ * the device is re-tiled.  Results do not depend on the shape: they are
+ * bit-identical, since every cell takes the same update (split where the cell
+ * is damped, plain elsewhere, whatever its tile holds), reads the same values
+ * and rounds in the same order. */
 int sfwi_set_tile_shape(sfwi_handle *h, int shape);
 /* Launch the time-step kernels with programmatic dependent launch (default
  * on): each may be scheduled while the previous one drains and waits for its

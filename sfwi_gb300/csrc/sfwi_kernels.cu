@@ -37,6 +37,12 @@
 // nonzero) also keep the x-part; the z-part is total minus x-part.  Away from
 // the frame the split update reduces to total += dir*coef*(Dx + Dz).
 //
+// Which update a cell takes depends on the cell alone (split where damped,
+// plain elsewhere), never on the tile that holds it, and this file builds
+// with -fmad=false with every fused multiply-add written as an intrinsic, so
+// no product is fused in one tile shape and not in another: every tile shape
+// and tile-grid origin gives the same bits.
+//
 // Three writes of the reference touch only the total field, never the split
 // parts, so the next split update discards them: the source added to txx/tzz
 // (GPUapplysource, FD2DGPU.cu:2104-2114), the residual assigned into the

@@ -262,17 +262,20 @@ def reference_gpu_sample(w, data, nshots, warm=True):
                       "wall clock per shot"}
 
 
-def run_serving(n, budget_gb=64.0, slots=4):
+def run_serving(n, budget_gb=64.0, slots=4, full=False):
     """Serving loop on a seeded Poisson stream (50 requests/s; grids, nt and
-    shots drawn from the serving configuration's ranges, then scaled by 0.3 in
-    each grid dimension and 0.1 in nt so the stream is served in seconds):
-    continuous admission against an HBM budget vs the plain FIFO loop, each
-    replayed twice and measured on the second replay."""
+    shots drawn from the serving configuration's ranges, then, unless `full`,
+    scaled by 0.3 in each grid dimension and 0.1 in nt so the stream is served
+    in seconds): continuous admission against an HBM budget vs the plain FIFO
+    loop, each replayed twice and measured on the second replay.  At the
+    drawn sizes a request takes about a second of GPU time, so a stream at
+    50/s queues: the latencies then measure the backlog."""
     from sfwi_gb300 import serve
-    reqs = serve.poisson_requests(n, 50.0, seed=4, grid_scale=0.3, nt_scale=0.1)
+    gs, ns = (1.0, 1.0) if full else (0.3, 0.1)
+    reqs = serve.poisson_requests(n, 50.0, seed=4, grid_scale=gs, nt_scale=ns)
     serve.run_request(reqs[0])  # warm the kernels and the allocator
     out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
-           "scale": "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
+           "scale": "the drawn sizes" if full else "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
     for name, srv in (("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
                       ("fifo", serve.Server(budget_gb * 2 ** 30, max_active=1))):
         srv.run(reqs)  # the first replay settles the allocator pools and host threads
@@ -331,6 +334,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=4, help="shots timed one at a time for the plain form")
     ap.add_argument("--serving-requests", type=int, default=48, help="requests of the serving-loop measurement")
+    ap.add_argument("--serving-full", action="store_true",
+                    help="serve the requests at the drawn sizes (200x100 to 2001x1001, nt 2000-6000) unscaled")
     ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     ap.add_argument("--reference-gpu-shots", type=int, default=1,
@@ -541,7 +546,8 @@ def main():
     for pz, px in obs:
         pz.free()
         px.free()
-    serving = run_serving(args.serving_requests) if args.serving_requests > 0 and rank == 0 else None
+    serving = (run_serving(args.serving_requests, full=args.serving_full)
+               if args.serving_requests > 0 and rank == 0 else None)
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": round(value, 3), "unit": "shot-gradients/s", "n_gpus": ws, "steps": args.steps,

@@ -220,6 +220,13 @@ int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms);
  * variables and imaging accumulators (zeroed per run), the rest the
  * coefficients.  sfwi_debug_read_grid copies X*P floats of one array. */
 int sfwi_debug_grid_shape(sfwi_handle *h, int *X, int *P, int *narrays, int *nstate);
+/* Debugging, host only (no device use): the tile grid a batch of shots with
+ * padded widths nxpml[0..nshots-1] and padded depth nzpml gets on tx x tz
+ * tiles.  z_start is the batch's first tile column (NOP - 8k), x_start[s]
+ * each shot's first tile row (at most NOP); tiles[s] and frame_tiles[s]
+ * (optional) count each shot's tiles and those holding PML cells. */
+int sfwi_debug_tile_grid(int pml, int nzpml, int tx, int tz, const int *nxpml, int nshots, int *z_start,
+                         int *x_start, int *tiles, int *frame_tiles);
 int sfwi_debug_read_grid(sfwi_handle *h, int array, float *dst);
 
 /* Failure path of the device-side waits, without a fault: runs the tile

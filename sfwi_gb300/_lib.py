@@ -62,6 +62,8 @@ SIGNATURES = {
     "sfwi_debug_grid_shape": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int)]),
     "sfwi_debug_read_grid": (C.c_int, [_h, C.c_int, _fp]),
+    "sfwi_debug_tile_grid": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _ip, C.c_int, C.POINTER(C.c_int), _ip,
+                                       _ip, _ip]),
     "sfwi_get_tile_shape": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sfwi_autotune": (C.c_int, [_h, C.c_int, C.POINTER(C.c_int), _fp]),
     "sfwi_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),

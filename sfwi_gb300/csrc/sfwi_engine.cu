@@ -331,21 +331,31 @@ AxisTiling best_x_tiling(int nxpml, int pml, int tx, const AxisTiling &z) {
 // before a shot's first row belong to the shot before it and are only read,
 // and every cell takes the same arithmetic in any tile, so the choice changes
 // no result.
-void build_tiles(sfwi_handle *h) {
-    Batch &b = h->b;
-    const int pml = h->pml, nzpml = h->nzpml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
+// The batch's z tiling: the start (NOP - 8k, k >= 0, with an updated column
+// in the first tile) of least summed cost over the shots, each with its best
+// x start; NOP on ties.
+AxisTiling plan_z_tiling(int pml, int nzpml, int tx, int tz, const int *nxpml, int nshots) {
     AxisTiling zt = axis_tiling(nzpml, pml, tz, NOP);
     double best = 0;
     static_assert(NOP % 8 == HALO % 8, "box columns NOP - HALO - 8k stay multiples of 8");
     for (int st = NOP; st > NOP - tz; st -= 8) {
         const AxisTiling z = axis_tiling(nzpml, pml, tz, st);
         double cost = 0;
-        for (int s = 0; s < b.nshots; s++) cost += tiling_cost(best_x_tiling(b.geo[s].nxpml, pml, tx, z), z);
+        for (int s = 0; s < nshots; s++) cost += tiling_cost(best_x_tiling(nxpml[s], pml, tx, z), z);
         if (st == NOP || cost < best) {
             best = cost;
             zt = z;
         }
     }
+    return zt;
+}
+
+void build_tiles(sfwi_handle *h) {
+    Batch &b = h->b;
+    const int pml = h->pml, nzpml = h->nzpml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
+    std::vector<int> widths;
+    for (const ShotGeo &g : b.geo) widths.push_back(g.nxpml);
+    const AxisTiling zt = plan_z_tiling(pml, nzpml, tx, tz, widths.data(), b.nshots);
     b.tiles.clear();
     for (int s = 0; s < b.nshots; s++) {
         const ShotGeo &g = b.geo[s];
@@ -1528,6 +1538,24 @@ int sfwi_autotune(sfwi_handle *h, int reps, int *choice, float *out_ms) {
     }
     if (choice) *choice = pick;
     return sfwi_set_tile_shape(h, pick);
+}
+
+int sfwi_debug_tile_grid(int pml, int nzpml, int tx, int tz, const int *nxpml, int nshots, int *z_start,
+                         int *x_start, int *tiles, int *frame_tiles) {
+    if (!nxpml || !z_start || !x_start || nshots < 1 || pml < NOP || nzpml < 2 * pml + 1 || tx < 1 || tz < 8 ||
+        tz % 8)
+        return fail(SFWI_E_ARG, "bad tile-grid arguments");
+    for (int s = 0; s < nshots; s++)
+        if (nxpml[s] < 2 * pml + 1) return fail(SFWI_E_ARG, "shot %d: padded width %d too small", s, nxpml[s]);
+    const AxisTiling zt = plan_z_tiling(pml, nzpml, tx, tz, nxpml, nshots);
+    *z_start = zt.start;
+    for (int s = 0; s < nshots; s++) {
+        const AxisTiling xt = best_x_tiling(nxpml[s], pml, tx, zt);
+        x_start[s] = xt.start;
+        if (tiles) tiles[s] = xt.count * zt.count;
+        if (frame_tiles) frame_tiles[s] = xt.count * zt.count - (xt.count - xt.frame) * (zt.count - zt.frame);
+    }
+    return SFWI_OK;
 }
 
 int sfwi_debug_grid_shape(sfwi_handle *h, int *X, int *P, int *narrays, int *nstate) {

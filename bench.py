@@ -277,6 +277,7 @@ def run_serving(n, budget_gb=64.0, slots=4, full=False):
     out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
            "scale": "the drawn sizes" if full else "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
     for name, srv in (("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
+                      ("served_shortest_first", serve.Server(budget_gb * 2 ** 30, max_active=slots, policy="shortest")),
                       ("fifo", serve.Server(budget_gb * 2 ** 30, max_active=1))):
         srv.run(reqs)  # the first replay settles the allocator pools and host threads
         res = srv.run(reqs)

@@ -80,6 +80,13 @@ def request_bytes(req):
     return 4 * floats + 8 * 4 * req.allnx * req.allnz + (1 << 20)
 
 
+def request_work(req):
+    """Cell-steps of one request (its shots' padded cells times nt): the
+    order of the shortest-first policy."""
+    P = req.allnz + 2 * req.pml
+    return sum((int(d["nx"]) + 2 * req.pml) * P for d in req.shots) * req.nt
+
+
 def run_request(req):
     """One request on a fresh engine: (misfit, grad_pp, grad_ps, illum)."""
     import sfwi_gb300 as sg
@@ -101,10 +108,20 @@ def run_request(req):
 
 
 class Server:
-    def __init__(self, budget_bytes, max_active=4, runner=run_request, sizer=request_bytes, clock=time.perf_counter):
+    """Admission loop: arrived requests start as slots (max_active) and the
+    HBM budget free up.  policy "oldest" admits in arrival order, letting a
+    later request that fits overtake one that does not; "shortest" admits the
+    request with the least work first (request_work); with max_active=1 the
+    loop is the plain FIFO."""
+
+    def __init__(self, budget_bytes, max_active=4, runner=run_request, sizer=request_bytes, clock=time.perf_counter,
+                 policy="oldest", work=request_work):
+        if policy not in ("oldest", "shortest"):
+            raise ValueError("policy must be 'oldest' or 'shortest'")
         self.budget = int(budget_bytes)
         self.max_active = int(max_active)
         self.runner, self.sizer, self.clock = runner, sizer, clock
+        self.policy, self.work = policy, work
 
     def run(self, requests):
         """Replay `requests` (arrival offsets in seconds) against the wall
@@ -143,8 +160,9 @@ class Server:
                 while nxt < len(reqs) and reqs[nxt].arrival <= t:
                     waiting.append(reqs[nxt])
                     nxt += 1
-                # admit, oldest first, every arrived request that fits
-                for r in list(waiting):
+                # admit every arrived request that fits, oldest or least work first
+                order = list(waiting) if self.policy == "oldest" else sorted(waiting, key=lambda q: (self.work(q), q.rid))
+                for r in order:
                     if state["active"] >= self.max_active:
                         break
                     size = self.sizer(r)

@@ -61,6 +61,18 @@ def test_fifo_runs_one_job_at_a_time_in_arrival_order():
     assert rec.order == [1, 3, 2, 0]
 
 
+def test_shortest_first_admits_the_least_work_among_the_waiting():
+    # one slot; the others arrive while the first runs and start by work
+    reqs = _fake_requests([10, 10, 10, 10], [0.0, 0.001, 0.002, 0.003])
+    work = {0: 5, 1: 30, 2: 10, 3: 20}
+    rec = Recorder(0.05)
+    serve.Server(100, max_active=1, runner=rec, sizer=lambda r: r.size, policy="shortest",
+                 work=lambda r: work[r.rid]).run(reqs)
+    assert rec.order == [0, 2, 3, 1]
+    with pytest.raises(ValueError):
+        serve.Server(100, policy="random")
+
+
 def test_oversized_request_is_refused():
     reqs = _fake_requests([200], [0.0])
     with pytest.raises(ValueError):

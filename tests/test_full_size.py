@@ -11,7 +11,10 @@
     with the OT misfit;
   * the Born records are linear in the model perturbation;
   * one full 38-shot pass gives finite, non-zero gradients with the misfit the
-    per-shot misfits add up to.
+    per-shot misfits add up to;
+  * on the full 376x201 grid (two shots, 400 steps) every tile shape gives
+    the same records and gradients bit for bit: there cells sit in PML tiles
+    under one shape and in interior tiles under another.
 """
 import numpy as np
 import pytest
@@ -147,3 +150,36 @@ def test_full_pass_gives_finite_gradients(survey):
     assert np.isfinite(m) and m > 0 and m == pytest.approx(per.sum(), rel=1e-12)
     for a in g + (grho,):
         assert np.all(np.isfinite(a)) and np.abs(a).max() > 0
+
+
+def test_every_tile_shape_gives_the_same_bits_on_the_full_grid(survey):
+    import sfwi_gb300 as sg
+    w, data = survey
+    nt = 400
+    pml = w["pml"]
+    pick = [data["shots"][i] for i in (3, 20)]
+    obs = [(_inputs(w, data, d, seed=i)["obs_z"][:, :nt].copy(), _inputs(w, data, d, seed=i)["obs_x"][:, :nt].copy())
+           for i, d in enumerate(pick)]
+
+    def run(shape):
+        fd = sg.FD2DGPU_ELASTIC(data["sou"][:nt], w["dx"], w["dx"], w["dt"], w["allnx"] + 2 * pml,
+                                w["allnz"] + 2 * pml, w["allnx"], w["allnz"], 1, pml, nt, 4, pick[0]["ntr"], stage=2)
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"])
+        fd.GPUbufferM(data["dvp"], data["dvs"])
+        fd.set_tile_shape(shape)
+        for d, o in zip(pick, obs):
+            _enqueue(fd, w, data, d, o)
+        m, per = fd.run()
+        out = ([fd.read_records(i, d["ntr"]) for i, d in enumerate(pick)], fd.read_gradients_f64(), per)
+        fd.close()
+        return out
+
+    base = run("16x32")
+    for shape in sg.TILE_SHAPES[1:]:
+        recs, grads, per = run(shape)
+        assert np.array_equal(per, base[2]), shape
+        for a, b in zip(recs, base[0]):
+            for k in a:
+                assert np.array_equal(a[k], b[k]), (shape, k)
+        for a, b in zip(grads, base[1]):
+            assert np.array_equal(a, b), shape

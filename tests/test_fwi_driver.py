@@ -109,3 +109,20 @@ def test_driver_options(tmp_path, opts):
     shape = (s["allnx"], s["allnz"])
     v1 = np.fromfile(os.path.join(s["out"], "vel_p_1_%d_%d.dat" % shape), np.float32).reshape(shape)
     assert np.all(np.isfinite(v1)) and not np.array_equal(v1, s["vp0"])
+
+
+def test_gradient_only_writes_one_gradient_and_no_model(tmp_path):
+    """--gradient-only: one gradient pass, its misfit logged and its raw
+    gradients written, no model update."""
+    from sfwi_gb300 import su
+    s = _survey(tmp_path)
+    r = subprocess.run([su.DRIVER, s["para"], "--stage", "1", "--gradient-only"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    log = open(os.path.join(s["out"], "misfit.txt")).read()
+    assert log.count("misfit =") == 1, log
+    shape = (s["allnx"], s["allnz"])
+    for name in ("sum_grad_pp", "sum_grad_ps", "sum_illum"):
+        g = np.fromfile(os.path.join(s["out"], "%s_0_%d_%d.dat" % ((name,) + shape)), np.float32)
+        assert g.size == shape[0] * shape[1] and np.all(np.isfinite(g)) and np.abs(g).max() > 0, name
+    assert not os.path.exists(os.path.join(s["out"], "vel_p_1_%d_%d.dat" % shape))

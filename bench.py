@@ -333,7 +333,7 @@ def main():
     ap.add_argument("--nt", type=int, default=None, help="override the number of time steps (testing)")
     ap.add_argument("--shots", type=int, default=None, help="override the number of shots (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--plain-shots", type=int, default=4, help="shots timed one at a time for the plain form")
+    ap.add_argument("--plain-shots", type=int, default=8, help="shots timed one at a time for the plain form")
     ap.add_argument("--serving-requests", type=int, default=48, help="requests of the serving-loop measurement")
     ap.add_argument("--serving-full", action="store_true",
                     help="serve the requests at the drawn sizes (200x100 to 2001x1001, nt 2000-6000) unscaled")

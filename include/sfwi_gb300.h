@@ -178,20 +178,23 @@ int sfwi_ot_power(const float *obs_x, const float *obs_z, const float *cal_x, co
 int sfwi_ot_alltrace(const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z, float *res_x,
                      float *res_z, int length, int tracenum, float dt, double *misfit);
 /* Allocation-free OT on device buffers.  No counterpart in the reference.
- * For callers that must not allocate device memory: code recording a CUDA
- * graph (cudaMalloc is not allowed while a stream is captured), programs
- * whose allocator owns all device memory, and latency-bound loops where an
- * allocation may stall the GPU.  obs/cal/res are DEVICE pointers
- * [tracenum][length] on the current device; kind is SFWI_MISFIT_OT,
- * SFWI_MISFIT_OT_POWER or SFWI_MISFIT_OT_ALLTRACE; misfit (host) += W2;
- * stream may be NULL (default stream).  The call waits for its stream.
+ * For callers that cannot allocate device memory: host programs whose own
+ * allocator reserves every device byte up front, and inner loops where a
+ * cudaMalloc/cudaFree could synchronise the device and stall the work of
+ * other streams.  obs/cal/res are DEVICE pointers [tracenum][length] on the
+ * current device; kind is SFWI_MISFIT_OT, SFWI_MISFIT_OT_POWER or
+ * SFWI_MISFIT_OT_ALLTRACE; misfit (host) += W2; stream may be NULL (default
+ * stream).  The call enqueues its kernels on `stream`, then waits for that
+ * stream to reach the misfit read-back.  tracenum = 0 adds nothing and
+ * returns SFWI_OK, as sfwi_ot does.
  * Working memory is a fixed 256 KB array that every device loading the
  * library keeps until the process exits: at most 8192 traces per call (larger
- * calls fail with SFWI_E_ARG) and length <= 7160.  The first call on a device
- * looks up that array's device address, so make it before any stream
- * capture.  All calls on a device share the array: calls that overlap on the
- * GPU (other streams or threads at the same time) race and must be serialised
- * by the caller. */
+ * calls fail with SFWI_E_ARG before any device work) and length <= 7160.
+ * The first call in a CUDA context looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
+ * on a device share the array and each call overwrites what the last one
+ * left there: calls that overlap on the GPU (other streams or threads at the
+ * same time) race on it and must be serialised by the caller. */
 int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z, const float *cal_x, const float *cal_z,
                     float *res_x, float *res_z, int length, int tracenum, float dt, double *misfit, void *stream);
 /* normalize(matrix, length, tracenum), sfwi-stage1/main.cpp:24-32: divide by
@@ -280,7 +283,7 @@ int sfwi_set_tile_shape(sfwi_handle *h, int shape);
 int sfwi_set_launch_overlap(sfwi_handle *h, int on);
 int sfwi_get_tile_shape(sfwi_handle *h, int *shape, int *tx, int *tz);
 
-/* Autotuner: after a gradient run (sfwi_run / sfwi_run_noalloc), time one
+/* Autotuner: after a gradient run (sfwi_run or sfwi_image_singleshot), time one
  * step of the four step kernels for every tile shape on the resident batch
  * (reps steps each, as sfwi_time_kernels) and keep the fastest.  *choice gets
  * its SFWI_TILE_* index, out_ms (optional, SFWI_NUM_TILE_SHAPES floats) the

@@ -19,6 +19,7 @@
 // One CTA handles one (trace, component); prefix and suffix sums are block
 // scans built on warp shuffles.
 #include <cfloat>
+#include <cudaTypedefs.h>
 #include <mutex>
 
 #include "sfwi_launch.h"
@@ -270,10 +271,10 @@ cudaError_t launch_ot(const OtArgs &a, cudaStream_t st) {
 //
 // Its working memory -- the per-trace scale of the positivity transform, the
 // per-trace misfits and their sum -- lives in the fixed array below instead
-// of buffers from cudaMalloc, for callers that may not allocate: code that
-// runs while a stream is being captured into a CUDA graph (cudaMalloc is not
-// allowed there), allocators that own every device byte of a process, and
-// latency-bound loops where an allocation may synchronise the device.
+// of buffers from cudaMalloc.  It serves callers that cannot allocate device
+// memory: a host program whose own allocator has reserved every device byte
+// up front, and inner loops where a cudaMalloc/cudaFree may synchronise the
+// device and stall other work in flight.
 // Every device that loads this library holds the array (256 KB) until the
 // process exits.  All calls on a device share it, so calls that overlap on the
 // GPU (different streams or threads at the same time) race on it.
@@ -342,10 +343,39 @@ __global__ void k_ot_sum(const double *trace_misfit, int ntr, double *out) {
 }  // namespace sfwi
 
 namespace {
-// device address of g_ot_noalloc_scratch per device, looked up on the first
-// call on that device with the device current
+// Device address of g_ot_noalloc_scratch, looked up once per CUDA context with
+// the device current: host code cannot take the address of a __device__
+// array (its name there is a host-side stand-in), and a new context on the
+// same device (after cudaDeviceReset) loads the module, and the array, anew.
+// The context is identified by cuCtxGetId, which never repeats in a process;
+// where the driver does not offer it, the address is kept per device.
+struct ScratchAddr {
+    unsigned long long ctx;
+    double *addr;
+};
 std::mutex g_noalloc_mu;
-double *g_noalloc_addr[128] = {};
+ScratchAddr g_noalloc_addr[128] = {};
+
+unsigned long long current_context_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_cur = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+        looked = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_cur && get_id && get_cur(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS) return id + 1;
+    return 0;  // unknown: one address per device
+}
 }  // namespace
 
 extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z, const float *cal_x,
@@ -353,7 +383,10 @@ extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z,
                                double *misfit, void *stream) {
     using namespace sfwi;
     if (kind < 1 || kind > 3) return record_error(-1, "sfwi_ot_noalloc: kind must be 1, 2 or 3");
-    if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z || !misfit || length < 1 || tracenum < 1)
+    if (!misfit || length < 1 || tracenum < 0) return record_error(-1, "sfwi_ot_noalloc: bad argument");
+    // an empty gather (a shot without receivers) adds nothing, as sfwi_ot
+    if (tracenum == 0) return 0;
+    if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z)
         return record_error(-1, "sfwi_ot_noalloc: bad argument");
     if (tracenum > OT_NOALLOC_MAX_TRACES)
         return record_error(-1, "sfwi_ot_noalloc: %d traces exceed the fixed scratch of %d traces", tracenum,
@@ -367,13 +400,23 @@ extern "C" int sfwi_ot_noalloc(int kind, const float *obs_x, const float *obs_z,
     double *scratch = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        unsigned long long ctx = current_context_id();
+        if (ctx == 0) {
+            // no context current yet: make the device's primary context
+            // current (it allocates nothing) so that its id can be read
+            if ((e = cudaSetDevice(dev)) != cudaSuccess)
+                return record_error(-2, "sfwi_ot_noalloc: %s", cudaGetErrorString(e));
+            ctx = current_context_id();
+        }
+        ScratchAddr &a = g_noalloc_addr[dev];
+        if (!a.addr || a.ctx != ctx) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_ot_noalloc_scratch);
             if (e != cudaSuccess) return record_error(-2, "sfwi_ot_noalloc: scratch address: %s", cudaGetErrorString(e));
-            g_noalloc_addr[dev] = static_cast<double *>(p);
+            a.addr = static_cast<double *>(p);
+            a.ctx = ctx;
         }
-        scratch = g_noalloc_addr[dev];
+        scratch = a.addr;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double *sigma = scratch, *tmis = scratch + 2 * OT_NOALLOC_MAX_TRACES, *sum = scratch + 4 * OT_NOALLOC_MAX_TRACES;

@@ -1,16 +1,19 @@
 """The allocation-free OT entry point (sfwi_ot_noalloc) against the
-allocating one (sfwi_ot and its siblings).
+allocating one (sfwi_ot and its siblings) and the FP64 oracle.
 
-sfwi_ot_noalloc serves callers that may not allocate device memory (stream
-capture, external allocators, latency-bound loops): it works on device
-buffers the caller owns and keeps its own working memory in a fixed array
-inside the library.  This file is collected last so that a failure here
-stops a run only after every other test has run.
+sfwi_ot_noalloc serves callers that cannot allocate device memory (a host
+program whose own allocator reserves every device byte, or a loop where a
+cudaMalloc would synchronise the device): it works on device buffers the
+caller owns and keeps its own working memory in a fixed array inside the
+library.  This file is collected last so that a failure here stops a run only
+after every other test has run.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
+
+from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4  # the parity tolerance of the GPU tests
@@ -26,11 +29,24 @@ def _case(seed, ntr, nt):
     return obs_x, obs_z, cal_x.astype(np.float32), cal_z
 
 
-def test_noalloc_matches_allocating_entry_point_twice():
+def _rel(a, b):
+    return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
+
+
+def _call(lib, kind, dev, rx, rz, nt, ntr, dt, stream=None):
+    m = C.c_double(0.0)
+    rc = lib.sfwi_ot_noalloc(kind, *[C.c_void_p(t.data_ptr()) for t in dev], C.c_void_p(rx.data_ptr()),
+                             C.c_void_p(rz.data_ptr()), nt, ntr, dt, C.byref(m), stream)
+    assert rc == 0, lib.sfwi_last_error()
+    return m.value
+
+
+def test_noalloc_matches_allocating_entry_point_and_oracle_twice():
     torch = pytest.importorskip("torch")
     import sfwi_gb300 as sg
     from sfwi_gb300 import _lib
     lib = _lib.load()
+    po.build()
     dt = 1e-3
     fns = {1: sg.OT, 2: sg.OT_power, 3: sg.OT_alltrace}
     for call, (seed, ntr, nt) in enumerate(((1, 37, 700), (2, 53, 512))):
@@ -38,18 +54,53 @@ def test_noalloc_matches_allocating_entry_point_twice():
         dev = [torch.from_numpy(a).cuda() for a in (obs_x, obs_z, cal_x, cal_z)]
         for kind, fn in fns.items():
             rx_ref, rz_ref, m_ref = fn(obs_x, obs_z, cal_x, cal_z, dt)
+            m64, rx64, rz64 = po.ot_gather(kind, dt, obs_x, obs_z, cal_x, cal_z)
             rx = torch.zeros((ntr, nt), dtype=torch.float32, device="cuda")
             rz = torch.zeros((ntr, nt), dtype=torch.float32, device="cuda")
-            m = C.c_double(0.0)
             torch.cuda.synchronize()
-            rc = lib.sfwi_ot_noalloc(kind, *[C.c_void_p(t.data_ptr()) for t in dev], C.c_void_p(rx.data_ptr()),
-                                     C.c_void_p(rz.data_ptr()), nt, ntr, dt, C.byref(m), None)
-            assert rc == 0, lib.sfwi_last_error()
+            m = _call(lib, kind, dev, rx, rz, nt, ntr, dt)
             rx, rz = rx.cpu().numpy(), rz.cpu().numpy()
-            for a, b in ((rx, rx_ref), (rz, rz_ref)):
-                err = np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b)
-                assert err < TOL, (call, kind, err)
-            assert m.value == pytest.approx(m_ref, rel=TOL), (call, kind)
+            for a, b, c in ((rx, rx_ref, rx64), (rz, rz_ref, rz64)):
+                assert _rel(a, b) < TOL, (call, kind, _rel(a, b))
+                assert _rel(a, c) < TOL, (call, kind, _rel(a, c))
+            assert m == pytest.approx(m_ref, rel=TOL), (call, kind)
+            assert m == pytest.approx(m64, rel=TOL), (call, kind)
+
+
+def test_noalloc_on_a_caller_stream():
+    """Inputs written on the caller's stream and no device-wide synchronize
+    before the call: the call must order its work on that stream."""
+    torch = pytest.importorskip("torch")
+    import sfwi_gb300 as sg
+    from sfwi_gb300 import _lib
+    lib = _lib.load()
+    dt = 1e-3
+    ntr, nt = 41, 900
+    obs_x, obs_z, cal_x, cal_z = _case(3, ntr, nt)
+    rx_ref, rz_ref, m_ref = sg.OT(obs_x, obs_z, cal_x, cal_z, dt)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        host = [torch.from_numpy(a).pin_memory() for a in (obs_x, obs_z, cal_x, cal_z)]
+        dev = [h.to("cuda", non_blocking=True) for h in host]
+        # a second pass over the inputs on the same stream, so that they are
+        # not complete when the call's kernels are enqueued unless ordered
+        dev = [d * 1.0 for d in dev]
+        rx = torch.full((ntr, nt), 7.0, dtype=torch.float32, device="cuda")
+        rz = torch.full((ntr, nt), 7.0, dtype=torch.float32, device="cuda")
+        m = _call(lib, 1, dev, rx, rz, nt, ntr, dt, C.c_void_p(s.cuda_stream))
+        out_x, out_z = rx.cpu().numpy(), rz.cpu().numpy()
+    assert _rel(out_x, rx_ref) < TOL
+    assert _rel(out_z, rz_ref) < TOL
+    assert m == pytest.approx(m_ref, rel=TOL)
+
+
+def test_noalloc_empty_gather_adds_nothing():
+    from sfwi_gb300 import _lib
+    lib = _lib.load()
+    m = C.c_double(1.5)
+    rc = lib.sfwi_ot_noalloc(1, None, None, None, None, None, None, 100, 0, 1e-3, C.byref(m), None)
+    assert rc == 0, lib.sfwi_last_error()
+    assert m.value == 1.5
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():

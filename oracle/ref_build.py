@@ -236,7 +236,8 @@ def born_symbols(stage):
     return {l.split()[2] for l in r.stdout.splitlines() if len(l.split()) == 3}
 
 
-DEFAULT_SRC = "/root/reference"
+# where the reference tree is mounted (override with SFWI_REFERENCE_SRC)
+DEFAULT_SRC = os.environ.get("SFWI_REFERENCE_SRC", "/root/reference")
 
 
 def sources_present(src=DEFAULT_SRC):

@@ -37,7 +37,6 @@
 
 namespace {
 
-constexpr int kCutLayer = 26;
 constexpr float kStep1 = 30.f, kStep2 = 150.f;
 
 void die(const char *what) {
@@ -81,23 +80,6 @@ std::vector<float> ricker(int nt, float dt, float fm) {
     for (int t = 0; t < nt; t++)
         w[t] = (float)((1.0 - 2.0 * Nk * (t - t0) * (t - t0)) * std::exp(-Nk * (t - t0) * (t - t0)));
     return w;
-}
-
-// normalize_all, main.cpp:35-49: both arrays divided by their joint max |.|
-void normalize_all(std::vector<float> &a, std::vector<float> &b) {
-    float m = 0;
-    for (float v : a) m = std::fabs(v) > m ? std::fabs(v) : m;
-    for (float v : b) m = std::fabs(v) > m ? std::fabs(v) : m;
-    if (m == 0) return;
-    for (float &v : a) v = v / m;
-    for (float &v : b) v = v / m;
-}
-
-// cal_step2, main.cpp:64-73: vertex of the parabola through the three misfits
-double cal_step2(double m0, double m1, double m2, float s1, float s2) {
-    const double fenzi = (s1 * s1 - s2 * s2) * m0 + (s2 * s2) * m1 + (-s1 * s1) * m2;
-    const double fenmu = (s1 - s2) * m0 + (s2)*m1 + (-s1) * m2;
-    return fenzi / fenmu / 2.0f;
 }
 
 struct Shot {
@@ -204,7 +186,7 @@ int main(int argc, char **argv) {
 
     std::vector<float> grad_pp(n), grad_ps(n), illum(n), cg_pp(n), cg_ps(n), cg_pp_old(n, 0.f), cg_ps_old(n, 0.f);
     std::vector<float> image_pp(n, 0.f), image_ps(n, 0.f);  // stage 2: model perturbation
-    double beta_fenmu = 0.0, max_misfit = 0.0;
+    double beta_fenmu = 0.0, max_misfit = 0.0;  // CG state across iterations
     const std::string out = par.outdir;
     auto enqueue_all = [&]() {
         for (auto &s : shots) check(sfwi_enqueue_shot(h, &s.d), "enqueue");
@@ -238,50 +220,22 @@ int main(int argc, char **argv) {
             write_model(out, "sum_illum", iter, allnx, allnz, illum.data());
             break;
         }
-        // preconditioning and the conjugate-gradient direction
-        double beta_fenzi = 0.0;
-        for (int i = 0; i < allnx; i++)
-            for (int j = 0; j < allnz; j++) {
-                const size_t k = (size_t)i * allnz + j;
-                if (stage == 1) {
-                    float gp = grad_pp[k] / illum[k], gs = grad_ps[k] / illum[k];
-                    if (j < kCutLayer) gp = gs = 0.f;
-                    cg_pp[k] = gp;
-                    cg_ps[k] = gs;
-                    beta_fenzi += grad_pp[k] * gp + grad_ps[k] * gs;
-                } else {
-                    if (j >= kCutLayer) {
-                        cg_pp[k] = grad_pp[k] / illum[k];
-                        cg_ps[k] = grad_ps[k] / illum[k];
-                    } else {
-                        grad_pp[k] = grad_ps[k] = 0.f;
-                        cg_pp[k] = cg_ps[k] = 0.f;
-                    }
-                    beta_fenzi += grad_pp[k] * grad_pp[k] / illum[k] + grad_ps[k] * grad_ps[k] / illum[k];
-                }
-            }
-        const double beta = iter == 0 ? 0.0 : beta_fenzi / beta_fenmu;
-        for (size_t k = 0; k < n; k++) {
-            cg_pp[k] = cg_pp[k] + beta * cg_pp_old[k];
-            cg_ps[k] = cg_ps[k] + beta * cg_ps_old[k];
-        }
-        cg_pp_old = cg_pp;
-        cg_ps_old = cg_ps;
-        beta_fenmu = beta_fenzi;
-        write_model(out, "sum_grad_pp", iter, allnx, allnz, grad_pp.data());
-        write_model(out, "sum_grad_ps", iter, allnx, allnz, grad_ps.data());
+        // preconditioning, the conjugate-gradient direction and the update
+        // (the reference's arithmetic, in libsfwi_host: sfwi_host.h)
         if (stage == 1) {
+            write_model(out, "sum_grad_pp", iter, allnx, allnz, grad_pp.data());
+            write_model(out, "sum_grad_ps", iter, allnx, allnz, grad_ps.data());
+            write_model(out, "sum_illum", iter, allnx, allnz, illum.data());
+            std::vector<float> d_pp(n), d_ps(n);
+            sfwi_stage1_direction(allnx, allnz, iter, grad_pp.data(), grad_ps.data(), illum.data(), cg_pp_old.data(),
+                                  cg_ps_old.data(), &beta_fenmu, cg_pp.data(), cg_ps.data(), d_pp.data(), d_ps.data());
             write_model(out, "sum_cg_pp", iter, allnx, allnz, cg_pp.data());
             // line search along the normalised direction, all shots and the
             // three trial models in one batch
-            std::vector<float> d_pp = cg_pp, d_ps = cg_ps;
-            normalize_all(d_pp, d_ps);
             double m3[3] = {0.0, 0.0, 0.0};
             enqueue_all();
             check(sfwi_line_search_parabola(h, d_pp.data(), d_ps.data(), kStep1, kStep2, m3, nullptr), "line search");
-            double alpha = cal_step2(m3[0], m3[1], m3[2], kStep1, kStep2);
-            if (alpha > 300) alpha = 300;
-            if (alpha < -100) alpha = -100;
+            const double alpha = sfwi_stage1_alpha(m3[0], m3[1], m3[2], kStep1, kStep2);
             {
                 FILE *f = std::fopen((out + "/misfit.txt").c_str(), "a");
                 if (f) {
@@ -289,19 +243,17 @@ int main(int argc, char **argv) {
                     std::fclose(f);
                 }
             }
-            std::printf("iter %d line search misfits %.6e %.6e %.6e alpha %.4g\n", iter, m3[0], m3[1], m3[2], alpha);
-            for (size_t k = 0; k < n; k++) {
-                vp[k] = vp[k] - alpha * d_pp[k];
-                vs[k] = vs[k] - alpha * d_ps[k];
-            }
-            for (int i = 0; i < allnx; i++)
-                for (int j = 0; j < kCutLayer && j < allnz; j++) {
-                    vp[(size_t)i * allnz + j] = vp[0];
-                    vs[(size_t)i * allnz + j] = vs[0];
-                }
+            std::printf("iter %d line search misfits %.17g %.17g %.17g alpha %.17g\n", iter, m3[0], m3[1], m3[2],
+                        alpha);
+            sfwi_stage1_update(allnx, allnz, alpha, d_pp.data(), d_ps.data(), vp.data(), vs.data());
             write_model(out, "vel_p", iter, allnx, allnz, vp.data());
             write_model(out, "vel_s", iter, allnx, allnz, vs.data());
         } else {
+            sfwi_stage2_direction(allnx, allnz, iter, grad_pp.data(), grad_ps.data(), illum.data(), cg_pp_old.data(),
+                                  cg_ps_old.data(), &beta_fenmu, cg_pp.data(), cg_ps.data());
+            // the gradients as the reference writes them, zeroed above the cut
+            write_model(out, "sum_grad_pp", iter, allnx, allnz, grad_pp.data());
+            write_model(out, "sum_grad_ps", iter, allnx, allnz, grad_ps.data());
             write_model(out, "sum_cggrad_pp", iter, allnx, allnz, cg_pp.data());
             write_model(out, "sum_cggrad_ps", iter, allnx, allnz, cg_ps.data());
             write_model(out, "sum_illum", iter, allnx, allnz, illum.data());
@@ -310,12 +262,9 @@ int main(int argc, char **argv) {
             check(sfwi_line_search_exact(h, image_pp.data(), image_ps.data(), cg_pp.data(), cg_ps.data(), &fenzi, &fenmu,
                                          nullptr),
                   "step length");
-            const double alpha = fenzi / fenmu;
-            std::printf("iter %d fenzi %.6e fenmu %.6e alpha %.4g\n", iter, fenzi, fenmu, alpha);
-            for (size_t k = 0; k < n; k++) {
-                image_pp[k] = image_pp[k] - alpha * cg_pp[k];
-                image_ps[k] = image_ps[k] - alpha * cg_ps[k];
-            }
+            const double alpha = sfwi_stage2_update(allnx, allnz, fenzi, fenmu, cg_pp.data(), cg_ps.data(),
+                                                    image_pp.data(), image_ps.data());
+            std::printf("iter %d fenzi %.17g fenmu %.17g alpha %.17g\n", iter, fenzi, fenmu, alpha);
             write_model(out, "sum_image_pp", iter, allnx, allnz, image_pp.data());
             write_model(out, "sum_image_ps", iter, allnx, allnz, image_ps.data());
         }

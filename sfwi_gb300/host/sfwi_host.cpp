@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -129,6 +130,133 @@ int sfwi_para_read(const char *path, sfwi_para *p) {
     if (std::fscanf(fp.f, "%d %d", &p->sy, &p->gy) != 2) return -1;
     if (std::fscanf(fp.f, "%d %d %d %d", &p->light, &p->rbc, &p->cpu_mem, &p->iointerval) != 4) return -1;
     return 0;
+}
+
+// ---- model-update arithmetic (sfwi_host.h) ----
+// Every float expression below keeps the reference's operand types: float
+// products and quotients, promoted to double where the reference adds them to
+// a double or multiplies them by one.  The library builds with
+// -ffp-contract=off, so no product is fused into a sum on any machine.
+
+// normalize_all, sfwi-stage1/main.cpp:35-49: both arrays divided by the
+// largest |value| of the two (a float), as the reference does even when it is 0
+static void normalize_pair(float *a, float *b, size_t n) {
+    float m = 0.f;
+    for (size_t i = 0; i < n; i++) m = std::fabs(a[i]) > m ? std::fabs(a[i]) : m;
+    for (size_t i = 0; i < n; i++) m = std::fabs(b[i]) > m ? std::fabs(b[i]) : m;
+    for (size_t i = 0; i < n; i++) {
+        a[i] = a[i] / m;
+        b[i] = b[i] / m;
+    }
+}
+
+// cg = cg + beta cg_old (a double product, stored as float), then cg_old = cg
+static void cg_recurrence(size_t n, double beta, float *cp, float *cs, float *cg_old_pp, float *cg_old_ps) {
+    for (size_t k = 0; k < n; k++) {
+        cp[k] = cp[k] + beta * cg_old_pp[k];
+        cs[k] = cs[k] + beta * cg_old_ps[k];
+    }
+    std::memcpy(cg_old_pp, cp, n * sizeof(float));
+    std::memcpy(cg_old_ps, cs, n * sizeof(float));
+}
+
+double sfwi_stage1_direction(int allnx, int allnz, int iter, const float *grad_pp, const float *grad_ps,
+                             const float *illum, float *cg_old_pp, float *cg_old_ps, double *beta_fenmu, float *cg_pp,
+                             float *cg_ps, float *d_pp, float *d_ps) {
+    const size_t n = (size_t)allnx * allnz;
+    std::vector<float> cp(n), cs(n);
+    double beta_fenzi = 0.0;
+    // sum_grad = grad / illumination (main.cpp:689-700), cut above layer 26
+    // (:702-714), cg = sum_grad and beta_fenzi += grad . sum_grad (:717-724)
+    for (int i = 0; i < allnx; i++)
+        for (int j = 0; j < allnz; j++) {
+            const size_t k = (size_t)i * allnz + j;
+            float gp = grad_pp[k] / illum[k], gs = grad_ps[k] / illum[k];
+            if (j < SFWI_CUT_LAYER) gp = gs = 0.f;
+            cp[k] = gp;
+            cs[k] = gs;
+            beta_fenzi += grad_pp[k] * gp + grad_ps[k] * gs;
+        }
+    // beta (:729-735), the recurrence (:739-748), beta_fenmu (:750)
+    const double beta = iter == 0 ? 0.0 : beta_fenzi / *beta_fenmu;
+    cg_recurrence(n, beta, cp.data(), cs.data(), cg_old_pp, cg_old_ps);
+    *beta_fenmu = beta_fenzi;
+    if (cg_pp) std::memcpy(cg_pp, cp.data(), n * sizeof(float));
+    if (cg_ps) std::memcpy(cg_ps, cs.data(), n * sizeof(float));
+    // the line-search direction: cg normalised (:832-841; again at :1060-1063,
+    // which leaves it unchanged: its largest |value| is then exactly 1)
+    if (d_pp && d_ps) {
+        normalize_pair(cp.data(), cs.data(), n);
+        std::memcpy(d_pp, cp.data(), n * sizeof(float));
+        std::memcpy(d_ps, cs.data(), n * sizeof(float));
+    }
+    return beta;
+}
+
+double sfwi_stage1_alpha(double misfit0, double misfit1, double misfit2, float step1, float step2) {
+    // cal_step2, main.cpp:64-73 (float products of the steps, double sums)
+    const double fenzi = (step1 * step1 - step2 * step2) * misfit0 + (step2 * step2) * misfit1 +
+                         (-step1 * step1) * misfit2;
+    const double fenmu = (step1 - step2) * misfit0 + (step2)*misfit1 + (-step1) * misfit2;
+    double alpha = fenzi / fenmu / 2.0f;
+    // main.cpp:1228-1237
+    if (alpha > 300) alpha = 300;
+    if (alpha < -100) alpha = -100;
+    return alpha;
+}
+
+void sfwi_stage1_update(int allnx, int allnz, double alpha, const float *d_pp, const float *d_ps, float *vp,
+                        float *vs) {
+    const size_t n = (size_t)allnx * allnz;
+    // main.cpp:1247-1253
+    for (size_t k = 0; k < n; k++) {
+        vp[k] = vp[k] - alpha * d_pp[k];
+        vs[k] = vs[k] - alpha * d_ps[k];
+    }
+    // main.cpp:1257-1264: the layers above the cut take the corner value
+    for (int i = 0; i < allnx; i++)
+        for (int j = 0; j < allnz && j < SFWI_CUT_LAYER; j++) {
+            vp[(size_t)i * allnz + j] = vp[0];
+            vs[(size_t)i * allnz + j] = vs[0];
+        }
+}
+
+double sfwi_stage2_direction(int allnx, int allnz, int iter, float *grad_pp, float *grad_ps, const float *illum,
+                             float *cg_old_pp, float *cg_old_ps, double *beta_fenmu, float *cg_pp, float *cg_ps) {
+    const size_t n = (size_t)allnx * allnz;
+    double beta_fenzi = 0.0;
+    // sfwi-stage2/main.cpp:646-671
+    for (int i = 0; i < allnx; i++)
+        for (int j = 0; j < allnz; j++) {
+            const size_t k = (size_t)i * allnz + j;
+            if (j >= SFWI_CUT_LAYER) {
+                cg_pp[k] = grad_pp[k] / illum[k];
+                cg_ps[k] = grad_ps[k] / illum[k];
+            } else {
+                grad_pp[k] = 0.f;
+                grad_ps[k] = 0.f;
+                cg_pp[k] = grad_pp[k];
+                cg_ps[k] = grad_ps[k];
+            }
+            beta_fenzi += grad_pp[k] * grad_pp[k] / illum[k] + grad_ps[k] * grad_ps[k] / illum[k];
+        }
+    // :674-703
+    const double beta = iter == 0 ? 0.0 : beta_fenzi / *beta_fenmu;
+    cg_recurrence(n, beta, cg_pp, cg_ps, cg_old_pp, cg_old_ps);
+    *beta_fenmu = beta_fenzi;
+    return beta;
+}
+
+double sfwi_stage2_update(int allnx, int allnz, double fenzi, double fenmu, const float *cg_pp, const float *cg_ps,
+                          float *image_pp, float *image_ps) {
+    // sfwi-stage2/main.cpp:865-875
+    const double alpha = fenzi / fenmu;
+    const size_t n = (size_t)allnx * allnz;
+    for (size_t k = 0; k < n; k++) {
+        image_pp[k] = (image_pp[k] - alpha * cg_pp[k]);
+        image_ps[k] = (image_ps[k] - alpha * cg_ps[k]);
+    }
+    return alpha;
 }
 
 }  // extern "C"

@@ -1,5 +1,5 @@
 /* sfwi_host.h — host-side pieces of the SFWI drivers: SU record I/O, shot
- * indexing and the para_stage parameter files.  Plain C++ (no CUDA), built
+ * indexing, the para_stage parameter files and the model-update arithmetic.  Plain C++ (no CUDA), built
  * into sfwi_gb300/lib/libsfwi_host.so and linked by the sfwi_fwi driver.
  *
  * SU traces are a 240-byte header followed by ns float32 samples, in the
@@ -61,6 +61,45 @@ typedef struct {
 
 /* Returns 0, or -1 when the file is missing or a field cannot be read. */
 int sfwi_para_read(const char *path, sfwi_para *out);
+
+/* ---- model-update arithmetic of the inversion drivers ----
+ * The steps rank 1 of the reference performs between the gradient reduction
+ * and the model broadcast, on [allnx][allnz] float arrays, with the
+ * reference's operand types (float products and quotients, double
+ * accumulators and CG/line-search scalars).  cut_layer = 26 and the alpha
+ * clamp [-100, 300] are the reference's constants.  State carried from one
+ * iteration to the next (the previous CG direction and beta's denominator)
+ * lives in the caller's cg_old arrays and *beta_fenmu. */
+#define SFWI_CUT_LAYER 26
+
+/* Stage 1 (sfwi-stage1/main.cpp:687-750, :832-841): g = grad / illumination,
+ * zero for z < 26; beta_fenzi = sum(grad . g) (float terms, double sum);
+ * beta = beta_fenzi / *beta_fenmu (0 at iter 0); cg = g + beta cg_old;
+ * cg_old = cg; *beta_fenmu = beta_fenzi; d = cg divided by the largest |cg|
+ * of both components (normalize_all, main.cpp:35-49).  cg and d may be
+ * NULL when not wanted.  Returns beta. */
+double sfwi_stage1_direction(int allnx, int allnz, int iter, const float *grad_pp, const float *grad_ps,
+                             const float *illum, float *cg_old_pp, float *cg_old_ps, double *beta_fenmu, float *cg_pp,
+                             float *cg_ps, float *d_pp, float *d_ps);
+/* Stage 1 step length (cal_step2, main.cpp:64-73, and the clamp, :1228-1237):
+ * the vertex of the parabola through the misfits at steps 0, step1, step2,
+ * clamped to [-100, 300]. */
+double sfwi_stage1_alpha(double misfit0, double misfit1, double misfit2, float step1, float step2);
+/* Stage 1 model update (main.cpp:1247-1264): vp -= alpha d_pp, vs -= alpha
+ * d_ps (double products, stored as float); then every cell with z < 26 takes
+ * the updated vp[0][0], vs[0][0]. */
+void sfwi_stage1_update(int allnx, int allnz, double alpha, const float *d_pp, const float *d_ps, float *vp, float *vs);
+
+/* Stage 2 (sfwi-stage2/main.cpp:646-703): for z >= 26 cg = grad / illum, for
+ * z < 26 grad = cg = 0 (grad is written); beta_fenzi = sum(grad^2/illum) over
+ * both components; beta, cg += beta cg_old, cg_old = cg, *beta_fenmu as in
+ * stage 1.  Returns beta. */
+double sfwi_stage2_direction(int allnx, int allnz, int iter, float *grad_pp, float *grad_ps, const float *illum,
+                             float *cg_old_pp, float *cg_old_ps, double *beta_fenmu, float *cg_pp, float *cg_ps);
+/* Stage 2 update (main.cpp:865-875): alpha = fenzi / fenmu; image -= alpha cg.
+ * Returns alpha. */
+double sfwi_stage2_update(int allnx, int allnz, double fenzi, double fenmu, const float *cg_pp, const float *cg_ps,
+                          float *image_pp, float *image_ps);
 
 #ifdef __cplusplus
 }

@@ -266,8 +266,10 @@ def run_serving(n, budget_gb=64.0, slots=4, full=False):
     """Serving loop on a seeded Poisson stream (50 requests/s; grids, nt and
     shots drawn from the serving configuration's ranges, then, unless `full`,
     scaled by 0.3 in each grid dimension and 0.1 in nt so the stream is served
-    in seconds): continuous admission against an HBM budget vs the plain FIFO
-    loop, each replayed twice and measured on the second replay.  At the
+    in seconds): continuous admission against an HBM budget -- the requests
+    admitted together sharing one run of the engine (two runs in flight), or
+    one engine per request -- vs the plain FIFO loop, each replayed twice and
+    measured on the second replay.  At the
     drawn sizes a request takes about a second of GPU time, so a stream at
     50/s queues: the latencies then measure the backlog."""
     from sfwi_gb300 import serve
@@ -276,7 +278,8 @@ def run_serving(n, budget_gb=64.0, slots=4, full=False):
     serve.run_request(reqs[0])  # warm the kernels and the allocator
     out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
            "scale": "the drawn sizes" if full else "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
-    for name, srv in (("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
+    for name, srv in (("served_batched", serve.Server(budget_gb * 2 ** 30, max_active=2, batch=True)),
+                      ("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
                       ("served_shortest_first", serve.Server(budget_gb * 2 ** 30, max_active=slots, policy="shortest")),
                       ("fifo", serve.Server(budget_gb * 2 ** 30, max_active=1))):
         srv.run(reqs)  # the first replay settles the allocator pools and host threads
@@ -316,11 +319,244 @@ def run_reference_arm(args, w):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(els)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "cpu": True, "sample": sample},
-            "cpu_baseline": {"value": value, "unit": "shot-gradients/s", "cores": threads, "kind": kind,
+            "cpu_baseline": {"value": value, "unit": "shot-gradients/s", "cores": threads, "cpu_model": cpu_model(),
+                             "kind": kind,
                              "sample": sample},
             "e2e": {"value": value, "unit": "shot-gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_model():
+    """the host CPU's model name (lscpu), for the baseline lines"""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
+def observed_records(sg, w, data):
+    """background records of the true model (untimed), in page-locked host
+    buffers: the observed data of every shot"""
+    pml, nt = w["pml"], w["nt"]
+    shots = data["shots"]
+    isz, igz = pml + w["sy"], pml + w["gy"]
+    fwd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], w["allnx"] + 2 * pml, w["allnz"] + 2 * pml,
+                             w["allnx"], w["allnz"], 1, pml, nt, 4, shots[0]["ntr"], stage=1)
+    fwd.GPUbufferVPVS(data["vp"], data["vs"], data["rho"])
+    if w.get("source") == "vz":
+        fwd.set_source(sg.SOURCE_VZ_FORCE)
+    for d in shots:
+        fwd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"])
+    fwd.run_forward()
+    obs = []
+    for i, d in enumerate(shots):
+        r = fwd.read_records(i, d["ntr"])
+        pz, px = sg.PinnedArray((d["ntr"], nt)), sg.PinnedArray((d["ntr"], nt))
+        pz.array[...] = r["syn_z"]
+        px.array[...] = r["syn_x"]
+        obs.append((pz, px))
+    fwd.close()
+    return obs
+
+
+def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, clocks=None, snap_check=0):
+    """One workload: `warmup` untimed passes (the autotuner after the first),
+    then `steps` timed passes through sfwi_run (device time from CUDA events
+    inside the engine; wall clock around the whole public call for e2e), the
+    per-kernel launch times, and the plain one-shot-at-a-time form on an
+    evenly spread sample of `plain_shots` shots.  Returns a dict."""
+    import sfwi_gb300 as sg
+    data = build_workload(w)
+    stage = w.get("stage", 2)
+    nt, pml = w["nt"], w["pml"]
+    nxpml, nzpml = w["allnx"] + 2 * pml, w["allnz"] + 2 * pml
+    shots = data["shots"]
+    isz, igz = pml + w["sy"], pml + w["gy"]
+    obs = observed_records(sg, w, data)
+    kbytes = dict(KERNEL_BYTES)
+    fd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml, nt,
+                            4, shots[0]["ntr"], stage=stage)
+    if stage == 2:
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"])
+        fd.GPUbufferM(data["dvp"], data["dvs"])
+    else:
+        fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])
+    if w.get("source") == "vz":
+        fd.set_source(sg.SOURCE_VZ_FORCE)
+    if w["misfit"] == "OT":
+        fd.set_misfit(sg.MISFIT_OT)
+    if w.get("snap"):
+        fd.set_snapshots(*w["snap"])
+    if w.get("rho_grad"):
+        fd.set_density_gradient(True)
+        kbytes["k_bwd_v"] += 8  # the density kernel's accumulator, read and written
+
+    def enqueue(d, i):
+        fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[i][0].array,
+                        obs[i][1].array)
+
+    def step():
+        for i, d in enumerate(shots):
+            enqueue(d, i)
+        m, _ = fd.run()
+        grho = fd.read_density_gradient_f64() if w.get("rho_grad") else None
+        g = fd.imagebuffer_resettozero()
+        return m, (g, grho)
+
+    tune = None
+    if args.tile != "auto":
+        fd.set_tile_shape(args.tile)
+    t0 = time.perf_counter()
+    m = None
+    for i in range(warmup):
+        m, g = step()
+        if i == 0 and args.tile == "auto":
+            # tile shape: time every shape on the resident batch, keep the
+            # fastest; the remaining warm-up steps capture its graphs
+            choice, tms = fd.autotune(reps=5)
+            tune = {"choice": choice, "ms_per_step": {k: round(v, 4) for k, v in tms.items()}}
+            log("%s autotune: %s" % (w["name"], tune))
+    if tune and warmup < 2:
+        m, g = step()  # the chosen shape's graphs are captured outside the timed steps
+    log("%s warm-up: %d steps in %.2f s, misfit %.6e" % (w["name"], warmup, time.perf_counter() - t0, m or 0.0))
+    out = {"fd": fd, "shots": shots, "obs": obs, "tune": tune, "data": data}
+    if args.profile_kernels:
+        return out
+
+    if pg:
+        pg.barrier()
+    if clocks:
+        clocks.start()
+    launches0 = fd.kernel_launches()
+    dev_ms, fwd_ms, bwd_ms, mis_ms = [], [], [], []
+    wall0 = time.perf_counter()
+    for _ in range(steps):
+        m, g = step()
+        t = fd.last_timing()
+        dev_ms.append(t["total_ms"])
+        fwd_ms.append(t["forward_ms"])
+        bwd_ms.append(t["backward_ms"])
+        mis_ms.append(t["misfit_ms"])
+    wall = time.perf_counter() - wall0
+    launches = fd.kernel_launches() - launches0
+    clk = clocks.stop() if clocks else None
+    total_dev_s = sum(dev_ms) / 1000.0
+    if pg:
+        import torch
+        tt = torch.tensor([total_dev_s, wall], dtype=torch.float64)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        total_dev_s, wall = float(tt[0]), float(tt[1])
+    nsh = len(shots) * ws
+    value = nsh * steps / total_dev_s
+    e2e = nsh * steps / wall
+    h2d = sum(2 * d["ntr"] * nt * 4 for d in shots)
+    d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots) + (8 * w["allnx"] * w["allnz"] if w.get("rho_grad") else 0)
+
+    # per-kernel average launch durations (CUDA events on the engine stream)
+    kt = fd.time_kernels(reps=20)
+    peak, peak_kind = measured_peak_hbm()
+    cells = sum((d["nx"] + 2 * pml) * nzpml for d in shots)
+    roof, fracs = None, None
+    if kt:
+        fracs = {k: round(kbytes[k] * cells / (v / 1000.0) / 1e9 / peak, 4) for k, v in kt.items()}
+        dom = max(kt, key=kt.get)
+        achieved = kbytes[dom] * cells / (kt[dom] / 1000.0) / 1e9
+        tpc = traffic_per_cell(dom)
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": round(tpc * cells) if tpc else None,
+                "traffic_note": "DRAM bytes per launch: ncu capture of a 16-shot launch scaled by cells",
+                "alg_bytes_per_launch": kbytes[dom] * cells, "peak_source": peak_kind,
+                "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()},
+                "all_kernels_frac": fracs}
+    pass_bytes = w.get("pass_bytes", PASS_BYTES_PER_CELL_STEP)
+    kernel_bytes = sum(kbytes[k] for k in kt) if kt else None
+    alg_bytes_step = pass_bytes * cells * nt
+
+    # plain form: the same engine, one shot per run (the reference's per-shot
+    # call pattern), device-timed on an evenly spread sample of the shots,
+    # with the tile shape the autotuner picks for a one-shot batch
+    plain = None
+    if plain_shots > 0 and len(shots) > 1:
+        pick = shots[:: max(1, len(shots) // plain_shots)][:plain_shots]
+        plain_ms = []
+        batch_tile = fd.tile_shape()
+        plain_tile = None
+        for j, d in enumerate(pick[:1] + pick):  # the first run warms the one-shot graph shape
+            i = shots.index(d)
+            enqueue(d, i)
+            fd.run()
+            if j == 0:
+                plain_tile = fd.autotune(reps=5)[0] if args.tile == "auto" else batch_tile
+                enqueue(d, i)
+                fd.run()  # captures the graphs of the chosen shape
+            else:
+                plain_ms.append(fd.last_timing()["total_ms"])
+        fd.imagebuffer_resettozero()
+        fd.set_tile_shape(batch_tile)
+        pv = len(pick) / (sum(plain_ms) / 1000.0)
+        plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick), "tile": plain_tile,
+                 "ms_per_shot": round(float(np.mean(plain_ms)), 2), "batched_over_plain": round(value / pv, 2)}
+    # compressed snapshots against FP32 snapshots at full size, on a few shots
+    snap_err = None
+    if w.get("snap") and snap_check > 0:
+        pick = shots[:: max(1, len(shots) // snap_check)][:snap_check]
+        grads = {}
+        for fmt in ("f32", "f16", "bf16"):
+            fd.set_snapshots(w["snap"][0], fmt)
+            for d in pick:
+                enqueue(d, shots.index(d))
+            fd.run()
+            grads[fmt] = fd.read_gradients_f64()
+            fd.imagebuffer_resettozero()
+        fd.set_snapshots(*w["snap"])
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+        snap_err = {"shots": len(pick), "reference": "FP32 snapshots, same interval (the FP64-oracle errors are "
+                                                      "measured by the parity tests)"}
+        for fmt in ("f16", "bf16"):
+            snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
+                             for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
+    out.update(value=value, e2e=e2e, wall=wall, total_dev_s=total_dev_s, steps=steps, launches=launches, clk=clk,
+               h2d=h2d, d2h=d2h, kt=kt, roof=roof, fracs=fracs, cells=cells, alg_bytes_step=alg_bytes_step,
+               kernel_bytes=kernel_bytes, plain=plain, snap_err=snap_err, tile=fd.tile_shape(),
+               phase_ms={"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2),
+                         "misfit": round(float(np.mean(mis_ms)), 2)})
+    return out
+
+
+def close_workload(r):
+    r["fd"].close()
+    for pz, px in r["obs"]:
+        pz.free()
+        px.free()
+
+
+def sub_record(w, r):
+    """the short form of a workload's measurement, nested in the main line"""
+    ms = 1000.0 * r["total_dev_s"] / r["steps"]
+    rec = {"workload": w["name"], "shots": len(r["shots"]), "nt": w["nt"],
+           "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], w["pml"]), "dx_m": w["dx"], "stage": w.get("stage", 2),
+           "misfit": w["misfit"], "value": round(r["value"], 3), "unit": "shot-gradients/s", "steps": r["steps"],
+           "ms_per_step": round(ms, 3), "e2e": round(r["e2e"], 3), "tile": r["tile"],
+           "alg_GBps_whole_step": round(r["alg_bytes_step"] / (ms / 1000.0) / 1e9, 1),
+           "roofline": r["roof"] and {k: r["roof"][k] for k in ("kernel", "achieved", "peak", "frac", "launch_ms",
+                                                                 "all_kernels_ms", "all_kernels_frac")},
+           "plain": r["plain"]}
+    return rec
 
 
 def main():
@@ -344,6 +580,9 @@ def main():
     ap.add_argument("--profile-reference-gpu", action="store_true",
                     help="only run the reference's CUDA path on one shot of the workload (for ncu captures)")
     ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or a name in sfwi_gb300.TILE_SHAPES")
+    ap.add_argument("--extra-workloads", default="salt401,shot376",
+                    help="workloads measured after the main one and reported as sub-records (comma list; '' for none)")
+    ap.add_argument("--extra-steps", type=int, default=3, help="timed steps of each extra workload")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.nt:
@@ -365,211 +604,60 @@ def main():
         dist.init_process_group(backend="gloo", init_method="env://")
         pg = dist
 
-    import sfwi_gb300 as sg
-    data = build_workload(w)
-    stage = w.get("stage", 2)
-    nt, pml = w["nt"], w["pml"]
-    nxpml, nzpml = w["allnx"] + 2 * pml, w["allnz"] + 2 * pml
-    shots = data["shots"]
-    isz, igz = pml + w["sy"], pml + w["gy"]
-
-    # observed data: background forward on the true model (untimed)
-    fwd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml,
-                             nt, 4, shots[0]["ntr"], stage=1)
-    fwd.GPUbufferVPVS(data["vp"], data["vs"], data["rho"])
-    if w.get("source") == "vz":
-        fwd.set_source(sg.SOURCE_VZ_FORCE)
-    for d in shots:
-        fwd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"])
-    fwd.run_forward()
-    obs = []
-    for i, d in enumerate(shots):
-        r = fwd.read_records(i, d["ntr"])
-        pz, px = sg.PinnedArray((d["ntr"], nt)), sg.PinnedArray((d["ntr"], nt))
-        pz.array[...] = r["syn_z"]
-        px.array[...] = r["syn_x"]
-        obs.append((pz, px))
-    fwd.close()
-
-    fd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml, nt,
-                            4, shots[0]["ntr"], stage=stage)
-    if stage == 2:
-        fd.GPUbufferVPVS(data["vp0"], data["vs0"])
-        fd.GPUbufferM(data["dvp"], data["dvs"])
-    else:
-        fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])
-    if w.get("source") == "vz":
-        fd.set_source(sg.SOURCE_VZ_FORCE)
-    if w["misfit"] == "OT":
-        fd.set_misfit(sg.MISFIT_OT)
-    if w.get("snap"):
-        fd.set_snapshots(*w["snap"])
-    if w.get("rho_grad"):
-        fd.set_density_gradient(True)
-        KERNEL_BYTES["k_bwd_v"] += 8  # the density kernel's accumulator, read and written
-
-    def step():
-        for d, (pz, px) in zip(shots, obs):
-            fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], pz.array,
-                            px.array)
-        m, _ = fd.run()
-        grho = fd.read_density_gradient_f64() if w.get("rho_grad") else None
-        g = fd.imagebuffer_resettozero()
-        return m, (g, grho)
-
-    tune = None
-    if args.tile != "auto":
-        fd.set_tile_shape(args.tile)
-    t0 = time.perf_counter()
-    for i in range(args.warmup):
-        m, g = step()
-        if i == 0 and args.tile == "auto":
-            # tile shape: time every shape on the resident batch, keep the
-            # fastest; the remaining warm-up steps capture its graphs
-            choice, tms = fd.autotune(reps=5)
-            tune = {"choice": choice, "ms_per_step": {k: round(v, 4) for k, v in tms.items()}}
-            log("autotune: %s" % tune)
-    if tune and args.warmup < 2:
-        m, g = step()  # the chosen shape's graphs are captured outside the timed steps
-    log("warm-up: %d steps in %.2f s, misfit %.6e" % (args.warmup, time.perf_counter() - t0, m))
+    r = measure(w, args, args.steps, args.warmup, args.plain_shots, pg=pg, ws=ws, clocks=Clocks(),
+                snap_check=args.snap_check)
     if args.profile_kernels:
+        close_workload(r)
         return 0
-
-    # device-timed steps (CUDA events inside the engine: set-up kernel .. final reduction)
-    if pg:
-        pg.barrier()
-    clocks = Clocks()
-    clocks.start()
-    launches0 = fd.kernel_launches()
-    dev_ms, fwd_ms, bwd_ms, mis_ms = [], [], [], []
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        m, g = step()
-        t = fd.last_timing()
-        dev_ms.append(t["total_ms"])
-        fwd_ms.append(t["forward_ms"])
-        bwd_ms.append(t["backward_ms"])
-        mis_ms.append(t["misfit_ms"])
-    wall = time.perf_counter() - wall0
-    launches = fd.kernel_launches() - launches0
-    clk = clocks.stop()
-    total_dev_s = sum(dev_ms) / 1000.0
-    if pg:
-        import torch
-        tt = torch.tensor([total_dev_s, wall], dtype=torch.float64)
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        total_dev_s, wall = float(tt[0]), float(tt[1])
-    nsh = len(shots) * ws
-    value = nsh * args.steps / total_dev_s
-    e2e = nsh * args.steps / wall
-    h2d = sum(2 * d["ntr"] * nt * 4 for d in shots)
-    d2h = 3 * w["allnx"] * w["allnz"] * 4 + 8 * len(shots) + (8 * w["allnx"] * w["allnz"] if w.get("rho_grad") else 0)
-
-    # per-kernel average launch durations (CUDA events on the engine stream)
-    kt = fd.time_kernels(reps=20)
-    fd_tile = fd.tile_shape()
-    peak, peak_kind = measured_peak_hbm()
-    cells = sum((d["nx"] + 2 * pml) * nzpml for d in shots)
-    roof = None
-    if kt:
-        shares = {k: v for k, v in kt.items()}
-        dom = max(shares, key=shares.get)
-        achieved = KERNEL_BYTES[dom] * cells / (kt[dom] / 1000.0) / 1e9
-        tpc = traffic_per_cell(dom)
-        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": round(tpc * cells) if tpc else None,
-                "traffic_note": "DRAM bytes per launch: ncu capture of a 16-shot launch scaled by cells",
-                "alg_bytes_per_launch": KERNEL_BYTES[dom] * cells, "peak_source": peak_kind,
-                "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()}}
-    alg_bytes_step = w.get("pass_bytes", PASS_BYTES_PER_CELL_STEP) * cells * nt
-
-    # plain form: the same engine, one shot per run (the reference's per-shot
-    # call pattern), device-timed on an evenly spread sample of the shots,
-    # with the tile shape the autotuner picks for a one-shot batch
-    plain = None
-    if args.plain_shots > 0:
-        pick = shots[:: max(1, len(shots) // args.plain_shots)][: args.plain_shots]
-        plain_ms = []
-        batch_tile = fd.tile_shape()
-        plain_tile = None
-        for j, d in enumerate(pick[:1] + pick):  # the first run warms the one-shot graph shape
-            i = shots.index(d)
-            fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[i][0].array,
-                            obs[i][1].array)
-            fd.run()
-            if j == 0:
-                plain_tile = fd.autotune(reps=5)[0] if args.tile == "auto" else batch_tile
-                fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"],
-                                obs[i][0].array, obs[i][1].array)
-                fd.run()  # captures the graphs of the chosen shape
-            else:
-                plain_ms.append(fd.last_timing()["total_ms"])
-        fd.imagebuffer_resettozero()
-        fd.set_tile_shape(batch_tile)
-        pv = len(pick) / (sum(plain_ms) / 1000.0)
-        plain = {"value": round(pv, 3), "unit": "shot-gradients/s", "shots_sampled": len(pick), "tile": plain_tile,
-                 "ms_per_shot": round(float(np.mean(plain_ms)), 2), "batched_over_plain": round(value / pv, 2)}
-    # compressed snapshots against FP32 snapshots at full size, on a few shots
-    snap_err = None
-    if w.get("snap") and args.snap_check > 0:
-        pick = shots[:: max(1, len(shots) // args.snap_check)][: args.snap_check]
-        grads = {}
-        for fmt in ("f32", "f16", "bf16"):
-            fd.set_snapshots(w["snap"][0], fmt)
-            for d in pick:
-                i = shots.index(d)
-                fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"],
-                                obs[i][0].array, obs[i][1].array)
-            fd.run()
-            grads[fmt] = fd.read_gradients_f64()
-            fd.imagebuffer_resettozero()
-        fd.set_snapshots(*w["snap"])
-
-        def rel(a, b):
-            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-
-        snap_err = {"shots": len(pick), "reference": "FP32 snapshots, same interval"}
-        for fmt in ("f16", "bf16"):
-            snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
-                             for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
+    data, shots = r["data"], r["shots"]
+    nt, pml = w["nt"], w["pml"]
     ref_gpu = None
     if rank == 0 and args.reference_gpu_shots > 0 and not w.get("snap"):
         ref_gpu = reference_gpu_sample(w, data, args.reference_gpu_shots)
         if "value" in ref_gpu:
-            ref_gpu["batched_over_reference_gpu"] = round(value / ref_gpu["value"], 1)
+            ref_gpu["batched_over_reference_gpu"] = round(r["value"] / ref_gpu["value"], 1)
+    close_workload(r)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, el = cpu_baseline_sample(w, data, 1, min(nt, 1000), "port")
-        cpu = {"value": v, "unit": "shot-gradients/s", "cores": 1, "kind": "port",
+        cpu = {"value": v, "unit": "shot-gradients/s", "cores": 1, "cpu_model": cpu_model(), "kind": "port",
                "sample": "one shot, %d of %d time steps (%.1f s), FP32 single-thread transliteration, scaled by nt"
                          % (min(nt, 1000), nt, el)}
-    fd.close()
-    for pz, px in obs:
-        pz.free()
-        px.free()
+    # the other benchmark workloads, short: batched, plain and per-kernel frac
+    extras = {}
+    if rank == 0 and not args.nt and not args.shots:
+        for name in [x for x in args.extra_workloads.split(",") if x and x != args.workload]:
+            we = dict(WORKLOADS[name])
+            re = measure(we, args, args.extra_steps, 2, args.plain_shots)
+            extras[name] = sub_record(we, re)
+            close_workload(re)
     serving = (run_serving(args.serving_requests, full=args.serving_full)
                if args.serving_requests > 0 and rank == 0 else None)
     if rank != 0:
         return 0
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "shot-gradients/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / args.steps, 3),
+    steps = args.steps
+    total_dev_s = r["total_dev_s"]
+    line = {"metric": METRIC, "value": round(r["value"], 3), "unit": "shot-gradients/s", "n_gpus": ws, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * total_dev_s / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["name"], "shots": len(shots), "grid": "%dx%d+pml%d" % (w["allnx"], w["allnz"], pml),
-                       "nt": nt, "misfit": w["misfit"], "born": stage == 2, "dx_m": w["dx"],
+                       "nt": nt, "misfit": w["misfit"], "born": w.get("stage", 2) == 2, "dx_m": w["dx"],
                        "source": "vertical force" if w.get("source") == "vz" else "txx+tzz",
                        "gradients": "vp, vs, rho" if w.get("rho_grad") else "vp, vs",
-                       "tile": fd_tile, "autotune": tune,
+                       "tile": r["tile"], "autotune": r["tune"],
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
                                    else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
-                       "l2": l2_note(cells, nt, len(shots), w),
-                       "alg_bytes_per_step_GB": round(alg_bytes_step / 1e9, 2),
-                       "alg_GBps_whole_step": round(alg_bytes_step / (total_dev_s / args.steps) / 1e9, 1)},
-            "e2e": {"value": round(e2e, 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "plain": plain, "serving": serving, "snapshot_error": snap_err,
-            "reference_gpu": ref_gpu,
-            "phase_ms": {"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2),
-                         "misfit": round(float(np.mean(mis_ms)), 2)}}
+                       "l2": l2_note(r["cells"], nt, len(shots), w),
+                       "alg_bytes_per_step_GB": round(r["alg_bytes_step"] / 1e9, 2),
+                       "alg_GBps_whole_step": round(r["alg_bytes_step"] / (total_dev_s / steps) / 1e9, 1),
+                       "alg_GBps_whole_step_kernel_accounting": (
+                           round(r["kernel_bytes"] * r["cells"] * nt / (total_dev_s / steps) / 1e9, 1)
+                           if r["kernel_bytes"] else None)},
+            "e2e": {"value": round(r["e2e"], 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"]},
+            "gpu_launches": r["launches"], "roofline": r["roof"], "cpu_baseline": cpu, "clocks": r["clk"],
+            "plain": r["plain"], "serving": serving, "snapshot_error": r["snap_err"], "reference_gpu": ref_gpu,
+            "workloads": extras or None, "phase_ms": r["phase_ms"]}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -144,6 +144,51 @@ int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit);
  * sfwi_read_records; clears the queue */
 int sfwi_run_forward(sfwi_handle *h);
 
+/* ---- the Born operator and its exact adjoint (stage 2) ----
+ * The Born modelling operator L maps a model perturbation (dVp, dVs) to the
+ * scattered records: sfwi_gpu_buffer_m(h, dvp, dvs) then sfwi_run_forward
+ * (scattered records in syn_z/syn_x of sfwi_read_records).
+ * sfwi_born_adjoint applies its exact transpose to the queued shots' records
+ * d (sfwi_enqueue_shot rec_z/rec_x, [ntr][nt]): img_vp, img_vs (host
+ * [allnx][allnz], FP64) += L^T d, with <L m, d> = <m, L^T d> to rounding,
+ * about the uploaded background model.  It is the transpose of the forward
+ * sweeps this library runs (split-field PML included), not of the
+ * continuous adjoint equations the gradient path uses
+ * (GPUcalculate_elastic_*_back, sfwi-stage1/born.cu:504-603), so
+ * L^T L m is the Gauss-Newton Hessian-vector product of the reference's
+ * ELSRTM_CALCULATE_Hessian_vector (sfwi-stage1/FD2DGPU.cu:5236-5774) for the
+ * discrete operator.  Device memory: 4 nt bytes per packed cell for the
+ * background velocities of every step, plus 88 bytes per packed cell.
+ * Clears the queue. */
+int sfwi_born_adjoint(sfwi_handle *h, double *img_vp, double *img_vs);
+
+/* ---- shots on several models in one run (request batching) ----
+ * No reference counterpart: the reference runs one model per MPI job.  Each
+ * model has its own grid (allnx x allnz, with allnz + 2*pml at most the
+ * handle's nzpml) and its own number of time steps (nt at most the handle's
+ * nt; the wavelet is the first nt samples of the handle's).  Spacing, dt,
+ * PML width and stage are the handle's.  A shot's window is cut from its
+ * model, so its nx, delta_left and receivers refer to that model. */
+typedef struct {
+    int allnx, allnz, nt;
+    const float *vp, *vs, *rho;  /* host [allnx][allnz]; rho needed in stage 1, ignored in stage 2 */
+    const float *dvp, *dvs;      /* stage-2 perturbation, or both NULL (zero) */
+} sfwi_model_desc;
+/* One gradient run of every queued shot (sfwi_enqueue_shot; records [ntr][the
+ * model's nt]), shot i on models[shot_model[i]]: all shots advance in the
+ * same kernel launches, a shot only for its model's nt steps.  Outputs, each
+ * may be NULL: per_shot_misfit[queue index]; the FP64 gradients and
+ * illumination of every model, concatenated in model order (model k at
+ * offset sum_{j<k} allnx_j allnz_j), computed afresh (the handle's own
+ * accumulated gradients are not touched); grad_rho when the density gradient
+ * is on.  A shot's results do not depend on the other shots of the run: they
+ * equal a run of that model's shots alone, bit for bit.  When the models'
+ * nt differ the misfit must be L2 and snapshots off.  sfwi_read_records(h,
+ * i, ...) afterwards takes the queue index and gives [ntr][handle nt] with
+ * zeros after the model's nt.  Clears the queue. */
+int sfwi_run_models(sfwi_handle *h, int nmodels, const sfwi_model_desc *models, const int *shot_model,
+                    double *per_shot_misfit, double *grad_pp, double *grad_ps, double *illum, double *grad_rho);
+
 /* ---- line searches ----
  * CALCULATE_ALPHA_parabola_mb (sfwi-stage1/FD2DGPU.cu:4819-5036, stage 1):
  * the L2 misfit of the current shot at the trial models vp - s grad_pp,

@@ -167,11 +167,15 @@ class FD2DGPU_ELASTIC:
         return out
 
     # -- batched shots --
-    def enqueue_shot(self, nx, isx, isz, igz, ngx_left, delta_left, record_left_in_v, gc, rec_z=None, rec_x=None):
+    def enqueue_shot(self, nx, isx, isz, igz, ngx_left, delta_left, record_left_in_v, gc, rec_z=None, rec_x=None,
+                     nt=None):
+        """Queue a shot; records are [ntr, nt] (nt: the handle's, or the
+        shot's model's for run_models)."""
         g = np.ascontiguousarray(gc, dtype=np.int32)
         ntr = int(g.size)
-        rz = _f32(rec_z if rec_z is not None else np.zeros((ntr, self.nt), np.float32), (ntr, self.nt))
-        rx = _f32(rec_x if rec_x is not None else np.zeros((ntr, self.nt), np.float32), (ntr, self.nt))
+        n = self.nt if nt is None else int(nt)
+        rz = _f32(rec_z if rec_z is not None else np.zeros((ntr, n), np.float32), (ntr, n))
+        rx = _f32(rec_x if rec_x is not None else np.zeros((ntr, n), np.float32), (ntr, n))
         self._keep += [g, rz, rx]  # must outlive run()
         d = ShotDesc(nx=nx, isx=isx, isz=isz, igz=igz, ngx_left=ngx_left, delta_left=delta_left,
                      record_left_in_v=record_left_in_v, ntr=ntr, gc=_ip(g), rec_z=_fp(rz), rec_x=_fp(rx))
@@ -187,6 +191,55 @@ class FD2DGPU_ELASTIC:
         finally:
             self._keep = []
         return m.value, per[:n]
+
+    def born_adjoint(self):
+        """L^T d of the Born operator (stage 2) for the queued shots, their
+        records being d: (img_vp, img_vs) float64 [allnx, allnz]."""
+        shp = (self.allnx, self.allnz)
+        ip, isv = np.zeros(shp, np.float64), np.zeros(shp, np.float64)
+        dp = C.POINTER(C.c_double)
+        try:
+            _lib.check(_lib.load().sfwi_born_adjoint(self._h, ip.ctypes.data_as(dp), isv.ctypes.data_as(dp)))
+        finally:
+            self._keep = []
+        return ip, isv
+
+    def run_models(self, models, shot_model):
+        """One gradient run of the queued shots, shot i on models[shot_model[i]]
+        (sfwi_run_models).  `models` are dicts with vp, vs, rho (stage 1),
+        optional dvp, dvs ([allnx, allnz] each) and nt.  Returns
+        (per_shot_misfit, [(grad_pp, grad_ps, illum, grad_rho) per model]) in
+        FP64."""
+        descs = (_lib.ModelDesc * len(models))()
+        keep = []
+        sizes = []
+        for d, m in zip(descs, models):
+            vp = _f32(m["vp"])
+            allnx, allnz = vp.shape
+            arrs = {k: (None if m.get(k) is None else _f32(m[k], (allnx, allnz))) for k in ("vs", "rho", "dvp", "dvs")}
+            keep.append((vp, arrs))
+            d.allnx, d.allnz, d.nt = allnx, allnz, int(m["nt"])
+            d.vp = _fp(vp)
+            for k, a in arrs.items():
+                setattr(d, k, _fp(a))
+            sizes.append((allnx, allnz))
+        n = sum(a * b for a, b in sizes)
+        sm = np.ascontiguousarray(shot_model, dtype=np.int32)
+        nq = len(sm)
+        per = np.zeros(max(nq, 1), np.float64)
+        g = [np.zeros(max(n, 1), np.float64) for _ in range(4)]
+        dp = C.POINTER(C.c_double)
+        try:
+            _lib.check(_lib.load().sfwi_run_models(self._h, len(models), descs, _ip(sm), per.ctypes.data_as(dp),
+                                                   *[a.ctypes.data_as(dp) for a in g]))
+        finally:
+            self._keep = []
+        out, o = [], 0
+        for allnx, allnz in sizes:
+            k = allnx * allnz
+            out.append(tuple(a[o:o + k].reshape(allnx, allnz).copy() for a in g))
+            o += k
+        return per[:nq], out
 
     # -- line searches --
     def CALCULATE_ALPHA_parabola_mb(self, grad_pp, grad_ps, step1, step2):

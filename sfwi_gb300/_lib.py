@@ -20,6 +20,11 @@ class ShotDesc(C.Structure):
                 ("rec_z", _fp), ("rec_x", _fp)]
 
 
+class ModelDesc(C.Structure):
+    _fields_ = [("allnx", C.c_int), ("allnz", C.c_int), ("nt", C.c_int), ("vp", _fp), ("vs", _fp), ("rho", _fp),
+                ("dvp", _fp), ("dvs", _fp)]
+
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "sfwi_create": (C.c_int, [C.POINTER(_h), C.c_int, _fp, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
@@ -41,6 +46,8 @@ SIGNATURES = {
     "sfwi_enqueue_shot": (C.c_int, [_h, C.POINTER(ShotDesc)]),
     "sfwi_run": (C.c_int, [_h, _dp, _dp]),
     "sfwi_run_forward": (C.c_int, [_h]),
+    "sfwi_born_adjoint": (C.c_int, [_h, _dp, _dp]),
+    "sfwi_run_models": (C.c_int, [_h, C.c_int, C.POINTER(ModelDesc), _ip, _dp, _dp, _dp, _dp, _dp]),
     "sfwi_calculate_alpha_parabola_mb": (C.c_int, [_h, _fp, _fp, C.c_float, C.c_float, _dp, _dp, _dp]),
     "sfwi_calculate_alpha": (C.c_int, [_h, _fp, _fp, _fp, _fp, _dp, _dp]),
     "sfwi_line_search_parabola": (C.c_int, [_h, _fp, _fp, C.c_float, C.c_float, _dp, _dp]),

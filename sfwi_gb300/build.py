@@ -36,7 +36,7 @@ UNITS = [("sfwi_kernels.cu", "sfwi_kernels_%s.o" % n,
            "-DSFWI_TILE_X=%d" % tx, "-DSFWI_TILE_Z=%d" % tz, "-DSFWI_CTAS=%d" % c, "-DSFWI_STAGES=%d" % ns,
            "-DSFWI_CPT=%d" % cpt, "-DSFWI_VARIANT_NS=v%s" % n, "-DSFWI_VARIANT_FN=tile_variant_%s" % n])
          for tx, tz, c, ns, cpt, n in TILE_SHAPES]
-UNITS += [(f, f.replace(".cu", ".o"), []) for f in ("sfwi_aux.cu", "sfwi_ot.cu", "sfwi_engine.cu")]
+UNITS += [(f, f.replace(".cu", ".o"), []) for f in ("sfwi_aux.cu", "sfwi_ot.cu", "sfwi_adjoint.cu", "sfwi_engine.cu")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 

@@ -16,16 +16,21 @@ namespace sfwi {
 __global__ void k_setup(SetupArgs a) {
     const int s = blockIdx.y;
     const ShotGeo g = a.geo[s];
+    const int nzpml = g.nzpml;
+    // the shot's model: a slot of the uploaded model arrays, or (several
+    // models in one batch) its own grid in the concatenated model arrays
+    const size_t mbase = a.aux ? (size_t)a.aux[s].moff : 0;
+    const int allnz = a.aux ? a.aux[s].allnz : a.allnz;
     const long long n = (long long)g.nxpml * a.P;
     const float l10 = log10f(1 / 0.001f);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int lx = (int)(i / a.P), lz = (int)(i - (long long)lx * a.P);
         const size_t o = (size_t)(g.row0 + lx) * a.P + lz;
         float vp = 0.f, vs = 0.f, rho = 0.f, dmp = 0.f, dms = 0.f, dx = 0.f, dz = 0.f;
-        if (lz < a.nzpml) {
+        if (lz < nzpml) {
             const int cx = min(max(lx, a.pml), g.nxpml - a.pml - 1) - a.pml;
-            const int cz = min(max(lz, a.pml), a.nzpml - a.pml - 1) - a.pml;
-            const size_t go = (size_t)(g.win0 + cx) * a.allnz + cz;
+            const int cz = min(max(lz, a.pml), nzpml - a.pml - 1) - a.pml;
+            const size_t go = mbase + (size_t)(g.win0 + cx) * allnz + cz;
             const size_t gv = go + (size_t)g.model * a.vslot, gm = go + (size_t)g.model * a.mslot;
             vp = a.vp_all[gv];
             vs = a.vs_all[gv];
@@ -37,8 +42,8 @@ __global__ void k_setup(SetupArgs a) {
             if (lx > g.nxpml - pml)
                 dx = (float)(l10 * (5.0 * vp / (2.0 * pml)) * powf((float)(1.0 * (lx - (g.nxpml - pml)) / pml), 4.0f));
             if (lz < pml) dz = (float)(l10 * (5.0 * vp / (2.0 * pml)) * powf((float)(1.0 * (pml - lz) / pml), 4.0f));
-            if (lz > a.nzpml - pml)
-                dz = (float)(l10 * (5.0 * vp / (2.0 * pml)) * powf((float)(1.0 * (lz - (a.nzpml - pml)) / pml), 4.0f));
+            if (lz > nzpml - pml)
+                dz = (float)(l10 * (5.0 * vp / (2.0 * pml)) * powf((float)(1.0 * (lz - (nzpml - pml)) / pml), 4.0f));
         }
         a.vp[o] = vp;
         a.vs[o] = vs;
@@ -48,7 +53,7 @@ __global__ void k_setup(SetupArgs a) {
         a.lam[o] = rho * (vp * vp - 2 * vs * vs);
         a.mu[o] = rho * vs * vs;
         a.ib[o] = rho != 0.f ? 1.0f / rho : 0.f;
-        const bool born = lx >= a.born_lo && lx < g.nxpml - a.born_lo && lz >= a.born_lo && lz < a.nzpml - a.born_lo;
+        const bool born = lx >= a.born_lo && lx < g.nxpml - a.born_lo && lz >= a.born_lo && lz < nzpml - a.born_lo;
         a.bp[o] = born ? 2 * (rho * vp) * dmp : 0.f;
         a.bs[o] = born ? 2 * (rho * vs) * dms : 0.f;
     }
@@ -63,17 +68,21 @@ void launch_setup(const SetupArgs &a, int nshots, int max_nxpml, cudaStream_t st
 
 // Receiver-row records [nt][nrc][X] -> trace-major records [nrc][ntr][nt]:
 // trace tr reads packed row trow[tr] (-1: a cell outside the update region,
-// which the reference records as zero).  32 traces x 32 steps per block,
-// transposed through shared memory so both sides are coalesced.
-__global__ void k_record_gather(const float *__restrict__ rrow, const int *__restrict__ trow, int nt, int nrc, int X,
-                                int ntr, float *__restrict__ out, size_t cstride) {
+// which the reference records as zero).  A trace of a shot that runs fewer
+// steps than the batch (tlen) gets zeros after its last step.  32 traces x 32
+// steps per block, transposed through shared memory so both sides are
+// coalesced.
+__global__ void k_record_gather(const float *__restrict__ rrow, const int *__restrict__ trow,
+                                const int *__restrict__ tlen, int nt, int nrc, int X, int ntr, float *__restrict__ out,
+                                size_t cstride) {
     __shared__ float tile[32][33];
     const int c = blockIdx.z, r0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
     const int tr = r0 + threadIdx.x;
     const int row = tr < ntr ? trow[tr] : -1;
+    const int len = tr < ntr && tlen ? tlen[tr] : nt;
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
         const int t = t0 + k;
-        tile[k][threadIdx.x] = (row >= 0 && t < nt) ? rrow[((size_t)t * nrc + c) * X + row] : 0.f;
+        tile[k][threadIdx.x] = (row >= 0 && t < len) ? rrow[((size_t)t * nrc + c) * X + row] : 0.f;
     }
     __syncthreads();
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
@@ -82,10 +91,10 @@ __global__ void k_record_gather(const float *__restrict__ rrow, const int *__res
     }
 }
 
-void launch_record_gather(const float *rrow, const int *trow, int nt, int nrc, int X, int ntr, float *out,
-                          size_t cstride, cudaStream_t st) {
+void launch_record_gather(const float *rrow, const int *trow, const int *tlen, int nt, int nrc, int X, int ntr,
+                          float *out, size_t cstride, cudaStream_t st) {
     dim3 grid((ntr + 31) / 32, (nt + 31) / 32, nrc), block(32, 8);
-    k_record_gather<<<grid, block, 0, st>>>(rrow, trow, nt, nrc, X, ntr, out, cstride);
+    k_record_gather<<<grid, block, 0, st>>>(rrow, trow, tlen, nt, nrc, X, ntr, out, cstride);
 }
 
 // Residual source per packed row: rs[row][2 it + 0|1] = res_z|res_x of the

@@ -72,6 +72,7 @@ struct ShotGeo {
     int tr0;       // first trace in the packed trace arrays
     int win0;      // global-model column of interior column 0 (delta_left + record_left_in_v)
     int model;     // model slot the shot's window is cut from (line searches run several models)
+    int nzpml;     // padded depth of the shot's own grid (<= P; equal for every shot of a one-model batch)
 };
 
 // tile table entry: shot, first local row, first column, flags
@@ -86,7 +87,15 @@ struct Tile {
 struct alignas(16) TileRec {
     Tile t;
     ShotGeo g;
-    int pad[2];
+    int pad[1];
+};
+// per-shot data of the set-up, record and reduction kernels only (not read by
+// the step kernels): where the shot's model lives and how long it runs
+struct ShotAux {
+    long long moff;  // offset (floats) of the shot's model in the model arrays
+    int allnx, allnz;  // the model's grid
+    int nt;          // time steps of the shot (<= the batch's nt; the shot is idle after)
+    int pad;
 };
 static_assert(sizeof(TileRec) == 64, "TileRec is four 16-byte words");
 // source kinds: sou[it] into txx and tzz ahead of the velocity sweep (the

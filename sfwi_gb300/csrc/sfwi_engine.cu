@@ -86,6 +86,8 @@ struct DevBuf {
 struct ShotIn {
     int nx, win0, isx, isz, igz, ngx_left, ntr;
     int model = 0;  // model slot (line searches)
+    int req = -1;   // model of a several-model batch (sfwi_run_models), -1: the uploaded model
+    int nt = 0;     // time steps of the shot (0: the handle's nt)
     std::vector<int> gc;
     const float *obs_z = nullptr, *obs_x = nullptr;  // host [ntr][nt]
 };
@@ -102,6 +104,9 @@ struct Batch {
     std::vector<std::vector<int>> rcols;  // per shot: recording and injection columns (tile flags)
     std::vector<int> trow;      // packed receiver row of each trace, -1 outside the update region
     std::vector<int> rtr;       // per packed row: the trace whose residual is injected there, or -1
+    std::vector<ShotAux> aux;   // per shot: model offset and grid, time steps (several-model batches)
+    std::vector<int> tlen;      // per trace: samples of its shot, empty when every shot runs nt steps
+    std::vector<int> active;    // per time step: tiles of the shots still running (empty: all tiles)
     int rsp = 0;                // row length of the residual source (2 nt rounded up to 4)
     // device
     DevBuf<float> grid;      // NGRID * X * P
@@ -114,10 +119,13 @@ struct Batch {
     DevBuf<float> recs;      // NREC * ntr_tot * nt
     DevBuf<double> tmis;     // 2 * ntr_tot
     DevBuf<double> dsigma;
+    DevBuf<double> otscr;    // OT work arrays of traces longer than shared memory holds
     DevBuf<ShotGeo> dgeo;
     std::vector<TileRec> trecs;  // tiles with their shot geometry, as uploaded
     DevBuf<TileRec> dtiles;
     DevBuf<int> dtrow, drtr;
+    DevBuf<ShotAux> daux;
+    DevBuf<int> dtlen;
     size_t cells = 0;        // X * P
     DevBuf<int> derr;        // device-side error flag (bounded waits)
     DevBuf<int> dctr;        // dynamic tile counters of the step kernels (zeroed per run)
@@ -175,6 +183,24 @@ struct sfwi_handle {
     const float *slot_vp = nullptr, *slot_vs = nullptr, *slot_dvp = nullptr, *slot_dvs = nullptr;
     bool force_l2 = false;  // the exact step length is defined on the L2 residual
     DevBuf<float> ls_buf;   // trial models and search directions
+    // a batch over several models (sfwi_run_models): each model's grid, time
+    // steps and offset in the concatenated model and gradient arrays; empty
+    // while shots use the uploaded model
+    struct ModelIn {
+        int allnx, allnz, nt;
+        size_t off;
+    };
+    std::vector<ModelIn> models;
+    DevBuf<float> mvp, mvs, mrho, mdvp, mdvs;
+    DevBuf<double> mgrad;   // [grad_pp | grad_ps | illum | grad_rho] over the models' cells
+    size_t mcells = 0;
+    bool m_rho = false, m_dm = false;
+    std::vector<int> last_perm;  // queue index -> batch index of the last several-model run
+    // exact Born adjoint (sfwi_born_adjoint): adjoint state and gathered
+    // fields, accumulators, per-row shot and receiver tables, the image
+    DevBuf<float> adj_f;
+    DevBuf<double> adj_d, adj_img;
+    DevBuf<int> adj_i;
 };
 
 namespace {
@@ -277,10 +303,17 @@ const TileVariant *tile_variant(int shape) {
 // and keep more of them in flight (one 376x201 shot: 196 16x32 tiles for 304
 // slots; a step is 20 % faster on those tiles; a 38-shot batch is 14 %
 // faster on 16x32).  sfwi_set_tile_shape or sfwi_autotune replace the rule.
+// padded depth of a shot: its own model's in a several-model batch
+int shot_nzpml(const sfwi_handle *h, const ShotIn &in) {
+    return in.req >= 0 ? h->models[in.req].allnz + 2 * h->pml : h->nzpml;
+}
+
 void pick_tile_shape(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     long long tiles = 0;
-    const int zt = (h->nzpml - 2 * NOP + 31) / 32;
-    for (const ShotIn &in : shots) tiles += (long long)((in.nx + 2 * h->pml - 2 * NOP + 15) / 16) * zt;
+    for (const ShotIn &in : shots) {
+        const int zt = (shot_nzpml(h, in) - 2 * NOP + 31) / 32;
+        tiles += (long long)((in.nx + 2 * h->pml - 2 * NOP + 15) / 16) * zt;
+    }
     h->tv = tile_variant(tiles < 4LL * 2 * std::max(h->nsm, 1) ? SFWI_TILE_8x32_2CELL_3STAGE : SFWI_TILE_16x32);
 }
 
@@ -334,32 +367,45 @@ AxisTiling best_x_tiling(int nxpml, int pml, int tx, const AxisTiling &z) {
 // The batch's z tiling: the start (NOP - 8k, k >= 0, with an updated column
 // in the first tile) of least summed cost over the shots, each with its best
 // x start; NOP on ties.
-AxisTiling plan_z_tiling(int pml, int nzpml, int tx, int tz, const int *nxpml, int nshots) {
-    AxisTiling zt = axis_tiling(nzpml, pml, tz, NOP);
+// Shots of different depths (several-model batches) share the start; each
+// shot's tiles run to its own depth.
+int plan_z_start(int pml, const int *nzpml, int tx, int tz, const int *nxpml, int nshots) {
+    int start = NOP;
     double best = 0;
     static_assert(NOP % 8 == HALO % 8, "box columns NOP - HALO - 8k stay multiples of 8");
     for (int st = NOP; st > NOP - tz; st -= 8) {
-        const AxisTiling z = axis_tiling(nzpml, pml, tz, st);
         double cost = 0;
-        for (int s = 0; s < nshots; s++) cost += tiling_cost(best_x_tiling(nxpml[s], pml, tx, z), z);
+        for (int s = 0; s < nshots; s++) {
+            const AxisTiling z = axis_tiling(nzpml[s], pml, tz, st);
+            cost += tiling_cost(best_x_tiling(nxpml[s], pml, tx, z), z);
+        }
         if (st == NOP || cost < best) {
             best = cost;
-            zt = z;
+            start = st;
         }
     }
-    return zt;
+    return start;
+}
+AxisTiling plan_z_tiling(int pml, int nzpml, int tx, int tz, const int *nxpml, int nshots) {
+    const std::vector<int> depth(std::max(nshots, 1), nzpml);
+    return axis_tiling(nzpml, pml, tz, plan_z_start(pml, depth.data(), tx, tz, nxpml, nshots));
 }
 
 void build_tiles(sfwi_handle *h) {
     Batch &b = h->b;
-    const int pml = h->pml, nzpml = h->nzpml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
-    std::vector<int> widths;
-    for (const ShotGeo &g : b.geo) widths.push_back(g.nxpml);
-    const AxisTiling zt = plan_z_tiling(pml, nzpml, tx, tz, widths.data(), b.nshots);
+    const int pml = h->pml, tx = h->tv->tx, tz = h->tv->tz, halo = h->tv->halo;
+    std::vector<int> widths, depths;
+    for (const ShotGeo &g : b.geo) {
+        widths.push_back(g.nxpml);
+        depths.push_back(g.nzpml);
+    }
+    const int zstart = plan_z_start(pml, depths.data(), tx, tz, widths.data(), b.nshots);
     b.tiles.clear();
+    std::vector<int> shot_tiles(b.nshots, 0);
     for (int s = 0; s < b.nshots; s++) {
         const ShotGeo &g = b.geo[s];
-        const int nxpml = g.nxpml;
+        const int nxpml = g.nxpml, nzpml = g.nzpml;
+        const AxisTiling zt = axis_tiling(nzpml, pml, tz, zstart);
         const std::vector<int> &cols = b.rcols[s];
         const AxisTiling xt = best_x_tiling(nxpml, pml, tx, zt);
         for (int x0 = xt.start; x0 < nxpml - NOP; x0 += tx)
@@ -384,9 +430,21 @@ void build_tiles(sfwi_handle *h) {
                         }
                 if (g.isx >= bx0 && g.isx < bx1 && g.isz >= bz0 && g.isz < bz1) f |= TILE_SOURCE;
                 b.tiles.push_back(Tile{s, x0, z0, f});
+                shot_tiles[s]++;
             }
     }
     b.ntiles = (int)b.tiles.size();
+    // shots that run fewer steps than the batch come last (non-increasing
+    // nt): at step it the tiles of the shots still running are a prefix of
+    // the table
+    b.active.clear();
+    bool uneven = false;
+    for (const ShotAux &a : b.aux) uneven |= a.nt != h->nt;
+    if (uneven) {
+        b.active.assign(h->nt, 0);
+        for (int s = 0; s < b.nshots; s++)
+            for (int it = 0; it < b.aux[s].nt; it++) b.active[it] += shot_tiles[s];
+    }
 }
 
 // The tile table as the step kernels read it: each tile with its shot's
@@ -431,23 +489,37 @@ int encode_tile_maps(sfwi_handle *h, bool forward_only) {
 
 int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     Batch &b = h->b;
-    const int pml = h->pml, nzpml = h->nzpml, nt = h->nt, nz = h->allnz;
+    const int pml = h->pml, nt = h->nt;
     b.nshots = (int)shots.size();
-    b.P = (nzpml + 3) & ~3;
+    int maxz = 0;
+    for (const ShotIn &in : shots) maxz = std::max(maxz, shot_nzpml(h, in));
+    b.P = (maxz + 3) & ~3;
     b.geo.assign(b.nshots, ShotGeo{});
+    b.aux.assign(b.nshots, ShotAux{});
     b.tiles.clear();
     b.rcols.clear();
     b.trow.clear();
     b.rtr.clear();
+    b.tlen.clear();
     int row = 0, tr0 = 0;
     b.max_nxpml = 0;
+    bool uneven = false;
     for (int s = 0; s < b.nshots; s++) {
         const ShotIn &in = shots[s];
         ShotGeo &g = b.geo[s];
-        const int nxpml = in.nx + 2 * pml;
-        if (in.nx < 1 || in.win0 < 0 || in.win0 + in.nx > h->allnx)
+        ShotAux &a = b.aux[s];
+        const int nxpml = in.nx + 2 * pml, nzpml = shot_nzpml(h, in);
+        const int allnx = in.req >= 0 ? h->models[in.req].allnx : h->allnx;
+        a.moff = in.req >= 0 ? (long long)h->models[in.req].off : 0;
+        a.allnx = allnx;
+        a.allnz = nzpml - 2 * pml;
+        a.nt = in.nt > 0 ? in.nt : nt;
+        if (a.nt > nt || (s > 0 && a.nt > b.aux[s - 1].nt))
+            return fail(SFWI_E_ARG, "shot %d: %d steps (at most %d, and no more than the shot before)", s, a.nt, nt);
+        uneven |= a.nt != nt;
+        if (in.nx < 1 || in.win0 < 0 || in.win0 + in.nx > allnx)
             return fail(SFWI_E_ARG, "shot %d: window [%d, %d) outside the model width %d", s, in.win0,
-                        in.win0 + in.nx, h->allnx);
+                        in.win0 + in.nx, allnx);
         if (in.isx < 0 || in.isx >= nxpml || in.isz < 0 || in.isz >= nzpml)
             return fail(SFWI_E_ARG, "shot %d: source cell (%d, %d) outside the %d x %d grid", s, in.isx, in.isz, nxpml,
                         nzpml);
@@ -463,6 +535,7 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
         g.tr0 = tr0;
         g.win0 = in.win0;
         g.model = in.model;
+        g.nzpml = nzpml;
         // receiver rows: the record of a trace is its cell (rix, igz), which
         // stays zero outside the update region [NOP, n-NOP); the residual
         // injected at a cell (iix, igz) is the highest-index trace injected there
@@ -490,6 +563,8 @@ int build_batch(sfwi_handle *h, const std::vector<ShotIn> &shots) {
     }
     b.X = row;
     b.ntr_tot = tr0;
+    if (uneven)
+        for (int s = 0; s < b.nshots; s++) b.tlen.insert(b.tlen.end(), b.geo[s].ntr, b.aux[s].nt);
     build_tiles(h);
     b.rsp = (2 * nt + 3) & ~3;
     b.cells = (size_t)b.X * b.P;
@@ -586,6 +661,8 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(b.dgeo.ensure(b.geo.size()));
     CK(b.dtrow.ensure(std::max<size_t>(b.trow.size(), 1)));
     CK(b.drtr.ensure(b.rtr.size()));
+    CK(b.daux.ensure(b.aux.size()));
+    if (!b.tlen.empty()) CK(b.dtlen.ensure(b.tlen.size()));
     CK(b.derr.ensure(1));
     CK(cudaMemsetAsync(b.derr.p, 0, sizeof(int), h->st));
     const size_t nctr = 4 * (size_t)std::max(h->nt, kTimeKernelsMaxReps + 1);
@@ -599,17 +676,30 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     if (!b.trow.empty())
         CK(cudaMemcpyAsync(b.dtrow.p, b.trow.data(), b.trow.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(b.drtr.p, b.rtr.data(), b.rtr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(b.daux.p, b.aux.data(), b.aux.size() * sizeof(ShotAux), cudaMemcpyHostToDevice, st));
+    if (!b.tlen.empty())
+        CK(cudaMemcpyAsync(b.dtlen.p, b.tlen.data(), b.tlen.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     // zero the state (fields, memory variables, accumulators) and the records
     CK(cudaMemsetAsync(b.grid.p, 0, (size_t)NSTATE * b.cells * sizeof(float), st));
     CK(cudaMemsetAsync(b.recs.p, 0, recs * sizeof(float), st));
-    // observed records, trace-major
+    // observed records, trace-major ([ntr][its nt] on the host; a shot with
+    // fewer steps than the batch keeps zeros after its last sample)
     if (with_obs) {
         for (size_t s = 0; s < shots.size(); s++) {
             const ShotIn &in = shots[s];
+            const int ns = b.aux[s].nt;
             const size_t off = (size_t)b.geo[s].tr0 * nt, n = (size_t)in.ntr * nt;
             if (!n) continue;
-            if (in.obs_z) CK(cudaMemcpyAsync(b.r(R_OBS_Z, nt) + off, in.obs_z, n * sizeof(float), cudaMemcpyHostToDevice, st));
-            if (in.obs_x) CK(cudaMemcpyAsync(b.r(R_OBS_X, nt) + off, in.obs_x, n * sizeof(float), cudaMemcpyHostToDevice, st));
+            const float *src[2] = {in.obs_z, in.obs_x};
+            float *dst[2] = {b.r(R_OBS_Z, nt) + off, b.r(R_OBS_X, nt) + off};
+            for (int c = 0; c < 2; c++) {
+                if (!src[c]) continue;
+                if (ns == nt)
+                    CK(cudaMemcpyAsync(dst[c], src[c], n * sizeof(float), cudaMemcpyHostToDevice, st));
+                else
+                    CK(cudaMemcpy2DAsync(dst[c], (size_t)nt * sizeof(float), src[c], (size_t)ns * sizeof(float),
+                                         (size_t)ns * sizeof(float), in.ntr, cudaMemcpyHostToDevice, st));
+            }
         }
     }
     SetupArgs a{};
@@ -629,6 +719,16 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     a.dvp_all = h->slot_dvp ? h->slot_dvp : (h->stage == 2 && h->have_m ? h->dvp_all.p : nullptr);
     a.dvs_all = h->slot_dvs ? h->slot_dvs : (h->stage == 2 && h->have_m ? h->dvs_all.p : nullptr);
     a.mslot = h->slot_dvp ? nmodel : 0;
+    if (!h->models.empty()) {
+        // several models: each shot's own, at its offset in the concatenated arrays
+        a.vp_all = h->mvp.p;
+        a.vs_all = h->mvs.p;
+        a.rho_all = h->m_rho ? h->mrho.p : h->mvp.p;
+        a.dvp_all = h->stage == 2 && h->m_dm ? h->mdvp.p : nullptr;
+        a.dvs_all = h->stage == 2 && h->m_dm ? h->mdvs.p : nullptr;
+        a.vslot = a.mslot = 0;
+        a.aux = b.daux.p;
+    }
     a.ib = b.g(C_IB);
     a.lam = b.g(C_LAM);
     a.mu = b.g(C_MU);
@@ -669,25 +769,36 @@ std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     for (auto &g : b.geo) {
         s.push_back(g.isx * 100003LL + g.isz);
         s.push_back(g.igz * 1000003LL + g.nx);
-        s.push_back(g.row0);
+        s.push_back(g.row0 * 100003LL + g.nzpml);
     }
+    s.insert(s.end(), b.active.begin(), b.active.end());
     return s;
+}
+
+// the launch parameters of step `it`: with shots of different lengths, only
+// the tiles of the shots still running (a prefix of the table)
+Params step_params(const sfwi_handle *h, const Params &p, int it) {
+    Params q = p;
+    if (!h->b.active.empty()) q.ntiles = h->b.active[it];
+    return q;
 }
 
 void enqueue_forward(sfwi_handle *h, const Params &p, bool forward_only) {
     const bool born = h->stage == 2;
     (void)forward_only;
     for (int it = 0; it < h->nt; it++) {
-        h->tv->launch(0, p, h->b.tm, it, born, 1.f, h->st);
-        h->tv->launch(1, p, h->b.tm, it, born, 1.f, h->st);
+        const Params q = step_params(h, p, it);
+        h->tv->launch(0, q, h->b.tm, it, born, 1.f, h->st);
+        h->tv->launch(1, q, h->b.tm, it, born, 1.f, h->st);
     }
 }
 
 void enqueue_backward(sfwi_handle *h, const Params &p) {
     const float adj = h->stage == 1 ? 1.f : -1.f;
     for (int it = h->nt - 1; it >= 0; it--) {
-        h->tv->launch(2, p, h->b.tm, it, false, adj, h->st);
-        h->tv->launch(3, p, h->b.tm, it, false, adj, h->st);
+        const Params q = step_params(h, p, it);
+        h->tv->launch(2, q, h->b.tm, it, false, adj, h->st);
+        h->tv->launch(3, q, h->b.tm, it, false, adj, h->st);
     }
 }
 
@@ -759,7 +870,7 @@ int finish_misfit(sfwi_handle *h, int misfit_kind, double *misfit, double *per_s
 enum RunMode { RUN_GRADIENT, RUN_FORWARD, RUN_MISFIT };
 
 int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double *misfit, double *per_shot) {
-    if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
+    if (!h->have_model && h->models.empty()) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
     if (shots.empty()) return fail(SFWI_E_ARG, "no shots queued");
     const bool forward_only = mode != RUN_GRADIENT;
     const int misfit_kind = h->force_l2 ? SFWI_MISFIT_L2 : h->misfit_kind;
@@ -774,8 +885,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     h->b.ready = false;  // until this batch is on the device
     int rc = build_batch(h, shots);
     if (rc) return rc;
-    if (mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2 && h->nt > ot_max_nt())
-        return fail(SFWI_E_ARG, "OT misfit supports nt <= %d", ot_max_nt());
+    if (!h->b.tlen.empty() && ((mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2) || h->snap_every > 0))
+        return fail(SFWI_E_ARG, "shots of different lengths in one run take the L2 misfit and no snapshots");
     rc = upload_batch(h, shots, forward_only, mode != RUN_FORWARD);
     if (rc) return rc;
     Batch &b = h->b;
@@ -805,8 +916,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     CK(cudaEventRecord(h->ev[1], st));
     // receiver-row records to trace-major records
     if (b.ntr_tot) {
-        launch_record_gather(b.rrow.p, b.dtrow.p, nt, h->stage == 2 ? 4 : 2, b.X, b.ntr_tot, b.r(R_SYN_Z, nt),
-                             (size_t)b.ntr_tot * nt, st);
+        launch_record_gather(b.rrow.p, b.dtrow.p, b.tlen.empty() ? nullptr : b.dtlen.p, nt, h->stage == 2 ? 4 : 2,
+                             b.X, b.ntr_tot, b.r(R_SYN_Z, nt), (size_t)b.ntr_tot * nt, st);
         h->launches++;
     }
     CK(cudaGetLastError());
@@ -845,6 +956,10 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
         o.res_x = b.r(R_RES_X, nt);
         o.sigma = b.dsigma.p;
         o.trace_misfit = b.tmis.p;
+        if (const size_t nscr = ot_scratch_doubles(nt, b.ntr_tot)) {
+            CK(b.otscr.ensure(nscr));
+            o.scratch = b.otscr.p;
+        }
         CK(launch_ot(o, st));
     }
     if (mode == RUN_MISFIT) return finish_misfit(h, misfit_kind, misfit, per_shot);
@@ -880,8 +995,32 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     fa.gil = h->gil.p;
     fa.grho = h->want_rho ? b.g(G_RHO) : nullptr;
     fa.grh = h->grh.p;
-    launch_finalize(fa, st);
-    h->launches++;
+    if (h->models.empty()) {
+        launch_finalize(fa, st);
+        h->launches++;
+    } else {
+        // several models: each model's shots (consecutive in the batch) into
+        // that model's own gradients, zeroed before the run
+        const size_t mc = h->mcells;
+        for (int s0 = 0; s0 < b.nshots;) {
+            const int m = shots[s0].req;
+            int s1 = s0 + 1;
+            while (s1 < b.nshots && shots[s1].req == m) s1++;
+            const sfwi_handle::ModelIn &mi = h->models[m];
+            FinalArgs f = fa;
+            f.allnx = mi.allnx;
+            f.allnz = mi.allnz;
+            f.nshots = s1 - s0;
+            f.geo = b.dgeo.p + s0;
+            f.gpp = h->mgrad.p + mi.off;
+            f.gps = h->mgrad.p + mc + mi.off;
+            f.gil = h->mgrad.p + 2 * mc + mi.off;
+            f.grh = h->mgrad.p + 3 * mc + mi.off;
+            launch_finalize(f, st);
+            h->launches++;
+            s0 = s1;
+        }
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[5], st));
     return collect_misfit(h, misfit_kind, misfit, per_shot, true);
@@ -892,9 +1031,11 @@ template <class F>
 void for_each_buf(sfwi_handle *h, F f) {
     Batch &b = h->b;
     f(b.grid), f(b.tb), f(b.lr), f(b.rrow), f(b.rsrc), f(b.recs), f(b.tmis), f(b.dsigma), f(b.dgeo), f(b.dtiles);
-    f(b.dtrow), f(b.drtr), f(b.derr), f(b.dctr), f(b.snap), f(b.sscale);
+    f(b.dtrow), f(b.drtr), f(b.derr), f(b.dctr), f(b.snap), f(b.sscale), f(b.otscr);
     f(h->sou), f(h->vp_all), f(h->vs_all), f(h->rho_all), f(h->dvp_all), f(h->dvs_all);
     f(h->gpp), f(h->gps), f(h->gil), f(h->grh), f(h->ls_buf);
+    f(h->mvp), f(h->mvs), f(h->mrho), f(h->mdvp), f(h->mdvs), f(h->mgrad);
+    f(h->adj_f), f(h->adj_d), f(h->adj_img), f(h->adj_i), f(b.daux), f(b.dtlen);
 }
 
 int check(sfwi_handle *h) {
@@ -1023,6 +1164,149 @@ int line_search_exact(sfwi_handle *h, const std::vector<ShotIn> &q, const float 
     return SFWI_OK;
 }
 
+// The exact adjoint of the stage-2 Born modelling operator over shots q, the
+// queued shots' records being the data d: img_vp, img_vs += L^T d.  The
+// background forward runs first and keeps its velocity after every step's
+// velocity sweep (FP32 snapshots, the fields the Born source differentiates);
+// then the transposed sweeps run from the last step to the first
+// (sfwi_adjoint.cu) and the window accumulators are folded into the model.
+int born_adjoint(sfwi_handle *h, const std::vector<ShotIn> &q, double *img_vp, double *img_vs) {
+    if (h->stage != 2) return fail(SFWI_E_STATE, "the Born operator belongs to stage 2");
+    if (!h->have_model) return fail(SFWI_E_STATE, "no model: call sfwi_gpu_buffer_vpvs first");
+    if (q.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    if (!img_vp || !img_vs) return fail(SFWI_E_ARG, "null output");
+    CK(cudaSetDevice(h->device));
+    const int snap_every = h->snap_every, snap_fmt = h->snap_fmt, misfit_kind = h->misfit_kind;
+    const bool want_rho = h->want_rho;
+    h->snap_every = 1;
+    h->snap_fmt = SNAP_F32;
+    h->want_rho = false;
+    h->misfit_kind = SFWI_MISFIT_L2;
+    struct Restore {
+        sfwi_handle *h;
+        int se, sf, mk;
+        bool wr;
+        ~Restore() {
+            h->snap_every = se;
+            h->snap_fmt = sf;
+            h->misfit_kind = mk;
+            h->want_rho = wr;
+        }
+    } restore{h, snap_every, snap_fmt, misfit_kind, want_rho};
+    if (h->tile_auto) pick_tile_shape(h, q);
+    h->b.ready = false;
+    h->last_perm.clear();
+    if (int rc = build_batch(h, q)) return rc;
+    if (int rc = upload_batch(h, q, false, true)) return rc;
+    Batch &b = h->b;
+    b.ready = true;
+    const Params p = make_params(h, false);
+    const int nt = h->nt;
+    cudaStream_t st = h->st;
+    // the strains of the Born source reach the outer rows and columns of a
+    // shot, which no tile stores: they must read as the zeros they are
+    CK(cudaMemsetAsync(b.snap.p, 0, (size_t)b.nsnap * 2 * b.X * b.PS * sizeof(float), st));
+    // the background forward with its snapshots (no scattered field)
+    CK(cudaEventRecord(h->ev[0], st));
+    for (int it = 0; it < nt; it++) {
+        h->tv->launch(0, p, b.tm, it, false, 1.f, st);
+        h->tv->launch(1, p, b.tm, it, false, 1.f, st);
+    }
+    h->launches += 2LL * nt;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[1], st));
+    // adjoint workspace: 18 float fields, 2 double accumulators, tables
+    const size_t cells = b.cells, gcells = (size_t)h->allnx * h->allnz;
+    CK(h->adj_f.ensure(18 * cells));
+    CK(h->adj_d.ensure(2 * cells));
+    CK(h->adj_img.ensure(2 * gcells));
+    CK(cudaMemsetAsync(h->adj_f.p, 0, 18 * cells * sizeof(float), st));
+    CK(cudaMemsetAsync(h->adj_d.p, 0, 2 * cells * sizeof(double), st));
+    CK(cudaMemsetAsync(h->adj_img.p, 0, 2 * gcells * sizeof(double), st));
+    // per packed row: its shot, and the traces recorded at its receiver cell
+    std::vector<int> tab(b.X + (b.X + 1) + std::max(b.ntr_tot, 1), 0);
+    int *rowshot = tab.data(), *rstart = rowshot + b.X, *rtr = rstart + b.X + 1;
+    for (int s2 = 0; s2 < b.nshots; s2++)
+        for (int r = 0; r < b.geo[s2].nxpml; r++) rowshot[b.geo[s2].row0 + r] = s2;
+    std::vector<int> cnt(b.X, 0);
+    for (int t = 0; t < b.ntr_tot; t++)
+        if (b.trow[t] >= 0) cnt[b.trow[t]]++;
+    for (int r = 0; r < b.X; r++) rstart[r + 1] = rstart[r] + cnt[r];
+    std::vector<int> fill(rstart, rstart + b.X);
+    for (int t = 0; t < b.ntr_tot; t++)
+        if (b.trow[t] >= 0) rtr[fill[b.trow[t]]++] = t;
+    CK(h->adj_i.ensure(tab.size()));
+    CK(cudaMemcpyAsync(h->adj_i.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    AdjArgs a{};
+    a.X = b.X;
+    a.P = b.P;
+    a.PS = b.PS;
+    a.pml = h->pml;
+    a.nt = nt;
+    a.born_lo = NOP;
+    a.dt = h->dt;
+    a.dtdx = h->dt / h->dx;
+    a.dtdz = h->dt / h->dz;
+    a.idx = 1.0f / h->dx;
+    a.idz = 1.0f / h->dz;
+    a.geo = b.dgeo.p;
+    a.rowshot = h->adj_i.p;
+    a.rstart = h->adj_i.p + b.X;
+    a.rtr = h->adj_i.p + 2 * b.X + 1;
+    a.ib = b.g(C_IB);
+    a.lam = b.g(C_LAM);
+    a.mu = b.g(C_MU);
+    a.dampx = b.g(C_DX);
+    a.dampz = b.g(C_DZ);
+    float *w = h->adj_f.p;
+    float **fields[18] = {&a.avx, &a.avz, &a.amx, &a.amz, &a.atxx, &a.atzz, &a.atxz, &a.amxx, &a.amzz,
+                          &a.amxz, &a.gax, &a.gbz, &a.gcz, &a.gdx, &a.hax, &a.hbz, &a.hdx, &a.hcz};
+    for (int k = 0; k < 18; k++) *fields[k] = w + (size_t)k * cells;
+    a.dbp = h->adj_d.p;
+    a.dbs = h->adj_d.p + cells;
+    a.snap = reinterpret_cast<const float *>(b.snap.p);
+    a.dz = b.r(R_OBS_Z, nt);
+    a.dx = b.r(R_OBS_X, nt);
+    CK(cudaEventRecord(h->ev[2], st));
+    for (int it = nt - 1; it >= 0; it--) launch_adjoint_step(a, it, st);
+    h->launches += 3LL * nt;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[3], st));
+    ImageArgs im{};
+    im.allnx = h->allnx;
+    im.allnz = h->allnz;
+    im.P = b.P;
+    im.pml = h->pml;
+    im.nshots = b.nshots;
+    im.geo = b.dgeo.p;
+    im.dbp = a.dbp;
+    im.dbs = a.dbs;
+    im.vp = b.g(C_VP);
+    im.vs = b.g(C_VS);
+    im.rho = b.g(C_RHO);
+    im.img_vp = h->adj_img.p;
+    im.img_vs = h->adj_img.p + gcells;
+    launch_born_image(im, st);
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[5], st));
+    std::vector<double> out(2 * gcells);
+    CK(cudaMemcpyAsync(out.data(), h->adj_img.p, 2 * gcells * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int derr = 0;
+    CK(cudaMemcpyAsync(&derr, b.derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (derr) return fail(SFWI_E_CUDA, "a device-side pipeline wait timed out (code %d)", derr);
+    cudaEventElapsedTime(&h->fwd_ms, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&h->bwd_ms, h->ev[2], h->ev[3]);
+    cudaEventElapsedTime(&h->total_ms, h->ev[4], h->ev[5]);
+    h->other_ms = 0.f;
+    for (size_t i = 0; i < gcells; i++) {
+        img_vp[i] += out[i];
+        img_vs[i] += out[gcells + i];
+    }
+    return SFWI_OK;
+}
+
 int ensure_grads(sfwi_handle *h) {
     const size_t n = (size_t)h->allnx * h->allnz;
     if (h->gpp.p) return SFWI_OK;
@@ -1049,12 +1333,13 @@ int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x
     if (!obs_x || !obs_z || !cal_x || !cal_z || !res_x || !res_z || !misfit || length < 1 || tracenum < 0)
         return fail(SFWI_E_ARG, "sfwi_ot: bad argument");
     if (tracenum == 0) return SFWI_OK;
-    if (length > ot_max_nt()) return fail(SFWI_E_ARG, "sfwi_ot: length %d exceeds %d samples", length, ot_max_nt());
     const size_t n = (size_t)length * tracenum;
     float *d = nullptr;
     double *dd = nullptr;
     CK(cudaMalloc(&d, 6 * n * sizeof(float)));
-    cudaError_t e = cudaMalloc(&dd, 4 * (size_t)tracenum * sizeof(double));
+    // traces too long for shared memory work in global scratch after the sums
+    const size_t nscr = ot_scratch_doubles(length, tracenum);
+    cudaError_t e = cudaMalloc(&dd, (4 * (size_t)tracenum + nscr) * sizeof(double));
     if (e != cudaSuccess) {
         cudaFree(d);
         return fail(SFWI_E_NOMEM, "sfwi_ot: %s", cudaGetErrorString(e));
@@ -1099,6 +1384,7 @@ int ot_host(int kind, const float *obs_x, const float *obs_z, const float *cal_x
         o.res_x = d + 5 * n;
         o.sigma = dd;
         o.trace_misfit = dd + 2 * tracenum;
+        o.scratch = nscr ? dd + 4 * (size_t)tracenum : nullptr;
         if ((e = launch_ot(o, 0)) != cudaSuccess) break;
         if ((e = cudaMemcpy(res_z, d + 4 * n, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
         if ((e = cudaMemcpy(res_x, d + 5 * n, n * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
@@ -1357,6 +1643,7 @@ int sfwi_read_records(sfwi_handle *h, int i, float *syn_z, float *syn_x, float *
     if (int rc = check(h)) return rc;
     if (!h->b.ready) return fail(SFWI_E_STATE, "no records: the last run did not complete");
     if (i < 0 || i >= (int)h->last_ntr.size()) return fail(SFWI_E_ARG, "shot %d not in the last run", i);
+    if (!h->last_perm.empty()) i = h->last_perm[i];  // several-model runs reorder the shots
     const int nt = h->nt;
     const size_t off = (size_t)h->last_tr0[i] * nt, n = (size_t)h->last_ntr[i] * nt;
     Batch &b = h->b;
@@ -1398,10 +1685,93 @@ int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit) {
     if (int rc = check(h)) return rc;
     std::vector<ShotIn> q;
     q.swap(h->queue);
+    h->last_perm.clear();
     double m = 0.0;
     int rc = run_batch(h, q, RUN_GRADIENT, &m, per_shot_misfit);
     if (rc) return rc;
     if (misfit) *misfit += m;
+    return SFWI_OK;
+}
+
+int sfwi_run_models(sfwi_handle *h, int nmodels, const sfwi_model_desc *models, const int *shot_model,
+                    double *per_shot_misfit, double *grad_pp, double *grad_ps, double *illum, double *grad_rho) {
+    if (int rc = check(h)) return rc;
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    h->last_perm.clear();
+    if (nmodels < 1 || !models || !shot_model) return fail(SFWI_E_ARG, "no models");
+    if (q.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    // the models: grids within the handle's depth, lengths within its nt
+    std::vector<sfwi_handle::ModelIn> mi(nmodels);
+    size_t cells = 0;
+    bool any_rho = false, any_dm = false;
+    for (int k = 0; k < nmodels; k++) {
+        const sfwi_model_desc &m = models[k];
+        if (m.allnx < 1 || m.allnz < 1 || m.allnz + 2 * h->pml > h->nzpml || m.nt < 1 || m.nt > h->nt || !m.vp ||
+            !m.vs)
+            return fail(SFWI_E_ARG, "model %d: %d x %d, nt %d (depth at most %d, nt at most %d)", k, m.allnx, m.allnz,
+                        m.nt, h->nzpml - 2 * h->pml, h->nt);
+        if (h->stage == 1 && !m.rho) return fail(SFWI_E_ARG, "model %d: stage 1 needs rho", k);
+        if ((m.dvp == nullptr) != (m.dvs == nullptr)) return fail(SFWI_E_ARG, "model %d: dvp and dvs go together", k);
+        mi[k] = sfwi_handle::ModelIn{m.allnx, m.allnz, m.nt, cells};
+        cells += (size_t)m.allnx * m.allnz;
+        any_rho |= m.rho != nullptr;
+        any_dm |= m.dvp != nullptr;
+    }
+    for (size_t i = 0; i < q.size(); i++)
+        if (shot_model[i] < 0 || shot_model[i] >= nmodels)
+            return fail(SFWI_E_ARG, "shot %zu: model %d of %d", i, shot_model[i], nmodels);
+    // batch order: longer runs first (the shots still running at a step are
+    // a prefix of the tile table), each model's shots together, queue order
+    std::vector<int> order(q.size());
+    for (size_t i = 0; i < q.size(); i++) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int na = mi[shot_model[a]].nt, nb = mi[shot_model[b]].nt;
+        return na != nb ? na > nb : shot_model[a] < shot_model[b];
+    });
+    std::vector<ShotIn> batch;
+    for (int i : order) {
+        batch.push_back(q[i]);
+        batch.back().req = shot_model[i];
+        batch.back().nt = mi[shot_model[i]].nt;
+    }
+    CK(cudaSetDevice(h->device));
+    const size_t bytes = std::max<size_t>(cells, 1);
+    DevBuf<float> *arr[5] = {&h->mvp, &h->mvs, &h->mrho, &h->mdvp, &h->mdvs};
+    for (int a = 0; a < 5; a++)
+        if (a < 2 || (a == 2 && any_rho) || (a > 2 && any_dm)) CK(arr[a]->ensure(bytes));
+    for (int k = 0; k < nmodels; k++) {
+        const sfwi_model_desc &m = models[k];
+        const size_t n = (size_t)m.allnx * m.allnz, o = mi[k].off;
+        const float *src[5] = {m.vp, m.vs, m.rho, m.dvp, m.dvs};
+        for (int a = 0; a < 5; a++) {
+            if (!arr[a]->p) continue;
+            if (src[a])
+                CK(cudaMemcpyAsync(arr[a]->p + o, src[a], n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+            else
+                CK(cudaMemsetAsync(arr[a]->p + o, 0, n * sizeof(float), h->st));
+        }
+    }
+    CK(h->mgrad.ensure(4 * bytes));
+    CK(cudaMemsetAsync(h->mgrad.p, 0, 4 * bytes * sizeof(double), h->st));
+    h->models = mi;
+    h->mcells = cells;
+    h->m_rho = any_rho;
+    h->m_dm = any_dm;
+    std::vector<double> per(batch.size());
+    int rc = run_batch(h, batch, RUN_GRADIENT, nullptr, per.data());
+    h->models.clear();
+    if (rc) return rc;
+    h->last_perm.assign(q.size(), 0);
+    for (size_t k = 0; k < order.size(); k++) {
+        h->last_perm[order[k]] = (int)k;
+        if (per_shot_misfit) per_shot_misfit[order[k]] = per[k];
+    }
+    double *outs[4] = {grad_pp, grad_ps, illum, grad_rho};
+    for (int a = 0; a < 4; a++)
+        if (outs[a] && cells)
+            CK(cudaMemcpyAsync(outs[a], h->mgrad.p + a * bytes, cells * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return SFWI_OK;
 }
 
@@ -1444,6 +1814,13 @@ int sfwi_line_search_exact(sfwi_handle *h, const float *image_pp, const float *i
     std::vector<ShotIn> q;
     q.swap(h->queue);
     return line_search_exact(h, q, image_pp, image_ps, cg_pp, cg_ps, fenzi, fenmu, per_shot2);
+}
+
+int sfwi_born_adjoint(sfwi_handle *h, double *img_vp, double *img_vs) {
+    if (int rc = check(h)) return rc;
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    return born_adjoint(h, q, img_vp, img_vs);
 }
 
 int sfwi_run_forward(sfwi_handle *h) {

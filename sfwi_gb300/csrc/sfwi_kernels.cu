@@ -321,8 +321,8 @@ __device__ __forceinline__ CellMap cell_map(const Params &p, const Tile &t, cons
     // lz is a multiple of CPT, as are NOP and P: the thread's cells lie wholly
     // before NOP (a tile grid may start there; not live) or at or after it,
     // and lz+CPT-1 < P
-    m.live = row_ok && m.lz >= NOP && m.lz < p.nzpml - NOP;
-    const int pml = p.pml, nzpml = p.nzpml, nxpml = g.nxpml;
+    m.live = row_ok && m.lz >= NOP && m.lz < g.nzpml - NOP;
+    const int pml = p.pml, nzpml = g.nzpml, nxpml = g.nxpml;
     const bool xi = m.lx >= pml && m.lx < nxpml - pml;
     // damping is non-zero exactly for lx < pml, lx > nxpml-pml, lz < pml or
     // lz > nzpml-pml (k_setup); every other cell takes the plain update in
@@ -914,7 +914,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // edge strips of the background velocity after this step: the core
         // cells of this tile inside each of the four bands
         if ((c.t.flags & TILE_STRIP) && p.tb) {
-            const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml;
+            const int pml = p.pml, nxpml = c.g.nxpml, nzpml = c.g.nzpml;
             for (int band = 0; band < 4; band++) {
                 const Band bb = band_rect(band, pml, nxpml, nzpml);
                 if (max(bb.x0, c.t.x0) >= min(bb.x1, c.t.x0 + TX) || max(bb.z0, c.t.z0) >= min(bb.z1, c.t.z0 + TZ))
@@ -1174,7 +1174,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
         const bool strip = c.t.flags & TILE_STRIP, recv = c.t.flags & TILE_RECV;
-        const StripPick sp = strip ? strip_pick(c, p.pml, p.nzpml) : StripPick{-1, -1};
+        const StripPick sp = strip ? strip_pick(c, p.pml, c.g.nzpml) : StripPick{-1, -1};
         const uint32_t bytes = S::NB * BOX_BYTES + (8 + (frame ? 6 : 0) + (image ? 2 : 0)) * CORE_BYTES +
                                (sp.tb >= 0 ? 2 * S::TBF * 4 : 0) + (sp.lr >= 0 ? 2 * S::LRF * 4 : 0) +
                                (recv ? S::RSF * 4 : 0);
@@ -1206,7 +1206,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     auto body = [&](const TileCtx &c, float *s, StageRelease &release) {
         float *s_vx = s, *s_vz = s + BOX, *a_vx = s + 2 * BOX, *a_vz = s + 3 * BOX;
         const float *core = s + S::NB * BOX;
-        const int pml = p.pml, nxpml = c.g.nxpml, nzpml = p.nzpml;
+        const int pml = p.pml, nxpml = c.g.nxpml, nzpml = c.g.nzpml;
         if (c.t.flags & TILE_STRIP) {
             // the saved strips of step `it` replace vx, vz in this sweep's view:
             // the box cells inside each band (a cell in two bands holds the

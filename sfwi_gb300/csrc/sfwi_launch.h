@@ -45,10 +45,15 @@ struct SetupArgs {
     size_t vslot, mslot;  // floats between model slots of vp/vs and of dvp/dvs (0: one model)
     float *ib, *lam, *mu, *dampx, *dampz, *bp, *bs, *vp, *vs, *rho;
     const ShotGeo *geo;
+    // batches of shots on several models (sfwi_run_models): each shot's model
+    // at aux[s].moff in the concatenated model arrays, with its own grid;
+    // null: every shot cuts its window from the model slots above
+    const ShotAux *aux;
 };
 void launch_setup(const SetupArgs &a, int nshots, int max_nxpml, cudaStream_t st);
-void launch_record_gather(const float *rrow, const int *trow, int nt, int nrc, int X, int ntr, float *out,
-                          size_t cstride, cudaStream_t st);
+// tlen (may be null): samples of each trace; later samples are written as zeros
+void launch_record_gather(const float *rrow, const int *trow, const int *tlen, int nt, int nrc, int X, int ntr,
+                          float *out, size_t cstride, cudaStream_t st);
 void launch_recv_source(const float *res_z, const float *res_x, const int *rtr, int nt, int X, int rsp, float *rs,
                         cudaStream_t st);
 void launch_residual_l2(int stage, int nt, int ntr_tot, const float *syn_z, const float *syn_x, const float *syn2_z,
@@ -84,14 +89,43 @@ struct OtArgs {
     float *res_z, *res_x;
     const double *sigma;          // [ntr][2] (z, x)
     double *trace_misfit;         // [ntr][2]
+    double *scratch;              // traces longer than ot_max_nt(): ot_scratch_doubles(nt, ntr) doubles
 };
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st);
 size_t ot_smem_bytes(int nt);
+// longest trace held in shared memory; longer ones need the global scratch
 int ot_max_nt();
+size_t ot_scratch_doubles(int nt, int ntr);
 // OT scales of a batch on the device: max |obs| per (trace, component),
 // floored per shot (sigma: 2 doubles per trace; geo: the batch's shots)
 void launch_ot_scales(const float *obs_z, const float *obs_x, int nt, int ntr, const ShotGeo *geo, int nshots,
                       int all, double *sigma, cudaStream_t st);
+
+// sfwi_adjoint.cu: the exact adjoint of the Born modelling operator
+struct AdjArgs {
+    int X, P, PS, pml, nt, born_lo;
+    float dt, dtdx, dtdz, idx, idz;
+    const ShotGeo *geo;
+    const int *rowshot;  // [X]: the shot of each packed row
+    const float *ib, *lam, *mu, *dampx, *dampz;
+    // adjoint state (velocities, stresses and their x-parts) and the fields
+    // the transposed stencils gather, each [X][P]
+    float *avx, *avz, *amx, *amz, *atxx, *atzz, *atxz, *amxx, *amzz, *amxz;
+    float *gax, *gbz, *gcz, *gdx, *hax, *hbz, *hdx, *hcz;
+    double *dbp, *dbs;   // adjoints of 2 rho vp dVp and 2 rho vs dVs per window cell
+    const float *snap;   // background vx, vz after each step's velocity sweep, [2 it + comp][X][PS]
+    const float *dz, *dx;  // the data (records' adjoint), trace-major [ntr][nt]
+    const int *rstart, *rtr;  // per packed row: the traces recorded there, rtr[rstart[row] .. rstart[row+1])
+};
+void launch_adjoint_step(const AdjArgs &a, int it, cudaStream_t st);
+struct ImageArgs {
+    int allnx, allnz, P, pml, nshots;
+    const ShotGeo *geo;
+    const double *dbp, *dbs;
+    const float *vp, *vs, *rho;
+    double *img_vp, *img_vs;
+};
+void launch_born_image(const ImageArgs &a, cudaStream_t st);
 
 // sfwi_engine.cu: set the calling thread's sfwi_last_error() message; returns code
 int record_error(int code, const char *fmt, ...);

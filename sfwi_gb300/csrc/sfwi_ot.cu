@@ -148,16 +148,23 @@ __device__ __forceinline__ int first_above(const double *G, int n, double y, int
 // fly from the chunk's running sum, the quantile search continues from the
 // previous sample's quantile, and divisions by per-trace constants are
 // multiplications by their reciprocals.
-constexpr int OT_MAX_CHUNK = 32;  // samples per thread: nt <= 32 * OT_THREADS
+constexpr int OT_MAX_CHUNK = 32;  // samples per thread of the shared-memory form: nt <= 32 * OT_THREADS
 
+// LONG = false: the per-trace arrays in shared memory (traces up to
+// ot_max_nt() samples); LONG = true: in the caller's global scratch, five
+// arrays of nt doubles per (trace, component), for longer traces (the
+// transport residuals r then go to the fifth array instead of registers).
+template <bool LONG>
 __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
     extern __shared__ double ot_sm[];
     __shared__ double wsum[32];
     __shared__ double cs[OT_THREADS];
     const int n = a.nt;
     // G: CDF of the observed trace; g: its density; P: p(cal); Q: the terms
-    // r f dt / g, then the adjoint weights A
-    double *G = ot_sm, *g = G + n, *P = g + n, *Q = P + n;
+    // r f dt / g, then the adjoint weights A; R (long form): r
+    double *G = LONG ? a.scratch + (size_t)blockIdx.x * 5 * n : ot_sm;
+    double *g = G + n, *P = g + n, *Q = P + n;
+    double *R = LONG ? Q + n : nullptr;
     const int tr = blockIdx.x >> 1, comp = blockIdx.x & 1;
     const size_t o = (size_t)tr * n;
     const float *cal = (comp ? a.cal_x : a.cal_z) + o;
@@ -211,7 +218,7 @@ __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
 
     // transport T_k = G^-1(F_k) and the misfit terms
     double w = 0.0, sq = 0.0, Fk = offF;
-    double r_loc[OT_MAX_CHUNK];
+    double r_loc[LONG ? 1 : OT_MAX_CHUNK];
     int m = 0;
     for (int i = 0; i < k1 - k0; i++) {
         const int k = k0 + i;
@@ -224,7 +231,10 @@ __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
         const double T = a.dt * (m + (Fk - Gm1) * inv_gm);
         const double r = (k + 1) * a.dt - T;
         w += r * r * fk;
-        r_loc[i] = r;
+        if (LONG)
+            R[k] = r;
+        else
+            r_loc[i] = r;
         const double q = r * fk * a.dt * inv_gm;
         Q[k] = q;
         sq += q;
@@ -236,7 +246,8 @@ __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
     for (int i = k1 - k0 - 1; i >= 0; i--) {
         const int k = k0 + i;
         run += Q[k];
-        const double A = r_loc[i] * r_loc[i] - 2.0 * run;
+        const double rk = LONG ? R[k] : r_loc[i];
+        const double A = rk * rk - 2.0 * run;
         Q[k] = A;
         fa += P[k] * inv_Sf * A;
     }
@@ -258,11 +269,18 @@ int ot_max_nt() {
     return by_smem < OT_MAX_CHUNK * OT_THREADS ? by_smem : OT_MAX_CHUNK * OT_THREADS;
 }
 
+size_t ot_scratch_doubles(int nt, int ntr) { return nt > ot_max_nt() ? (size_t)5 * nt * 2 * ntr : 0; }
+
 cudaError_t launch_ot(const OtArgs &a, cudaStream_t st) {
+    if (a.nt > ot_max_nt()) {
+        if (!a.scratch) return cudaErrorInvalidValue;
+        k_ot<true><<<2 * a.ntr, OT_THREADS, 0, st>>>(a);
+        return cudaGetLastError();
+    }
     const size_t sm = ot_smem_bytes(a.nt);
-    cudaError_t e = cudaFuncSetAttribute(k_ot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_ot<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k_ot<<<2 * a.ntr, OT_THREADS, sm, st>>>(a);
+    k_ot<false><<<2 * a.ntr, OT_THREADS, sm, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -92,8 +92,11 @@ def test_gpu_ot_entry_points_match_oracle(kind):
     import sfwi_gb300 as sg
     fn = {1: sg.OT, 2: sg.OT_power, 3: sg.OT_alltrace}[kind]
     # lengths: short, the 3000-sample gathers, one sample a thread past a
-    # block (257), the 6000-sample snapshot workload and the longest taken
-    for seed, ntr, nt in ((1, 5, 300), (2, 96, 3000), (3, 1, 7), (4, 3, 257), (5, 4, 6000), (6, 2, 7160)):
+    # block (257), the 6000-sample snapshot workload, the longest a trace
+    # held in shared memory (7160), and longer traces worked in global
+    # scratch (7161; 12000 = 6 s at 0.5 ms)
+    for seed, ntr, nt in ((1, 5, 300), (2, 96, 3000), (3, 1, 7), (4, 3, 257), (5, 4, 6000), (6, 2, 7160),
+                          (7, 2, 7161), (8, 3, 12000)):
         obs_x, obs_z, cal_x, cal_z = _gather(seed, ntr, nt, shift=min(6, nt // 2))
         m_ref, rx_ref, rz_ref = po.ot_gather(kind, 1e-3, obs_x, obs_z, cal_x, cal_z)
         rx, rz, m = fn(obs_x, obs_z, cal_x, cal_z, 1e-3)

@@ -30,7 +30,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # one process per GPU under torchrun: pin this process's device before any CUDA use
-if "LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+# (SFWI_SHARE_GPU=1 keeps every rank on the first device: a check of the
+# multi-rank path on a one-GPU machine, whose ranks never wait on each other)
+if ("LOCAL_RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1
+        and os.environ.get("SFWI_SHARE_GPU") != "1"):
     os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
 
 import numpy as np  # noqa: E402
@@ -371,20 +374,31 @@ def observed_records(sg, w, data):
     return obs
 
 
-def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, clocks=None, snap_check=0):
+def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, rank=0, clocks=None, snap_check=0):
     """One workload: `warmup` untimed passes (the autotuner after the first),
     then `steps` timed passes through sfwi_run (device time from CUDA events
     inside the engine; wall clock around the whole public call for e2e), the
     per-kernel launch times, and the plain one-shot-at-a-time form on an
-    evenly spread sample of `plain_shots` shots.  Returns a dict."""
+    evenly spread sample of `plain_shots` shots.  With N ranks the survey's
+    shots are taken N times over and split by cost (sfwi_gb300.shard), each
+    rank runs its share and the FP64 gradients and misfit are summed over
+    the ranks inside every timed step (weak scaling).  Returns a dict."""
     import sfwi_gb300 as sg
+    from sfwi_gb300 import shard
     data = build_workload(w)
     stage = w.get("stage", 2)
     nt, pml = w["nt"], w["pml"]
     nxpml, nzpml = w["allnx"] + 2 * pml, w["allnz"] + 2 * pml
-    shots = data["shots"]
+    base = data["shots"]
     isz, igz = pml + w["sy"], pml + w["gy"]
     obs = observed_records(sg, w, data)
+    # this rank's shots, as indices into the survey's (all of them on one rank)
+    mine = list(range(len(base)))
+    if pg is not None and ws > 1:
+        every = [i for _ in range(ws) for i in range(len(base))]
+        part = shard.partition([shard.shot_cost(base[i], pml, nzpml, nt) for i in every], ws)[rank]
+        mine = [every[k] for k in part]
+    shots = [base[i] for i in mine]
     kbytes = dict(KERNEL_BYTES)
     fd = sg.FD2DGPU_ELASTIC(data["sou"], w["dx"], w["dx"], w["dt"], nxpml, nzpml, w["allnx"], w["allnz"], 1, pml, nt,
                             4, shots[0]["ntr"], stage=stage)
@@ -404,13 +418,26 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, clocks=None, sna
         kbytes["k_bwd_v"] += 8  # the density kernel's accumulator, read and written
 
     def enqueue(d, i):
-        fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[i][0].array,
-                        obs[i][1].array)
+        b = mine[i]  # the survey shot whose observed records these are
+        fd.enqueue_shot(d["nx"], d["isx"], isz, igz, d["ngx_left"], d["delta_left"], 0, d["gc"], obs[b][0].array,
+                        obs[b][1].array)
+
+    allreduce_s = []
 
     def step():
         for i, d in enumerate(shots):
             enqueue(d, i)
         m, _ = fd.run()
+        if pg is not None:
+            # the reference's gradient reduction (sfwi-stage1/main.cpp:637-666)
+            g64 = list(fd.read_gradients_f64())
+            if w.get("rho_grad"):
+                g64.append(fd.read_density_gradient_f64())
+            t = time.perf_counter()
+            m = shard.allreduce_gradients(g64, m)
+            allreduce_s.append(time.perf_counter() - t)
+            fd.imagebuffer_resettozero()
+            return m, g64
         grho = fd.read_density_gradient_f64() if w.get("rho_grad") else None
         g = fd.imagebuffer_resettozero()
         return m, (g, grho)
@@ -441,6 +468,7 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, clocks=None, sna
         clocks.start()
     launches0 = fd.kernel_launches()
     dev_ms, fwd_ms, bwd_ms, mis_ms = [], [], [], []
+    del allreduce_s[:]
     wall0 = time.perf_counter()
     for _ in range(steps):
         m, g = step()
@@ -531,6 +559,7 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, clocks=None, sna
             snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
                              for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
     out.update(value=value, e2e=e2e, wall=wall, total_dev_s=total_dev_s, steps=steps, launches=launches, clk=clk,
+               allreduce_ms=round(1000.0 * float(np.mean(allreduce_s)), 3) if allreduce_s else None,
                h2d=h2d, d2h=d2h, kt=kt, roof=roof, fracs=fracs, cells=cells, alg_bytes_step=alg_bytes_step,
                kernel_bytes=kernel_bytes, plain=plain, snap_err=snap_err, tile=fd.tile_shape(),
                phase_ms={"forward": round(float(np.mean(fwd_ms)), 2), "backward": round(float(np.mean(bwd_ms)), 2),
@@ -604,8 +633,8 @@ def main():
         dist.init_process_group(backend="gloo", init_method="env://")
         pg = dist
 
-    r = measure(w, args, args.steps, args.warmup, args.plain_shots, pg=pg, ws=ws, clocks=Clocks(),
-                snap_check=args.snap_check)
+    r = measure(w, args, args.steps, args.warmup, args.plain_shots if ws == 1 else 0, pg=pg, ws=ws, rank=rank,
+                clocks=Clocks(), snap_check=args.snap_check)
     if args.profile_kernels:
         close_workload(r)
         return 0
@@ -646,7 +675,9 @@ def main():
                        "gradients": "vp, vs, rho" if w.get("rho_grad") else "vp, vs",
                        "tile": r["tile"], "autotune": r["tune"],
                        "imaging": ("%s snapshots every %d steps" % (w["snap"][1], w["snap"][0]) if w.get("snap")
-                                   else "reconstruction with saved edge strips"), "parallelism": "shots-per-gpu",
+                                   else "reconstruction with saved edge strips"),
+                       "parallelism": ("shots split by cost over %d ranks, FP64 gradient all-reduce in every step"
+                                       % ws if ws > 1 else "shots-per-gpu"),
                        "l2": l2_note(r["cells"], nt, len(shots), w),
                        "alg_bytes_per_step_GB": round(r["alg_bytes_step"] / 1e9, 2),
                        "alg_GBps_whole_step": round(r["alg_bytes_step"] / (total_dev_s / steps) / 1e9, 1),
@@ -657,7 +688,8 @@ def main():
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"], "roofline": r["roof"], "cpu_baseline": cpu, "clocks": r["clk"],
             "plain": r["plain"], "serving": serving, "snapshot_error": r["snap_err"], "reference_gpu": ref_gpu,
-            "workloads": extras or None, "phase_ms": r["phase_ms"]}
+            "workloads": extras or None, "phase_ms": r["phase_ms"],
+            "allreduce_ms": r["allreduce_ms"]}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -4,17 +4,25 @@ GPU, admitted against a fixed HBM budget while others are running.
 A request is one model (vp, vs, rho on its own allnx x allnz grid) with 1..8
 shots and their observed records; its result is the misfit and the FP64
 Vp/Vs gradients and illumination.  Requests arrive over time.  The server
-admits an arrived request as soon as a slot is free and its device memory
-fits in what the running requests leave of the budget (oldest first; a
-younger request that fits may pass an older one that does not yet fit).
-Each admitted request runs on its own engine, whose kernels, graphs and
-stream-ordered allocations live on its own CUDA stream, so the work of
-concurrent requests overlaps on the device.  `Server(max_active=1)` is the
-plain one-job-at-a-time FIFO loop.
+admits arrived requests as soon as a slot is free and their device memory
+fits in what the running work leaves of the budget (oldest first; a younger
+request that fits may pass an older one that does not yet fit).
 
-Results do not depend on what else is running: every request's engine is
-independent and its kernels are deterministic, so a request gives the same
-numbers alone and in the mix (tests/test_serve.py).
+Two ways to run what is admitted:
+  - batched (Server(batch=True)): every request admitted at once joins ONE
+    run of the engine, sfwi_run_models: all their shots, on their own models,
+    grids and numbers of time steps, advance in the same kernel launches, so
+    small requests fill the tile queue of large ones instead of running
+    launch-bound on their own.  Up to max_active such runs overlap on the
+    device, each on its own engine and stream, and requests that arrive
+    while runs are in flight form the next run as soon as a slot frees up;
+  - one engine per request (the default), each on its own stream.
+`Server(max_active=1)` without batching is the plain one-job-at-a-time FIFO.
+
+Results do not depend on what else is running: every shot's arithmetic is
+independent of the other shots of its run and the kernels are
+deterministic, so a request gives the same numbers, bit for bit, alone and
+in the mix, batched or not (tests/test_serve.py, tests/test_model_batches.py).
 """
 import dataclasses
 import threading
@@ -80,6 +88,63 @@ def request_bytes(req):
     return 4 * floats + 8 * 4 * req.allnx * req.allnz + (1 << 20)
 
 
+def batch_bytes(reqs):
+    """Device memory of one shared run of several requests: the packed grid
+    at the deepest request's depth, strips and records for the longest
+    request's nt, the models and their FP64 gradients."""
+    pml = reqs[0].pml
+    P = (max(r.allnz for r in reqs) + 2 * pml + 3) // 4 * 4
+    X = sum(int(d["nx"]) + 2 * pml for r in reqs for d in r.shots)
+    ntr = sum(len(d["gc"]) for r in reqs for d in r.shots)
+    nt = max(r.nt for r in reqs)
+    ns = sum(len(r.shots) for r in reqs)
+    cells = sum(r.allnx * r.allnz for r in reqs)
+    floats = (NGRID * X * P + nt * 4 * X * 8 + nt * 4 * ns * 8 * P + nt * 2 * X + X * ((2 * nt + 3) // 4 * 4)
+              + NREC * ntr * nt + 5 * cells + nt)
+    return 4 * floats + 8 * 4 * cells + (1 << 20)
+
+
+def run_requests(reqs):
+    """Several requests in one run of one engine (sfwi_run_models): a list of
+    (misfit, grad_pp, grad_ps, illum), one per request."""
+    import sfwi_gb300 as sg
+    pml, dx, dt = reqs[0].pml, reqs[0].dx, reqs[0].dt
+    for r in reqs:
+        if (r.pml, r.dx, r.dt) != (pml, dx, dt) or r.misfit_kind != reqs[0].misfit_kind:
+            raise ValueError("requests of one run share spacing, dt, PML width and misfit")
+    nt = max(r.nt for r in reqs)
+    longest = max(reqs, key=lambda r: r.nt)
+    for r in reqs:  # every request's wavelet is the start of the run's
+        if not np.array_equal(np.asarray(r.sou, np.float32), np.asarray(longest.sou, np.float32)[:r.nt]):
+            raise ValueError("request %d: its wavelet is not the start of the run's" % r.rid)
+    allnx = max(r.allnx for r in reqs)
+    allnz = max(r.allnz for r in reqs)
+    maxnx = max(int(d["nx"]) for r in reqs for d in r.shots)
+    fd = sg.FD2DGPU_ELASTIC(longest.sou, dx, dx, dt, maxnx + 2 * pml, allnz + 2 * pml, allnx, allnz, 1, pml, nt, 4,
+                            0, stage=1)
+    try:
+        if reqs[0].misfit_kind:
+            fd.set_misfit(reqs[0].misfit_kind)
+        shot_model = []
+        for k, r in enumerate(reqs):
+            for d in r.shots:
+                fd.enqueue_shot(d["nx"], d["isx"], d["isz"], d["igz"], d["ngx_left"], d["delta_left"], 0, d["gc"],
+                                d["obs_z"], d["obs_x"], nt=r.nt)
+                shot_model.append(k)
+        models = [dict(vp=r.vp, vs=r.vs, rho=r.rho, nt=r.nt) for r in reqs]
+        per, grads = fd.run_models(models, shot_model)
+    finally:
+        fd.close()
+    out, i = [], 0
+    for r, g in zip(reqs, grads):
+        m = 0.0
+        for _ in r.shots:  # the request's shots in its own order, as a run of it alone sums them
+            m += float(per[i])
+            i += 1
+        out.append((m,) + tuple(g[:3]))
+    return out
+
+
 def request_work(req):
     """Cell-steps of one request (its shots' padded cells times nt): the
     order of the shortest-first policy."""
@@ -115,21 +180,26 @@ class Server:
     loop is the plain FIFO."""
 
     def __init__(self, budget_bytes, max_active=4, runner=run_request, sizer=request_bytes, clock=time.perf_counter,
-                 policy="oldest", work=request_work):
+                 policy="oldest", work=request_work, batch=False, batch_runner=run_requests, batch_sizer=batch_bytes,
+                 max_batch=64):
         if policy not in ("oldest", "shortest"):
             raise ValueError("policy must be 'oldest' or 'shortest'")
         self.budget = int(budget_bytes)
         self.max_active = int(max_active)
         self.runner, self.sizer, self.clock = runner, sizer, clock
         self.policy, self.work = policy, work
+        # batched: the requests admitted together share one run (batch_runner)
+        self.batch, self.batch_runner, self.batch_sizer = batch, batch_runner, batch_sizer
+        self.max_batch = int(max_batch)
 
     def run(self, requests):
         """Replay `requests` (arrival offsets in seconds) against the wall
         clock and serve them; returns the results in request-id order."""
         reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
         for r in reqs:
-            if self.sizer(r) > self.budget:
-                raise ValueError("request %d needs %d bytes, more than the whole budget" % (r.rid, self.sizer(r)))
+            need = self.batch_sizer([r]) if self.batch else self.sizer(r)
+            if need > self.budget:
+                raise ValueError("request %d needs %d bytes, more than the whole budget" % (r.rid, need))
         cv = threading.Condition()
         waiting, results, errors = [], {}, []
         state = {"used": 0, "active": 0}
@@ -138,12 +208,13 @@ class Server:
         def now():
             return self.clock() - t0
 
-        def worker(r, size, admitted):
+        def worker(group, size, admitted):
             try:
-                out = self.runner(r)
+                outs = self.batch_runner(group) if self.batch else [self.runner(group[0])]
                 done = now()
                 with cv:
-                    results[r.rid] = Result(r.rid, out[0], out[1], out[2], out[3], r.arrival, admitted, done)
+                    for r, out in zip(group, outs):
+                        results[r.rid] = Result(r.rid, out[0], out[1], out[2], out[3], r.arrival, admitted, done)
             except BaseException as e:  # surfaced to the caller after the loop
                 with cv:
                     errors.append(e)
@@ -162,6 +233,26 @@ class Server:
                     nxt += 1
                 # admit every arrived request that fits, oldest or least work first
                 order = list(waiting) if self.policy == "oldest" else sorted(waiting, key=lambda q: (self.work(q), q.rid))
+                if self.batch:
+                    # one shared run of every waiting request that fits the budget
+                    if state["active"] < self.max_active and order:
+                        group, size = [], 0
+                        for r in order:
+                            if len(group) >= self.max_batch:
+                                break
+                            trial = self.batch_sizer(group + [r])
+                            if state["used"] + trial <= self.budget:
+                                group.append(r)
+                                size = trial
+                        if group:
+                            for r in group:
+                                waiting.remove(r)
+                            state["used"] += size
+                            state["active"] += 1
+                            th = threading.Thread(target=worker, args=(group, size, now()), daemon=True)
+                            th.start()
+                            threads.append(th)
+                    order = []
                 for r in order:
                     if state["active"] >= self.max_active:
                         break
@@ -170,7 +261,7 @@ class Server:
                         waiting.remove(r)
                         state["used"] += size
                         state["active"] += 1
-                        th = threading.Thread(target=worker, args=(r, size, now()), daemon=True)
+                        th = threading.Thread(target=worker, args=([r], size, now()), daemon=True)
                         th.start()
                         threads.append(th)
                     elif self.max_active == 1:

@@ -92,6 +92,70 @@ def test_request_bytes_grows_with_the_request():
     assert serve.request_bytes(b) > serve.request_bytes(a) > 0
 
 
+class BatchRecorder:
+    """Batch runner that sleeps and records the groups it was given."""
+
+    def __init__(self, dur=0.05):
+        self.lock = threading.Lock()
+        self.groups, self.active, self.max_active = [], 0, 0
+        self.dur = dur
+
+    def __call__(self, group):
+        with self.lock:
+            self.active += 1
+            self.max_active = max(self.max_active, self.active)
+            self.groups.append([r.rid for r in group])
+        time.sleep(self.dur)
+        with self.lock:
+            self.active -= 1
+        z = np.zeros((1, 1))
+        return [(float(r.rid), z, z, z) for r in group]
+
+
+def test_batched_admission_groups_the_waiting_requests():
+    # two arrive at once and share the first run; the next three arrive while
+    # it runs (one slot) and share the second, within the budget of 60
+    reqs = _fake_requests([20, 20, 20, 20, 20, 30], [0.0, 0.0, 0.01, 0.01, 0.02, 0.02])
+    rec = BatchRecorder(0.05)
+    srv = serve.Server(60, max_active=1, batch=True, batch_runner=rec,
+                       batch_sizer=lambda g: sum(r.size for r in g))
+    res = srv.run(reqs)
+    assert [r.rid for r in res] == list(range(6))
+    assert rec.groups[0] == [0, 1]
+    assert rec.groups[1] == [2, 3, 4]  # 20+20+20 fit; request 5 (30) waits for the next run
+    assert rec.groups[2] == [5]
+    assert rec.max_active == 1
+    # results of a run complete together
+    assert res[2].done == res[3].done == res[4].done
+    # at most max_batch requests per run
+    rec2 = BatchRecorder(0.02)
+    serve.Server(1000, max_active=1, batch=True, batch_runner=rec2, batch_sizer=lambda g: len(g),
+                 max_batch=2).run(_fake_requests([1] * 5, [0.0] * 5))
+    assert [len(g) for g in rec2.groups] == [2, 2, 1]
+
+
+def test_batch_bytes_covers_its_requests():
+    a, b = serve.poisson_requests(2, 10.0, grid=((60, 30), (90, 50)), nt=(100, 140), shots=(1, 2))
+    both = serve.batch_bytes([a, b])
+    assert both >= max(serve.batch_bytes([a]), serve.batch_bytes([b]))
+    assert serve.batch_bytes([a]) >= serve.request_bytes(a) * 0.9
+
+
+@pytest.mark.gpu
+def test_batched_serving_gives_each_request_its_result_alone():
+    """The shared-run path: requests of different grids and lengths served in
+    shared runs equal each request run alone on its own engine, bit for bit."""
+    reqs = serve.poisson_requests(5, 1000.0, seed=9, grid=((64, 32), (110, 48)), nt=(180, 260), shots=(1, 3))
+    assert len({r.nt for r in reqs}) > 1 and len({(r.allnx, r.allnz) for r in reqs}) > 1
+    alone = [serve.run_request(r) for r in reqs]
+    mixed = serve.run_requests(reqs)
+    res = serve.Server(8 << 30, max_active=2, batch=True).run(reqs)
+    for a, m, r in zip(alone, mixed, res):
+        assert a[0] == m[0] == r.misfit
+        for x, y, z in zip(a[1:], m[1:], (r.grad_pp, r.grad_ps, r.illum)):
+            assert np.array_equal(x, y) and np.array_equal(x, z)
+
+
 @pytest.mark.gpu
 def test_request_gives_the_same_result_alone_and_in_the_mix():
     reqs = serve.poisson_requests(4, 1000.0, seed=7, grid=((64, 32), (110, 48)), nt=(180, 260), shots=(1, 3))

@@ -157,11 +157,3 @@ def test_gpu_ot_trace_without_signal_matches_oracle(kind):
     assert np.linalg.norm(rz - rz_ref) <= TOL * np.linalg.norm(rz_ref)
     assert np.linalg.norm(rx - rx_ref) <= TOL * np.linalg.norm(rx_ref)
     assert abs(m - m_ref) <= TOL * abs(m_ref)
-
-
-@pytest.mark.gpu
-def test_gpu_ot_refuses_traces_longer_than_its_shared_memory():
-    import sfwi_gb300 as sg
-    obs_x, obs_z, cal_x, cal_z = _gather(7, 1, 7161)
-    with pytest.raises(sg.SfwiError):
-        sg.OT(obs_x, obs_z, cal_x, cal_z, 1e-3)

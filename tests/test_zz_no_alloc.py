@@ -111,3 +111,16 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     rc = lib.sfwi_ot_noalloc(1, p, p, p, p, p, p, 100, 8193, 1e-3, C.byref(m), None)
     assert rc == -1
     assert b"8192" in lib.sfwi_last_error()
+
+
+def test_noalloc_rejects_traces_longer_than_its_shared_memory():
+    """The fixed scratch holds per-trace sums only: a trace is worked in
+    shared memory, so the allocation-free form keeps the 7160-sample limit
+    (the allocating entry points take longer traces in global scratch)."""
+    from sfwi_gb300 import _lib
+    lib = _lib.load()
+    m = C.c_double(0.0)
+    p = C.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = lib.sfwi_ot_noalloc(1, p, p, p, p, p, p, 7161, 4, 1e-3, C.byref(m), None)
+    assert rc == -1
+    assert b"7160" in lib.sfwi_last_error()

@@ -23,9 +23,9 @@
  *     (sfwi-stage2/FD2DGPU.cuh:297).  Any other call made first selects
  *     stage 1.
  *   - rbc (random boundary, cuRAND) is not provided: rbc = true throws.
- *     cpu_mem / ntt (edge strips offloaded to the host in ntt-step chunks)
- *     are accepted and change nothing: the strips stay in device memory,
- *     which gives the same values.
+ *     cpu_mem / ntt keep the edge strips in pinned host memory with a device
+ *     ring of two ntt-step chunks (sfwi_set_cpu_mem), with the same values
+ *     as strips kept on the device.
  *   - OT, OT_power and OT_alltrace are only declared in the reference
  *     (sfwi-stage1/FD2DGPU.cuh:23-25).  Here they are defined; the misfit
  *     depends on the sample interval, which their arguments do not carry, so
@@ -171,16 +171,18 @@ inline void no_random_boundary(bool rbc, const char *call) {
 // shot described by the object's fields and its last record_copytoGPU.
 // misfit += the shot's misfit; the gradients and the illumination accumulate
 // on the device until imagebuffer_resettozero.  sxnum, nDim, myid, iter,
+// cpu_mem and ntt keep the edge strips in host memory (sfwi_set_cpu_mem);
 // iter_round1, maxiter, snapdir, image_pp/ps, the old gradients and
 // misfit_ot take no part in the reference's live path and are not read.
 inline void IMAGE_SINGLESHOT(FD2DGPU_ELASTIC &fdtdgpu, const int sxnum, const int nDim, const int myid, float *record,
                              float *record_x, int *gc, bool rbc, bool cpu_mem, int ntt, int iter, int iter_round1,
                              int maxiter, char *snapdir, float *image_pp, float *image_ps, float *cpu_pp_grad_old,
                              float *cpu_ps_grad_old, double &misfit, float *misfit_ot) {
-    (void)sxnum, (void)nDim, (void)myid, (void)record, (void)record_x, (void)gc, (void)cpu_mem, (void)ntt, (void)iter;
+    (void)sxnum, (void)nDim, (void)myid, (void)record, (void)record_x, (void)gc, (void)iter;
     (void)iter_round1, (void)maxiter, (void)snapdir, (void)image_pp, (void)image_ps, (void)cpu_pp_grad_old;
     (void)cpu_ps_grad_old, (void)misfit_ot;
     sfwi_compat::no_random_boundary(rbc, "IMAGE_SINGLESHOT");
+    sfwi_compat::check(sfwi_set_cpu_mem(fdtdgpu.handle(), cpu_mem ? 1 : 0, ntt), "IMAGE_SINGLESHOT");
     fdtdgpu.push_geometry();
     sfwi_compat::check(sfwi_image_singleshot(fdtdgpu.handle(), &misfit), "IMAGE_SINGLESHOT");
 }
@@ -191,9 +193,10 @@ inline void IMAGE_SINGLESHOT(FD2DGPU_ELASTIC &fdtdgpu, const int sxnum, const in
                              float *record_x, int *gc, bool rbc, bool cpu_mem, int ntt, int iter, char *snapdir,
                              float *image_pp, float *image_ps, float *cpu_pp_grad_old, float *cpu_ps_grad_old,
                              double &misfit3) {
-    (void)sxnum, (void)nDim, (void)myid, (void)record, (void)record_x, (void)gc, (void)cpu_mem, (void)ntt, (void)iter;
+    (void)sxnum, (void)nDim, (void)myid, (void)record, (void)record_x, (void)gc, (void)iter;
     (void)snapdir, (void)image_pp, (void)image_ps, (void)cpu_pp_grad_old, (void)cpu_ps_grad_old;
     sfwi_compat::no_random_boundary(rbc, "IMAGE_SINGLESHOT");
+    sfwi_compat::check(sfwi_set_cpu_mem(fdtdgpu.handle(), cpu_mem ? 1 : 0, ntt), "IMAGE_SINGLESHOT");
     fdtdgpu.push_geometry();
     sfwi_compat::check(sfwi_image_singleshot(fdtdgpu.handle(), &misfit3), "IMAGE_SINGLESHOT");
 }

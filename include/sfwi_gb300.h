@@ -114,6 +114,20 @@ int sfwi_set_density_gradient(sfwi_handle *h, int on);
 #define SFWI_SNAP_F16 2
 #define SFWI_SNAP_BF16 3
 int sfwi_set_snapshots(sfwi_handle *h, int every, int format);
+
+/* Edge strips in host memory: IMAGE_SINGLESHOT's cpu_mem and ntt
+ * (sfwi-stage1/FD2DGPU.cuh:466-467; the buffers of FD2DGPU.cu:4382-4421 and
+ * the copies of :4548-4561, :4600-4622).  With cpu_mem set, later gradient
+ * runs keep on the device a ring of two chunks of ntt steps of strips instead
+ * of all nt steps; every full chunk but the last two goes to pinned host
+ * memory during the forward sweeps and comes back during the backward
+ * sweeps, copied on a second stream while the step kernels run, so the
+ * results are the same bits as with the strips on the device.  When 2 ntt >= nt
+ * the ring would hold every step and the strips stay on the device.
+ * cpu_mem = 0 restores device strips; cpu_mem != 0 needs ntt >= 1. */
+int sfwi_set_cpu_mem(sfwi_handle *h, int cpu_mem, int ntt);
+/* strip bytes of the last run: on the device, and in pinned host memory */
+int sfwi_strip_bytes(sfwi_handle *h, size_t *device_bytes, size_t *host_bytes);
 int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho);
 
 /* Records of the last shot-gradient call(s): forward records (stage 1:

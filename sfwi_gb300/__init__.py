@@ -152,6 +152,18 @@ class FD2DGPU_ELASTIC:
         _lib.check(_lib.load().sfwi_set_snapshots(self._h, int(every), code))
         self._snap = (int(every), fmt) if every else None
 
+    def set_cpu_mem(self, cpu_mem, ntt=0):
+        """Keep the edge strips of later gradient runs in pinned host memory,
+        with a device ring of two chunks of `ntt` steps (IMAGE_SINGLESHOT's
+        cpu_mem and ntt); the results are the same bits."""
+        _lib.check(_lib.load().sfwi_set_cpu_mem(self._h, 1 if cpu_mem else 0, int(ntt)))
+
+    def strip_bytes(self):
+        """(device bytes, pinned host bytes) of the last run's edge strips"""
+        dev, host = C.c_size_t(0), C.c_size_t(0)
+        _lib.check(_lib.load().sfwi_strip_bytes(self._h, C.byref(dev), C.byref(host)))
+        return dev.value, host.value
+
     def read_density_gradient_f64(self):
         out = np.zeros((self.allnx, self.allnz), np.float64)
         _lib.check(_lib.load().sfwi_read_density_gradient_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
@@ -361,10 +373,15 @@ class FD2DGPU_ELASTIC:
 
 def IMAGE_SINGLESHOT(fdtdgpu, misfit=0.0, *reference_args):
     """IMAGE_SINGLESHOT(fd, misfit) -> misfit + this shot's misfit
-    (sfwi-stage1/FD2DGPU.cuh:466-467).  The reference's remaining arguments
-    (sxnum, nDim, myid, record, record_x, gc, rbc, cpu_mem, ntt, iter, ...)
-    select MPI bookkeeping, host offload and disabled options and are
-    accepted and ignored."""
+    (sfwi-stage1/FD2DGPU.cuh:466-467).  Of the reference's remaining
+    arguments (sxnum, nDim, myid, record, record_x, gc, rbc, cpu_mem, ntt,
+    iter, ...), cpu_mem and ntt keep the edge strips in host memory
+    (set_cpu_mem) and rbc = True (random boundary) is refused; the others
+    are MPI bookkeeping or disabled options and are not read."""
+    if len(reference_args) >= 7 and reference_args[6]:
+        raise SfwiError("IMAGE_SINGLESHOT: the random boundary (rbc) is not provided")
+    if len(reference_args) >= 9:
+        fdtdgpu.set_cpu_mem(reference_args[7], reference_args[8])
     return misfit + fdtdgpu.image_singleshot()
 
 

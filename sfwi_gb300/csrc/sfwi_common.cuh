@@ -136,6 +136,8 @@ struct Params {
     const TileRec *tiles;
     const float *sou;           // [nt]
     float *tb, *lr;             // edge strips (layout below); null in modelling-only runs
+    int strip_steps;            // steps the strip arrays hold: nt, or the device ring of a run whose
+                                // strips are kept in host memory (step it is at it % strip_steps)
     float *rrow;                // receiver-row records [nt][nrc][X]
     int nrc;                    // record components: vz, vx (+ background vz, vx in stage 2)
     // forward snapshots (snap_every = k > 0, no reconstruction): the

@@ -83,6 +83,33 @@ struct DevBuf {
     }
 };
 
+// Pinned host buffer that grows on demand (edge strips kept in host memory).
+// Growing it frees the old block with cudaFreeHost, which waits for the
+// device; it only grows while no run is in flight.
+template <class T>
+struct HostBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t m) {
+        if (m <= n && p) return cudaSuccess;
+        release();
+        cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&p), std::max<size_t>(m, 1) * sizeof(T),
+                                      cudaHostAllocDefault);
+        if (e == cudaSuccess) {
+            n = m;
+        } else {
+            p = nullptr;
+            cudaGetLastError();
+        }
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
 struct ShotIn {
     int nx, win0, isx, isz, igz, ngx_left, ntr;
     int model = 0;  // model slot (line searches)
@@ -111,6 +138,11 @@ struct Batch {
     // device
     DevBuf<float> grid;      // NGRID * X * P
     DevBuf<float> tb, lr;    // edge strips (sfwi_common.cuh layout)
+    // steps the strip arrays hold (nt, or a ring of two chunks when the
+    // strips live in host memory), the chunk length and count of that ring
+    // (0 when the strips stay on the device), and the strip bytes of the run
+    int strip_steps = 0, strip_chunk = 0, strip_chunks = 0;
+    size_t strip_dev_bytes = 0, strip_host_bytes = 0;
     DevBuf<float> rrow;      // receiver-row records [nt][nrc][X]
     DevBuf<float> rsrc;      // residual source [X][rsp]
     DevBuf<float> snap;      // forward snapshots (FP32 or 16-bit elements)
@@ -182,6 +214,16 @@ struct sfwi_handle {
     // these slot arrays instead of the uploaded model
     const float *slot_vp = nullptr, *slot_vs = nullptr, *slot_dvp = nullptr, *slot_dvs = nullptr;
     bool force_l2 = false;  // the exact step length is defined on the L2 residual
+    // edge strips kept in host memory (the reference's cpu_mem and ntt,
+    // sfwi-stage1/FD2DGPU.cu:4382-4421, :4548-4561, :4600-4622): the device
+    // holds a ring of two chunks of ntt steps; every full chunk but the last
+    // two moves to pinned host memory during the forward sweeps and comes
+    // back during the backward sweeps, copied on a second stream while the
+    // step kernels run
+    int cpu_mem = 0, ntt = 0;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_copy[2] = {nullptr, nullptr};
+    HostBuf<float> htb, hlr;
     DevBuf<float> ls_buf;   // trial models and search directions
     // a batch over several models (sfwi_run_models): each model's grid, time
     // steps and offset in the concatenated model and gradient arrays; empty
@@ -468,7 +510,6 @@ int upload_tiles(sfwi_handle *h) {
 int encode_tile_maps(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     const int tx = h->tv->tx, tz = h->tv->tz, bx = tx + 2 * h->tv->halo, bz = tz + 2 * h->tv->halo;
-    const int nt = h->nt;
     for (int d = 0; d < 3; d++) {
         if (int rc = encode_grid_map(&b.tm.box[d], b.grid.p, b.P, b.X, bz, bx, d + 1)) return rc;
         if (int rc = encode_grid_map(&b.tm.core[d], b.grid.p, b.P, b.X, tz, tx, d + 1)) return rc;
@@ -479,9 +520,9 @@ int encode_tile_maps(sfwi_handle *h, bool forward_only) {
         if (int rc = encode_snap_map(&b.tm.snap, b.snap.p, h->snap_fmt, b.PS, b.X, 2 * b.nsnap, bx, bz)) return rc;
     } else {
         // strips: boxes of (BX rows x 8) and (8 rows x BZ)
-        if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, (unsigned long long)nt * 4 * b.X, 8, bx)) return rc;
-        if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, (unsigned long long)nt * 4 * b.nshots * 8, bz, 8))
-            return rc;
+        const unsigned long long ns = b.strip_steps;
+        if (int rc = encode_2d_map(&b.tm.tb, b.tb.p, 8, ns * 4 * b.X, 8, bx)) return rc;
+        if (int rc = encode_2d_map(&b.tm.lr, b.lr.p, b.P, ns * 4 * b.nshots * 8, bz, 8)) return rc;
     }
     // residual source: BX rows x 4
     return encode_2d_map(&b.tm.rs, b.rsrc.p, b.rsp, b.X, 4, bx);
@@ -610,6 +651,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     p.sou = h->sou.p;
     const bool snap = !forward_only && h->snap_every > 0;
     p.tb = forward_only || snap ? nullptr : b.tb.p;  // modelling only / snapshots: no strips
+    p.strip_steps = b.strip_steps > 0 ? b.strip_steps : std::max(h->nt, 1);
     p.lr = forward_only || snap ? nullptr : b.lr.p;
     p.snap = snap ? b.snap.p : nullptr;
     p.sscale = snap ? b.sscale.p : nullptr;
@@ -634,11 +676,20 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     const bool snap = !forward_only && h->snap_every > 0;
     b.PS = (b.P + 7) & ~7;
     b.nsnap = snap ? (nt + h->snap_every - 1) / h->snap_every : 0;
+    const bool strips = !forward_only && !snap;
+    const bool offload = strips && h->cpu_mem && 2 * h->ntt < nt;
+    b.strip_chunk = offload ? h->ntt : 0;
+    b.strip_chunks = offload ? (nt + h->ntt - 1) / h->ntt : 0;
+    b.strip_steps = offload ? 2 * h->ntt : nt;
+    // floats of one step of each strip array
+    const size_t tb_step = (size_t)4 * b.X * 8, lr_step = (size_t)4 * b.nshots * 8 * b.P;
+    b.strip_dev_bytes = strips ? (size_t)b.strip_steps * (tb_step + lr_step) * sizeof(float) : 0;
+    b.strip_host_bytes = offload ? (size_t)(b.strip_chunks - 2) * h->ntt * (tb_step + lr_step) * sizeof(float) : 0;
     // TMA row coordinates of the strip arrays are 32-bit
-    if (!forward_only && !snap &&
-        ((long long)nt * 4 * b.X >= (1LL << 31) || (long long)nt * 4 * b.nshots * 8 >= (1LL << 31)))
-        return fail(SFWI_E_ARG, "batch too large for one run (nt x packed rows = %lld); split the shots",
-                    (long long)nt * b.X);
+    if (strips && ((long long)b.strip_steps * 4 * b.X >= (1LL << 31) ||
+                   (long long)b.strip_steps * 4 * b.nshots * 8 >= (1LL << 31)))
+        return fail(SFWI_E_ARG, "batch too large for one run (strip steps x packed rows = %lld); split the shots "
+                    "or keep the strips in host memory", (long long)b.strip_steps * b.X);
     if (snap && b.nshots > SNAP_MAX_SHOTS)
         return fail(SFWI_E_ARG, "snapshot runs take at most %d shots at a time", SNAP_MAX_SHOTS);
     CK(b.grid.ensure((size_t)NGRID * b.cells));
@@ -649,8 +700,27 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
             CK(b.sscale.ensure((size_t)b.nshots * b.nsnap * 2));
             CK(cudaMemsetAsync(b.sscale.p, 0, (size_t)b.nshots * b.nsnap * 2 * sizeof(float), h->st));
         } else {
-            CK(b.tb.ensure((size_t)nt * 4 * b.X * 8));
-            CK(b.lr.ensure((size_t)nt * 4 * b.nshots * 8 * b.P));
+            const size_t ntb = (size_t)b.strip_steps * tb_step, nlr = (size_t)b.strip_steps * lr_step;
+            if (offload) {
+                // the ring replaces strips of a larger earlier run
+                if (b.tb.n > ntb) b.tb.release();
+                if (b.lr.n > nlr) b.lr.release();
+            }
+            CK(b.tb.ensure(ntb));
+            CK(b.lr.ensure(nlr));
+            if (offload) {
+                if (!h->cs) {
+                    CK(cudaStreamCreateWithFlags(&h->cs, cudaStreamNonBlocking));
+                    CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+                    for (auto &ev : h->ev_copy) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                }
+                const size_t held = (size_t)(b.strip_chunks - 2) * h->ntt;
+                if (h->htb.n < held * tb_step || h->hlr.n < held * lr_step) {
+                    CK(cudaStreamSynchronize(h->st));  // no copy of an earlier run still reads them
+                    CK(h->htb.ensure(held * tb_step));
+                    CK(h->hlr.ensure(held * lr_step));
+                }
+            }
         }
         CK(b.rsrc.ensure((size_t)b.X * b.rsp));
     }
@@ -764,7 +834,8 @@ std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
                                 (long long)(uintptr_t)b.lr.p, (long long)(uintptr_t)b.rrow.p,
                                 (long long)(uintptr_t)b.rsrc.p, (long long)(uintptr_t)b.dtiles.p,
-                                (long long)(uintptr_t)b.dgeo.p, (long long)(uintptr_t)h->sou.p};
+                                (long long)(uintptr_t)b.dgeo.p, (long long)(uintptr_t)h->sou.p, b.strip_steps,
+                                b.strip_chunk, (long long)(uintptr_t)h->htb.p, (long long)(uintptr_t)h->hlr.p};
     for (auto &t : b.tiles) s.push_back(((long long)t.shot << 40) ^ ((long long)t.x0 << 24) ^ (t.z0 << 8) ^ t.flags);
     for (auto &g : b.geo) {
         s.push_back(g.isx * 100003LL + g.isz);
@@ -783,33 +854,76 @@ Params step_params(const sfwi_handle *h, const Params &p, int it) {
     return q;
 }
 
-void enqueue_forward(sfwi_handle *h, const Params &p, bool forward_only) {
+// Copy chunk `chunk` of the edge strips between its ring slot (chunk % 2) on
+// the device and its place in host memory, on the copy stream, after the
+// work queued so far on the run's stream; ev_copy[slot] marks its end.
+int strip_copy(sfwi_handle *h, int chunk, bool to_host) {
+    Batch &b = h->b;
+    const size_t tb_step = (size_t)4 * b.X * 8, lr_step = (size_t)4 * b.nshots * 8 * b.P;
+    const size_t n = b.strip_chunk, slot = chunk % 2;
+    float *dtb = b.tb.p + slot * n * tb_step, *htb = h->htb.p + (size_t)chunk * n * tb_step;
+    float *dlr = b.lr.p + slot * n * lr_step, *hlr = h->hlr.p + (size_t)chunk * n * lr_step;
+    CK(cudaEventRecord(h->ev_fork, h->st));
+    CK(cudaStreamWaitEvent(h->cs, h->ev_fork, 0));
+    if (to_host) {
+        CK(cudaMemcpyAsync(htb, dtb, n * tb_step * sizeof(float), cudaMemcpyDeviceToHost, h->cs));
+        CK(cudaMemcpyAsync(hlr, dlr, n * lr_step * sizeof(float), cudaMemcpyDeviceToHost, h->cs));
+    } else {
+        CK(cudaMemcpyAsync(dtb, htb, n * tb_step * sizeof(float), cudaMemcpyHostToDevice, h->cs));
+        CK(cudaMemcpyAsync(dlr, hlr, n * lr_step * sizeof(float), cudaMemcpyHostToDevice, h->cs));
+    }
+    CK(cudaEventRecord(h->ev_copy[slot], h->cs));
+    return SFWI_OK;
+}
+
+// The forward time loop.  With the strips in host memory, chunk c (steps
+// [c ntt, (c+1) ntt)) is written into ring slot c % 2 once the copy of chunk
+// c - 2 out of that slot has ended, and goes to host memory itself when it
+// is full, unless it is one of the last two chunks (those stay in the ring
+// for the first backward steps).
+int enqueue_forward(sfwi_handle *h, const Params &p, bool forward_only) {
     const bool born = h->stage == 2;
     (void)forward_only;
+    const int n = h->b.strip_chunk, nc = h->b.strip_chunks;
     for (int it = 0; it < h->nt; it++) {
+        if (n && it % n == 0 && it / n >= 2) CK(cudaStreamWaitEvent(h->st, h->ev_copy[(it / n) % 2], 0));
         const Params q = step_params(h, p, it);
         h->tv->launch(0, q, h->b.tm, it, born, 1.f, h->st);
         h->tv->launch(1, q, h->b.tm, it, born, 1.f, h->st);
+        if (n && (it + 1) % n == 0 && (it + 1) / n <= nc - 2)
+            if (int rc = strip_copy(h, it / n, true)) return rc;
     }
+    return SFWI_OK;
 }
 
-void enqueue_backward(sfwi_handle *h, const Params &p) {
+// The backward time loop.  With the strips in host memory, the first
+// backward step of chunk c <= nc - 3 waits for its copy back into slot c % 2,
+// which starts once chunk c + 2, the slot's last user, is done.
+int enqueue_backward(sfwi_handle *h, const Params &p) {
     const float adj = h->stage == 1 ? 1.f : -1.f;
+    const int n = h->b.strip_chunk, nc = h->b.strip_chunks;
     for (int it = h->nt - 1; it >= 0; it--) {
+        const int c = n ? it / n : 0;
+        if (n && (it + 1) % n == 0 && c <= nc - 3) CK(cudaStreamWaitEvent(h->st, h->ev_copy[c % 2], 0));
         const Params q = step_params(h, p, it);
         h->tv->launch(2, q, h->b.tm, it, false, adj, h->st);
         h->tv->launch(3, q, h->b.tm, it, false, adj, h->st);
+        if (n && it % n == 0 && c >= 2)
+            if (int rc = strip_copy(h, c - 2, false)) return rc;
     }
+    return SFWI_OK;
 }
 
 int capture(sfwi_handle *h, cudaGraphExec_t *out, bool fwd, const Params &p, bool forward_only) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    if (fwd)
-        enqueue_forward(h, p, forward_only);
-    else
-        enqueue_backward(h, p);
+    const int rc = fwd ? enqueue_forward(h, p, forward_only) : enqueue_backward(h, p);
     cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc;
+    }
     if (e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
         return fail(SFWI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -909,8 +1023,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     CK(cudaEventRecord(h->ev[0], st));
     if (h->use_graphs)
         CK(cudaGraphLaunch(b.gfwd, st));
-    else
-        enqueue_forward(h, p, forward_only);
+    else if ((rc = enqueue_forward(h, p, forward_only)))
+        return rc;
     h->launches += 2LL * nt;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[1], st));
@@ -972,8 +1086,8 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     CK(cudaEventRecord(h->ev[2], st));
     if (h->use_graphs)
         CK(cudaGraphLaunch(b.gbwd, st));
-    else
-        enqueue_backward(h, p);
+    else if ((rc = enqueue_backward(h, p)))
+        return rc;
     h->launches += 2LL * nt;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[3], st));
@@ -1484,8 +1598,15 @@ int sfwi_destroy(sfwi_handle *h) {
     h->b.drop_graphs();
     for_each_buf(h, [](auto &d) { d.release(); });
     if (h->st) cudaStreamSynchronize(h->st);  // the stream-ordered frees
+    if (h->cs) cudaStreamSynchronize(h->cs);
+    h->htb.release();
+    h->hlr.release();
     for (auto &ev : h->ev)
         if (ev) cudaEventDestroy(ev);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    for (auto &ev : h->ev_copy)
+        if (ev) cudaEventDestroy(ev);
+    if (h->cs) cudaStreamDestroy(h->cs);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return SFWI_OK;
@@ -1576,6 +1697,21 @@ int sfwi_set_snapshots(sfwi_handle *h, int every, int format) {
     if (every > 0 && h->want_rho) return fail(SFWI_E_STATE, "the density kernel needs the reconstruction");
     h->snap_every = every;
     h->snap_fmt = every > 0 ? format : SNAP_OFF;
+    return SFWI_OK;
+}
+
+int sfwi_set_cpu_mem(sfwi_handle *h, int cpu_mem, int ntt) {
+    if (int rc = check(h)) return rc;
+    if (cpu_mem && ntt < 1) return fail(SFWI_E_ARG, "ntt must be at least 1 step when cpu_mem is set (got %d)", ntt);
+    h->cpu_mem = cpu_mem ? 1 : 0;
+    h->ntt = cpu_mem ? ntt : 0;
+    return SFWI_OK;
+}
+
+int sfwi_strip_bytes(sfwi_handle *h, size_t *device_bytes, size_t *host_bytes) {
+    if (int rc = check(h)) return rc;
+    if (device_bytes) *device_bytes = h->b.strip_dev_bytes;
+    if (host_bytes) *host_bytes = h->b.strip_host_bytes;
     return SFWI_OK;
 }
 

@@ -859,6 +859,7 @@ template <bool BORN>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdS<BORN>;
+    const int sit = it % p.strip_steps;  // row block of this step in the strip arrays
     __shared__ float s_sc[2 * SNAP_MAX_SHOTS];  // snapshot scales of this step (16-bit formats)
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME;
@@ -936,12 +937,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                     const int bi = (lx - c.t.x0 + HALO) * BZ + (lz - c.t.z0 + HALO);
                     if (band < 2) {
                         const long long o = c.g.row0 + lx;
-                        p.tb[tb_row(it, 0, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vx[bi];
-                        p.tb[tb_row(it, 1, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vz[bi];
+                        p.tb[tb_row(sit, 0, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vx[bi];
+                        p.tb[tb_row(sit, 1, band, p.X, (int)o) * 8 + (lz - bb.z0)] = s_vz[bi];
                     } else {
                         const int r = lx - bb.x0;
-                        p.lr[lr_row(it, 0, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vx[bi];
-                        p.lr[lr_row(it, 1, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vz[bi];
+                        p.lr[lr_row(sit, 0, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vx[bi];
+                        p.lr[lr_row(sit, 1, band - 2, p.nshots, c.t.shot, r) * p.P + lz] = s_vz[bi];
                     }
                 }
             }
@@ -1171,6 +1172,7 @@ __device__ __forceinline__ void patch_residual(const TileCtx &c, const float *rs
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
     using S = BwdS;
+    const int sit = it % p.strip_steps;  // row block of this step in the strip arrays
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
         const bool frame = c.t.flags & TILE_FRAME, image = c.t.flags & TILE_IMAGE;
         const bool strip = c.t.flags & TILE_STRIP, recv = c.t.flags & TILE_RECV;
@@ -1196,10 +1198,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // (negative coordinate) or rows no band cell maps to
         for (int comp = 0; comp < 2; comp++) {
             if (sp.tb >= 0)
-                tma_load_2d(s + S::STRIPS + comp * S::TBF, &tm.tb, 0, (int)tb_row(it, comp, sp.tb, p.X, c.brow), bar);
+                tma_load_2d(s + S::STRIPS + comp * S::TBF, &tm.tb, 0, (int)tb_row(sit, comp, sp.tb, p.X, c.brow), bar);
             if (sp.lr >= 0)
                 tma_load_2d(s + S::STRIPS + 2 * S::TBF + comp * S::LRF, &tm.lr, c.bcol,
-                            (int)lr_row(it, comp, sp.lr, p.nshots, c.t.shot, 0), bar);
+                            (int)lr_row(sit, comp, sp.lr, p.nshots, c.t.shot, 0), bar);
         }
         if (recv) tma_load_2d(s + S::RS, &tm.rs, (2 * it) & ~3, c.brow, bar);
     };
@@ -1240,16 +1242,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                             vz = tbs[S::TBF + i];
                         } else {
                             const int prow = c.g.row0 + lx;
-                            vx = p.tb[tb_row(it, 0, band, p.X, prow) * 8 + (lz - bb.z0)];
-                            vz = p.tb[tb_row(it, 1, band, p.X, prow) * 8 + (lz - bb.z0)];
+                            vx = p.tb[tb_row(sit, 0, band, p.X, prow) * 8 + (lz - bb.z0)];
+                            vz = p.tb[tb_row(sit, 1, band, p.X, prow) * 8 + (lz - bb.z0)];
                         }
                     } else {
                         if (staged) {
                             vx = lrs[i];  // slot (lx - x0) * BZ + (lz - bz)
                             vz = lrs[S::LRF + i];
                         } else {
-                            vx = p.lr[lr_row(it, 0, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
-                            vz = p.lr[lr_row(it, 1, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
+                            vx = p.lr[lr_row(sit, 0, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
+                            vz = p.lr[lr_row(sit, 1, band - 2, p.nshots, c.t.shot, lx - bb.x0) * p.P + lz];
                         }
                     }
                     const int bi = (lx - bx) * BZ + (lz - bz);

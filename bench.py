@@ -265,31 +265,45 @@ def reference_gpu_sample(w, data, nshots, warm=True):
                       "wall clock per shot"}
 
 
-def run_serving(n, budget_gb=64.0, slots=4, full=False):
-    """Serving loop on a seeded Poisson stream (50 requests/s; grids, nt and
-    shots drawn from the serving configuration's ranges, then, unless `full`,
-    scaled by 0.3 in each grid dimension and 0.1 in nt so the stream is served
-    in seconds): continuous admission against an HBM budget -- the requests
-    admitted together sharing one run of the engine (two runs in flight), or
-    one engine per request -- vs the plain FIFO loop, each replayed twice and
-    measured on the second replay.  At the
-    drawn sizes a request takes about a second of GPU time, so a stream at
-    50/s queues: the latencies then measure the backlog."""
+def run_serving(n, budget_gb=64.0, slots=4, full=True):
+    """Serving loop on a seeded Poisson stream (50 requests/s; grids 200x100
+    to 2001x1001, nt 2000-6000 and 1-8 shots drawn per request; with
+    full=False scaled by 0.3 in each grid dimension and 0.1 in nt).  Four
+    servers on the same stream, each replayed once after one warm request:
+      fifo                   one request at a time in arrival order;
+      served_shortest_first  up to `slots` requests at once, each on its own
+                             engine and stream, least work first;
+      batched                the requests admitted together share one engine
+                             run (sfwi_run_models), two runs in flight;
+      batched_shortest_first as batched, but a run forms once the oldest
+                             waiting request has waited 0.3 s, from the
+                             least-work requests, at most 4 per run.
+    At the drawn sizes a request takes up to several seconds of GPU time, so
+    a stream at 50/s queues: the latencies measure the backlog."""
     from sfwi_gb300 import serve
     gs, ns = (1.0, 1.0) if full else (0.3, 0.1)
     reqs = serve.poisson_requests(n, 50.0, seed=4, grid_scale=gs, nt_scale=ns)
     serve.run_request(reqs[0])  # warm the kernels and the allocator
     out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
+           "shot_gradients": sum(r.shot_gradients for r in reqs),
            "scale": "the drawn sizes" if full else "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
-    for name, srv in (("served_batched", serve.Server(budget_gb * 2 ** 30, max_active=2, batch=True)),
-                      ("served", serve.Server(budget_gb * 2 ** 30, max_active=slots)),
-                      ("served_shortest_first", serve.Server(budget_gb * 2 ** 30, max_active=slots, policy="shortest")),
-                      ("fifo", serve.Server(budget_gb * 2 ** 30, max_active=1))):
-        srv.run(reqs)  # the first replay settles the allocator pools and host threads
+    B = budget_gb * 2 ** 30
+    for name, srv in (("fifo", serve.Server(B, max_active=1)),
+                      ("served_shortest_first", serve.Server(B, max_active=slots, policy="shortest")),
+                      ("batched", serve.Server(B, max_active=2, batch=True)),
+                      ("batched_shortest_first", serve.Server(B, max_active=2, batch=True, policy="shortest",
+                                                              max_batch=4, window=0.3))):
+        if not full:
+            srv.run(reqs)  # short requests: a first replay settles the allocator pools and host threads
         res = srv.run(reqs)
         st = serve.latency_stats(res)
         st["shot_gradients_per_s"] = sum(r.shot_gradients for r in reqs) / st["span_s"]
         out[name] = {k: round(v, 3) if isinstance(v, float) else v for k, v in st.items()}
+    f = out["fifo"]
+    for name in ("served_shortest_first", "batched", "batched_shortest_first"):
+        o = out[name]
+        o["vs_fifo"] = {"p50": round(o["p50_ms"] / f["p50_ms"], 3), "p99": round(o["p99_ms"] / f["p99_ms"], 3),
+                        "throughput": round(o["shot_gradients_per_s"] / f["shot_gradients_per_s"], 3)}
     return out
 
 
@@ -599,9 +613,10 @@ def main():
     ap.add_argument("--shots", type=int, default=None, help="override the number of shots (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-shots", type=int, default=8, help="shots timed one at a time for the plain form")
-    ap.add_argument("--serving-requests", type=int, default=48, help="requests of the serving-loop measurement")
-    ap.add_argument("--serving-full", action="store_true",
-                    help="serve the requests at the drawn sizes (200x100 to 2001x1001, nt 2000-6000) unscaled")
+    ap.add_argument("--serving-requests", type=int, default=12, help="requests of the serving-loop measurement")
+    ap.add_argument("--serving-scaled", action="store_true",
+                    help="serve the requests scaled to 0.3x grid and 0.1x nt (default: the drawn sizes, 200x100 to "
+                         "2001x1001, nt 2000-6000)")
     ap.add_argument("--snap-check", type=int, default=4, help="shots of the compressed-vs-FP32 snapshot check")
     ap.add_argument("--profile-kernels", action="store_true", help="only run warm-up steps (for ncu captures)")
     ap.add_argument("--reference-gpu-shots", type=int, default=1,
@@ -660,7 +675,7 @@ def main():
             re = measure(we, args, args.extra_steps, 2, args.plain_shots)
             extras[name] = sub_record(we, re)
             close_workload(re)
-    serving = (run_serving(args.serving_requests, full=args.serving_full)
+    serving = (run_serving(args.serving_requests, full=not args.serving_scaled)
                if args.serving_requests > 0 and rank == 0 else None)
     if rank != 0:
         return 0

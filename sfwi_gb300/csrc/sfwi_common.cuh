@@ -154,6 +154,7 @@ struct Params {
     int overlap;                // host side: launch step kernels with programmatic dependent launch
     int src_kind;               // SRC_TXX_TZZ (the reference's) or SRC_VZ_FORCE
     unsigned wait_limit;        // tries of a pipeline mbarrier wait before it is declared lost
+    unsigned reverse_tiles;     // bit k: step kernel k draws its tiles in reverse table order
 };
 // tries of mbarrier.try_wait before a pipeline wait is declared lost (each try
 // may suspend the thread for a while; the bound is several seconds)

@@ -27,6 +27,9 @@ using namespace sfwi;
 namespace {
 
 constexpr int kTimeKernelsMaxReps = 64;
+// step kernels that draw their tiles in reverse order (k_fwd_s, k_bwd_v):
+// each sweep starts on the tiles the sweep before finished with
+constexpr unsigned kReverseTiles = (1u << 1) | (1u << 3);
 constexpr double kOtSigmaFloor = OT_SIGMA_FLOOR;
 thread_local std::string g_err;
 
@@ -623,6 +626,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     Params p{};
     p.overlap = h->launch_overlap ? 1 : 0;
     p.wait_limit = PIPE_WAIT_LIMIT;
+    p.reverse_tiles = kReverseTiles;
     p.src_kind = h->src_kind;
     p.X = b.X;
     p.P = b.P;
@@ -2016,9 +2020,15 @@ int sfwi_time_kernels(sfwi_handle *h, int reps, float *out_ms) {
         // step indices 0..reps select fresh tile counters; the kernels read
         // records and strips at those steps, which exist for every run
         CK(cudaMemsetAsync(h->b.dctr.p, 0, 4 * (size_t)(reps + 1) * sizeof(int), h->st));
-        h->tv->launch(k, p, h->b.tm, reps, born, adj, h->st);  // warm
+        // consecutive launches alternate the tile order, as consecutive
+        // sweeps of a time loop do: each starts where the one before ended
+        Params q = p;
+        h->tv->launch(k, q, h->b.tm, reps, born, adj, h->st);  // warm
         CK(cudaEventRecord(h->ev[0], h->st));
-        for (int r = 0; r < reps; r++) h->tv->launch(k, p, h->b.tm, r, born, adj, h->st);
+        for (int r = 0; r < reps; r++) {
+            q.reverse_tiles = p.reverse_tiles ^ ((unsigned)((r + 1) & 1) << k);
+            h->tv->launch(k, q, h->b.tm, r, born, adj, h->st);
+        }
         CK(cudaEventRecord(h->ev[1], h->st));
         CK(cudaEventSynchronize(h->ev[1]));
         CK(cudaGetLastError());

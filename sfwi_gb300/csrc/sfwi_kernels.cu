@@ -591,6 +591,13 @@ __device__ __forceinline__ void load_cores(float *dst, const TmaMaps &tm, const 
 //                                  done, so the refill overlaps its arithmetic
 //                                  and stores (run_tiles releases after the
 //                                  body for a thread that did not)
+// Kernel `kid` (0..3: k_fwd_v, k_fwd_s, k_bwd_s, k_bwd_v) draws its tiles
+// in reverse table order (the k-th drawn index takes entry ntiles-1-k) when
+// bit kid of p.reverse_tiles is set.  A time loop reverses the second sweep
+// of each step (k_fwd_s, k_bwd_v): consecutive sweeps then meet where one
+// ended, and the first tiles a sweep stages are the ones whose outputs the
+// sweep before wrote last, most of them still in L2.  Each tile's arithmetic
+// does not depend on the order.
 constexpr int PRODUCER_WARP = NTHREADS / 32;
 constexpr int BLOCK_THREADS = NTHREADS + 32;
 
@@ -610,7 +617,8 @@ struct StageRelease {
 };
 
 template <int STAGE_FLOATS, class Issue, class Body>
-__device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body) {
+__device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body, int kid) {
+    const bool reverse = (p.reverse_tiles >> kid) & 1;
     __shared__ uint64_t full[NSTAGE], empty[NSTAGE];
     __shared__ TileCtx s_ctx[NSTAGE];
     __shared__ int s_tile[NSTAGE];
@@ -636,7 +644,7 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
         int t = atomicAdd(counter, 1);
         int t_next = atomicAdd(counter, 1);
         TileCtx ctx;
-        if (t < p.ntiles) ctx = tile_ctx(p, t);
+        if (t < p.ntiles) ctx = tile_ctx(p, reverse ? p.ntiles - 1 - t : t);
         griddep_wait();
         for (int k = 0;; k++) {
             const int s = k % NSTAGE;
@@ -654,7 +662,7 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
             // indices only grow: once one is past the end, so are all later ones
             t = t_next;
             if (t < p.ntiles) {
-                ctx = tile_ctx(p, t);
+                ctx = tile_ctx(p, reverse ? p.ntiles - 1 - t : t);
                 t_next = atomicAdd(counter, 1);
             }
         }
@@ -840,7 +848,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             }
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1033,7 +1041,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         griddep_wait();  // the scales come from the velocity sweep just before
         load_snap_scales(p, it / p.snap_every, s_sc);
     }
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1318,7 +1326,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             stc(p.gmu + m.gi, gm);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body, 2);
 }
 
 // Lame-weighted adjoint stresses of a staged box, in place (consumers):
@@ -1460,7 +1468,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             stc(p.grho + m.gi, gr);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body, 3);
 }
 
 // ---------------------------------------------------------------------------
@@ -1569,7 +1577,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         griddep_wait();
         load_snap_scales(p, k, s_sc);
     }
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body, 2);
 }
 
 struct BwdVSnap {
@@ -1629,7 +1637,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body);
+    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body, 3);
 }
 
 // ---------------------------------------------------------------------------
@@ -1644,7 +1652,7 @@ constexpr int PROBE_STAGE = 32;
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM) k_wait_probe(const Params p) {
     auto issue = [&](const TileCtx &, float *, uint64_t *) {};
     auto body = [&](const TileCtx &, float *, StageRelease &) {};
-    run_tiles<PROBE_STAGE>(p, p.counters, issue, body);
+    run_tiles<PROBE_STAGE>(p, p.counters, issue, body, 0);
 }
 
 // ---------------------------------------------------------------------------

@@ -72,15 +72,23 @@ class Result:
         return self.done - self.arrival
 
 
-def request_bytes(req):
+def strip_steps(nt, strip_chunk=0):
+    """Steps of edge strips the device holds: nt, or the two-chunk ring when
+    the strips live in host memory (sfwi_set_cpu_mem)"""
+    return 2 * strip_chunk if 0 < strip_chunk and 2 * strip_chunk < nt else nt
+
+
+def request_bytes(req, strip_chunk=0):
     """Device memory of one request's engine (the engine's allocations,
-    sfwi_engine.cu:upload_batch, plus the model and the FP64 gradients)."""
+    sfwi_engine.cu:upload_batch, plus the model and the FP64 gradients);
+    strip_chunk > 0: edge strips in host memory in chunks of that many steps."""
     P = (req.allnz + 2 * req.pml + 3) // 4 * 4
     X = sum(int(d["nx"]) + 2 * req.pml for d in req.shots)
     ntr = sum(len(d["gc"]) for d in req.shots)
     nt, ns = req.nt, len(req.shots)
+    ss = strip_steps(nt, strip_chunk)
     floats = (NGRID * X * P                       # wavefields, memory variables, coefficients
-              + nt * 4 * X * 8 + nt * 4 * ns * 8 * P  # edge strips
+              + ss * 4 * X * 8 + ss * 4 * ns * 8 * P  # edge strips
               + nt * 2 * X                        # receiver-row records
               + X * ((2 * nt + 3) // 4 * 4)       # residual source
               + NREC * ntr * nt                   # records
@@ -88,7 +96,7 @@ def request_bytes(req):
     return 4 * floats + 8 * 4 * req.allnx * req.allnz + (1 << 20)
 
 
-def batch_bytes(reqs):
+def batch_bytes(reqs, strip_chunk=0):
     """Device memory of one shared run of several requests: the packed grid
     at the deepest request's depth, strips and records for the longest
     request's nt, the models and their FP64 gradients."""
@@ -99,12 +107,13 @@ def batch_bytes(reqs):
     nt = max(r.nt for r in reqs)
     ns = sum(len(r.shots) for r in reqs)
     cells = sum(r.allnx * r.allnz for r in reqs)
-    floats = (NGRID * X * P + nt * 4 * X * 8 + nt * 4 * ns * 8 * P + nt * 2 * X + X * ((2 * nt + 3) // 4 * 4)
+    ss = strip_steps(nt, strip_chunk)
+    floats = (NGRID * X * P + ss * 4 * X * 8 + ss * 4 * ns * 8 * P + nt * 2 * X + X * ((2 * nt + 3) // 4 * 4)
               + NREC * ntr * nt + 5 * cells + nt)
     return 4 * floats + 8 * 4 * cells + (1 << 20)
 
 
-def run_requests(reqs):
+def run_requests(reqs, strip_chunk=0):
     """Several requests in one run of one engine (sfwi_run_models): a list of
     (misfit, grad_pp, grad_ps, illum), one per request."""
     import sfwi_gb300 as sg
@@ -125,6 +134,8 @@ def run_requests(reqs):
     try:
         if reqs[0].misfit_kind:
             fd.set_misfit(reqs[0].misfit_kind)
+        if strip_chunk:
+            fd.set_cpu_mem(1, strip_chunk)
         shot_model = []
         for k, r in enumerate(reqs):
             for d in r.shots:
@@ -152,7 +163,7 @@ def request_work(req):
     return sum((int(d["nx"]) + 2 * req.pml) * P for d in req.shots) * req.nt
 
 
-def run_request(req):
+def run_request(req, strip_chunk=0):
     """One request on a fresh engine: (misfit, grad_pp, grad_ps, illum)."""
     import sfwi_gb300 as sg
     maxnx = max(int(d["nx"]) for d in req.shots)
@@ -162,6 +173,8 @@ def run_request(req):
         fd.GPUbufferVPVS(req.vp, req.vs, req.rho)
         if req.misfit_kind:
             fd.set_misfit(req.misfit_kind)
+        if strip_chunk:
+            fd.set_cpu_mem(1, strip_chunk)
         for d in req.shots:
             fd.enqueue_shot(d["nx"], d["isx"], d["isz"], d["igz"], d["ngx_left"], d["delta_left"], 0, d["gc"],
                             d["obs_z"], d["obs_x"])
@@ -177,20 +190,34 @@ class Server:
     HBM budget free up.  policy "oldest" admits in arrival order, letting a
     later request that fits overtake one that does not; "shortest" admits the
     request with the least work first (request_work); with max_active=1 the
-    loop is the plain FIFO."""
+    loop is the plain FIFO.
 
-    def __init__(self, budget_bytes, max_active=4, runner=run_request, sizer=request_bytes, clock=time.perf_counter,
-                 policy="oldest", work=request_work, batch=False, batch_runner=run_requests, batch_sizer=batch_bytes,
-                 max_batch=64):
+    Batched (batch=True): the requests admitted together share one run, at
+    most max_batch of them; a run forms once the oldest waiting request has
+    waited `window` seconds (or no request is still due), so requests that
+    arrive close together can share it and the shortest-first order sees
+    them all.  strip_chunk > 0 keeps every run's edge strips in host memory
+    in chunks of that many steps (sfwi_set_cpu_mem): the budget then counts
+    the device ring only, and more requests fit at once."""
+
+    def __init__(self, budget_bytes, max_active=4, runner=None, sizer=None, clock=time.perf_counter,
+                 policy="oldest", work=request_work, batch=False, batch_runner=None, batch_sizer=None,
+                 max_batch=64, window=0.0, strip_chunk=0):
         if policy not in ("oldest", "shortest"):
             raise ValueError("policy must be 'oldest' or 'shortest'")
         self.budget = int(budget_bytes)
         self.max_active = int(max_active)
-        self.runner, self.sizer, self.clock = runner, sizer, clock
+        sc = int(strip_chunk)
+        self.runner = runner or (lambda r: run_request(r, sc))
+        self.sizer = sizer or (lambda r: request_bytes(r, sc))
+        self.clock = clock
         self.policy, self.work = policy, work
         # batched: the requests admitted together share one run (batch_runner)
-        self.batch, self.batch_runner, self.batch_sizer = batch, batch_runner, batch_sizer
+        self.batch = batch
+        self.batch_runner = batch_runner or (lambda g: run_requests(g, sc))
+        self.batch_sizer = batch_sizer or (lambda g: batch_bytes(g, sc))
         self.max_batch = int(max_batch)
+        self.window = float(window)
 
     def run(self, requests):
         """Replay `requests` (arrival offsets in seconds) against the wall
@@ -235,7 +262,8 @@ class Server:
                 order = list(waiting) if self.policy == "oldest" else sorted(waiting, key=lambda q: (self.work(q), q.rid))
                 if self.batch:
                     # one shared run of every waiting request that fits the budget
-                    if state["active"] < self.max_active and order:
+                    due = bool(waiting) and (nxt >= len(reqs) or t - min(q.arrival for q in waiting) >= self.window)
+                    if state["active"] < self.max_active and order and due:
                         group, size = [], 0
                         for r in order:
                             if len(group) >= self.max_batch:
@@ -269,6 +297,10 @@ class Server:
                 if errors:
                     break
                 timeout = None if nxt >= len(reqs) else max(0.0, reqs[nxt].arrival - now())
+                if self.batch and waiting and state["active"] < self.max_active and nxt < len(reqs):
+                    # wake when the oldest waiting request's window closes
+                    dl = max(0.0, min(q.arrival for q in waiting) + self.window - now())
+                    timeout = dl if timeout is None else min(timeout, dl)
                 cv.wait(timeout=timeout if timeout is None else min(timeout, 0.5))
         for th in threads:
             th.join()

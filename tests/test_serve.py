@@ -134,6 +134,41 @@ def test_batched_admission_groups_the_waiting_requests():
     assert [len(g) for g in rec2.groups] == [2, 2, 1]
 
 
+def test_batching_window_collects_requests_arriving_close_together():
+    # without a window the first request runs alone; with a 0.1 s window the
+    # three arrivals within 0.06 s share one run
+    arrivals = [0.0, 0.03, 0.06]
+    rec = BatchRecorder(0.05)
+    serve.Server(100, max_active=1, batch=True, batch_runner=rec, batch_sizer=lambda g: len(g)).run(
+        _fake_requests([1] * 3, arrivals))
+    assert rec.groups[0] == [0]
+    rec = BatchRecorder(0.05)
+    res = serve.Server(100, max_active=1, batch=True, batch_runner=rec, batch_sizer=lambda g: len(g),
+                       window=0.1).run(_fake_requests([1] * 3, arrivals))
+    assert rec.groups == [[0, 1, 2]]
+    # the run forms at the last arrival: no request is still due
+    assert 0.06 <= res[0].admitted < 0.1
+
+
+def test_batched_shortest_first_takes_the_least_work_into_the_first_runs():
+    # sizes double as work: with a window covering every arrival the runs
+    # are the two smallest, then the next two, then the largest
+    reqs = _fake_requests([50, 10, 40, 20, 30], [0.0, 0.005, 0.01, 0.015, 0.02])
+    rec = BatchRecorder(0.03)
+    serve.Server(1000, max_active=1, batch=True, batch_runner=rec, batch_sizer=lambda g: len(g), policy="shortest",
+                 work=lambda r: r.size, max_batch=2, window=0.05).run(reqs)
+    assert rec.groups == [[1, 3], [4, 2], [0]]
+
+
+def test_host_strips_shrink_the_device_bytes_of_a_request():
+    r = serve.poisson_requests(1, 10.0, grid=((300, 150), (300, 150)), nt=(2000, 2000), shots=(4, 4))[0]
+    full, ring = serve.request_bytes(r), serve.request_bytes(r, strip_chunk=100)
+    assert ring < full / 2  # records and the grid stay
+    assert serve.request_bytes(r, strip_chunk=1000) == full  # a ring of 2 x 1000 steps holds them all
+    assert serve.batch_bytes([r], strip_chunk=100) < serve.batch_bytes([r]) / 2
+    assert serve.strip_steps(2000, 100) == 200 and serve.strip_steps(2000, 0) == 2000
+
+
 def test_batch_bytes_covers_its_requests():
     a, b = serve.poisson_requests(2, 10.0, grid=((60, 30), (90, 50)), nt=(100, 140), shots=(1, 2))
     both = serve.batch_bytes([a, b])
@@ -149,11 +184,13 @@ def test_batched_serving_gives_each_request_its_result_alone():
     assert len({r.nt for r in reqs}) > 1 and len({(r.allnx, r.allnz) for r in reqs}) > 1
     alone = [serve.run_request(r) for r in reqs]
     mixed = serve.run_requests(reqs)
+    host = serve.run_requests(reqs, strip_chunk=37)  # edge strips in host memory
     res = serve.Server(8 << 30, max_active=2, batch=True).run(reqs)
-    for a, m, r in zip(alone, mixed, res):
-        assert a[0] == m[0] == r.misfit
-        for x, y, z in zip(a[1:], m[1:], (r.grad_pp, r.grad_ps, r.illum)):
-            assert np.array_equal(x, y) and np.array_equal(x, z)
+    sjf = serve.Server(8 << 30, max_active=2, batch=True, policy="shortest", max_batch=2, window=0.05).run(reqs)
+    for a, m, h, r, q in zip(alone, mixed, host, res, sjf):
+        assert a[0] == m[0] == h[0] == r.misfit == q.misfit
+        for x, y, u, z, w in zip(a[1:], m[1:], h[1:], (r.grad_pp, r.grad_ps, r.illum), (q.grad_pp, q.grad_ps, q.illum)):
+            assert np.array_equal(x, y) and np.array_equal(x, u) and np.array_equal(x, z) and np.array_equal(x, w)
 
 
 @pytest.mark.gpu

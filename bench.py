@@ -599,6 +599,8 @@ def sub_record(w, r):
            "roofline": r["roof"] and {k: r["roof"][k] for k in ("kernel", "achieved", "peak", "frac", "launch_ms",
                                                                  "all_kernels_ms", "all_kernels_frac")},
            "plain": r["plain"]}
+    if r.get("snap_err"):
+        rec["snapshot_error"] = r["snap_err"]
     return rec
 
 
@@ -624,7 +626,7 @@ def main():
     ap.add_argument("--profile-reference-gpu", action="store_true",
                     help="only run the reference's CUDA path on one shot of the workload (for ncu captures)")
     ap.add_argument("--tile", default="auto", help="tile shape of the step kernels: auto (autotuner) or a name in sfwi_gb300.TILE_SHAPES")
-    ap.add_argument("--extra-workloads", default="salt401,shot376",
+    ap.add_argument("--extra-workloads", default="salt401,shot376,snap2001",
                     help="workloads measured after the main one and reported as sub-records (comma list; '' for none)")
     ap.add_argument("--extra-steps", type=int, default=3, help="timed steps of each extra workload")
     args = ap.parse_args()
@@ -672,7 +674,11 @@ def main():
     if rank == 0 and not args.nt and not args.shots:
         for name in [x for x in args.extra_workloads.split(",") if x and x != args.workload]:
             we = dict(WORKLOADS[name])
-            re = measure(we, args, args.extra_steps, 2, args.plain_shots)
+            # the 2001x801 survey takes seconds a pass: two timed passes, and
+            # its compressed snapshots checked against FP32 ones on two shots
+            big = bool(we.get("snap"))
+            re = measure(we, args, min(args.extra_steps, 2) if big else args.extra_steps, 2,
+                         min(args.plain_shots, 4) if big else args.plain_shots, snap_check=2 if big else 0)
             extras[name] = sub_record(we, re)
             close_workload(re)
     serving = (run_serving(args.serving_requests, full=not args.serving_scaled)

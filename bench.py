@@ -277,7 +277,11 @@ def run_serving(n, budget_gb=64.0, slots=4, full=True):
                              run (sfwi_run_models), two runs in flight;
       batched_shortest_first as batched, but a run forms once the oldest
                              waiting request has waited 0.3 s, from the
-                             least-work requests, at most 4 per run.
+                             least-work requests, at most 4 per run;
+      served_shortest_first_host_strips_8gb
+                             served_shortest_first in an 8 GB budget, the
+                             edge strips in pinned host memory (100-step
+                             chunks; pinned blocks reused across engines).
     At the drawn sizes a request takes up to several seconds of GPU time, so
     a stream at 50/s queues: the latencies measure the backlog."""
     from sfwi_gb300 import serve
@@ -292,7 +296,9 @@ def run_serving(n, budget_gb=64.0, slots=4, full=True):
                       ("served_shortest_first", serve.Server(B, max_active=slots, policy="shortest")),
                       ("batched", serve.Server(B, max_active=2, batch=True)),
                       ("batched_shortest_first", serve.Server(B, max_active=2, batch=True, policy="shortest",
-                                                              max_batch=4, window=0.3))):
+                                                              max_batch=4, window=0.3)),
+                      ("served_shortest_first_host_strips_8gb",
+                       serve.Server(min(B, 8 << 30), max_active=slots, policy="shortest", strip_chunk=100))):
         if not full:
             srv.run(reqs)  # short requests: a first replay settles the allocator pools and host threads
         res = srv.run(reqs)
@@ -300,7 +306,7 @@ def run_serving(n, budget_gb=64.0, slots=4, full=True):
         st["shot_gradients_per_s"] = sum(r.shot_gradients for r in reqs) / st["span_s"]
         out[name] = {k: round(v, 3) if isinstance(v, float) else v for k, v in st.items()}
     f = out["fifo"]
-    for name in ("served_shortest_first", "batched", "batched_shortest_first"):
+    for name in ("served_shortest_first", "batched", "batched_shortest_first", "served_shortest_first_host_strips_8gb"):
         o = out[name]
         o["vs_fifo"] = {"p50": round(o["p50_ms"] / f["p50_ms"], 3), "p99": round(o["p99_ms"] / f["p99_ms"], 3),
                         "throughput": round(o["shot_gradients_per_s"] / f["shot_gradients_per_s"], 3)}

@@ -128,6 +128,12 @@ int sfwi_set_snapshots(sfwi_handle *h, int every, int format);
 int sfwi_set_cpu_mem(sfwi_handle *h, int cpu_mem, int ntt);
 /* strip bytes of the last run: on the device, and in pinned host memory */
 int sfwi_strip_bytes(sfwi_handle *h, size_t *device_bytes, size_t *host_bytes);
+/* Pinned host memory released by handles (their host-held strips) is kept,
+ * up to `bytes` in all, in a process-wide cache and reused by the next
+ * handle whose strips fit in a cached block, instead of being page-locked
+ * again.  0 (the default) keeps nothing; lowering the limit frees cached
+ * blocks at once.  No reference counterpart. */
+int sfwi_set_pinned_cache(size_t bytes);
 int sfwi_read_density_gradient_f64(sfwi_handle *h, double *grad_rho);
 
 /* Records of the last shot-gradient call(s): forward records (stage 1:

@@ -24,6 +24,7 @@ from . import _lib
 from ._lib import SfwiError, ShotDesc
 
 __all__ = ["FD2DGPU_ELASTIC", "IMAGE_SINGLESHOT", "OT", "OT_power", "OT_alltrace", "normalize", "SfwiError",
+           "set_pinned_cache",
            "MISFIT_L2", "MISFIT_OT", "MISFIT_OT_POWER", "MISFIT_OT_ALLTRACE", "library_path"]
 
 MISFIT_L2, MISFIT_OT, MISFIT_OT_POWER, MISFIT_OT_ALLTRACE = 0, 1, 2, 3
@@ -369,6 +370,12 @@ class FD2DGPU_ELASTIC:
         f, b, o, t = C.c_float(), C.c_float(), C.c_float(), C.c_float()
         _lib.check(_lib.load().sfwi_last_timing(self._h, C.byref(f), C.byref(b), C.byref(o), C.byref(t)))
         return {"forward_ms": f.value, "backward_ms": b.value, "misfit_ms": o.value, "total_ms": t.value}
+
+
+def set_pinned_cache(nbytes):
+    """Keep up to `nbytes` of the pinned host memory that engines release
+    (their host-held edge strips) for reuse by later engines; 0 frees it."""
+    _lib.check(_lib.load().sfwi_set_pinned_cache(int(nbytes)))
 
 
 def IMAGE_SINGLESHOT(fdtdgpu, misfit=0.0, *reference_args):

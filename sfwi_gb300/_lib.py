@@ -43,6 +43,7 @@ SIGNATURES = {
     "sfwi_set_snapshots": (C.c_int, [_h, C.c_int, C.c_int]),
     "sfwi_set_cpu_mem": (C.c_int, [_h, C.c_int, C.c_int]),
     "sfwi_strip_bytes": (C.c_int, [_h, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "sfwi_set_pinned_cache": (C.c_int, [C.c_size_t]),
     "sfwi_read_density_gradient_f64": (C.c_int, [_h, _dp]),
     "sfwi_read_records": (C.c_int, [_h, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp]),
     "sfwi_enqueue_shot": (C.c_int, [_h, C.POINTER(ShotDesc)]),

@@ -14,6 +14,7 @@
 #include <vector>
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "../../include/sfwi_gb300.h"
 #include <cudaTypedefs.h>
@@ -86,20 +87,85 @@ struct DevBuf {
     }
 };
 
-// Pinned host buffer that grows on demand (edge strips kept in host memory).
-// Growing it frees the old block with cudaFreeHost, which waits for the
-// device; it only grows while no run is in flight.
+// Pinned host memory for edge strips kept in host memory.  Page-locking
+// takes about a second per 10 GB, so released blocks can be kept in a
+// process-wide cache (up to sfwi_set_pinned_cache bytes, none by default)
+// and handed to the next buffer that fits: a server that builds one engine
+// per request then pins each size once.
+struct PinnedCache {
+    std::mutex mu;
+    std::vector<std::pair<void *, size_t>> blocks;  // cached, not in use
+    size_t cached = 0, limit = 0;
+    // a cached block of at least `bytes` (the smallest such), or nullptr
+    void *take(size_t bytes, size_t *got) {
+        std::lock_guard<std::mutex> g(mu);
+        size_t best = blocks.size();
+        for (size_t i = 0; i < blocks.size(); i++)
+            if (blocks[i].second >= bytes && (best == blocks.size() || blocks[i].second < blocks[best].second))
+                best = i;
+        if (best == blocks.size()) return nullptr;
+        void *p = blocks[best].first;
+        *got = blocks[best].second;
+        cached -= *got;
+        blocks.erase(blocks.begin() + best);
+        return p;
+    }
+    // keep the block if the cache has room for it, else free it
+    void give(void *p, size_t bytes) {
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (cached + bytes <= limit) {
+                blocks.emplace_back(p, bytes);
+                cached += bytes;
+                return;
+            }
+        }
+        cudaFreeHost(p);
+    }
+    // free cached blocks until at most `keep` bytes remain
+    void trim(size_t keep) {
+        std::vector<void *> drop;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            std::sort(blocks.begin(), blocks.end(),
+                      [](const std::pair<void *, size_t> &a, const std::pair<void *, size_t> &b) { return a.second < b.second; });
+            while (cached > keep && !blocks.empty()) {
+                drop.push_back(blocks.back().first);
+                cached -= blocks.back().second;
+                blocks.pop_back();
+            }
+        }
+        for (void *p : drop) cudaFreeHost(p);
+    }
+};
+PinnedCache &pinned_cache() {
+    static PinnedCache c;
+    return c;
+}
+
+// Pinned host buffer that grows on demand.  Growing it returns the old block
+// to the cache (or frees it with cudaFreeHost, which waits for the device);
+// it only grows while no run is in flight.
 template <class T>
 struct HostBuf {
     T *p = nullptr;
-    size_t n = 0;
+    size_t n = 0;       // elements asked for
+    size_t bytes = 0;   // bytes of the block held
     cudaError_t ensure(size_t m) {
         if (m <= n && p) return cudaSuccess;
         release();
-        cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&p), std::max<size_t>(m, 1) * sizeof(T),
-                                      cudaHostAllocDefault);
+        const size_t want = std::max<size_t>(m, 1) * sizeof(T);
+        size_t got = 0;
+        if (void *c = pinned_cache().take(want, &got)) {
+            p = static_cast<T *>(c);
+            n = got / sizeof(T);
+            bytes = got;
+            return cudaSuccess;
+        }
+        cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(&p), want, cudaHostAllocDefault);
         if (e == cudaSuccess) {
             n = m;
+            bytes = want;
         } else {
             p = nullptr;
             cudaGetLastError();
@@ -107,9 +173,10 @@ struct HostBuf {
         return e;
     }
     void release() {
-        if (p) cudaFreeHost(p);
+        if (p) pinned_cache().give(p, bytes);
         p = nullptr;
         n = 0;
+        bytes = 0;
     }
 };
 
@@ -1709,6 +1776,16 @@ int sfwi_set_cpu_mem(sfwi_handle *h, int cpu_mem, int ntt) {
     if (cpu_mem && ntt < 1) return fail(SFWI_E_ARG, "ntt must be at least 1 step when cpu_mem is set (got %d)", ntt);
     h->cpu_mem = cpu_mem ? 1 : 0;
     h->ntt = cpu_mem ? ntt : 0;
+    return SFWI_OK;
+}
+
+int sfwi_set_pinned_cache(size_t bytes) {
+    PinnedCache &c = pinned_cache();
+    {
+        std::lock_guard<std::mutex> g(c.mu);
+        c.limit = bytes;
+    }
+    c.trim(bytes);
     return SFWI_OK;
 }
 

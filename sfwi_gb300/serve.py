@@ -198,11 +198,13 @@ class Server:
     arrive close together can share it and the shortest-first order sees
     them all.  strip_chunk > 0 keeps every run's edge strips in host memory
     in chunks of that many steps (sfwi_set_cpu_mem): the budget then counts
-    the device ring only, and more requests fit at once."""
+    the device ring only, and more requests fit at once.  During run() the
+    pinned blocks that finished engines release are kept (up to
+    pinned_cache_bytes) for the next engines, and freed when it returns."""
 
     def __init__(self, budget_bytes, max_active=4, runner=None, sizer=None, clock=time.perf_counter,
                  policy="oldest", work=request_work, batch=False, batch_runner=None, batch_sizer=None,
-                 max_batch=64, window=0.0, strip_chunk=0):
+                 max_batch=64, window=0.0, strip_chunk=0, pinned_cache_bytes=64 << 30):
         if policy not in ("oldest", "shortest"):
             raise ValueError("policy must be 'oldest' or 'shortest'")
         self.budget = int(budget_bytes)
@@ -218,10 +220,22 @@ class Server:
         self.batch_sizer = batch_sizer or (lambda g: batch_bytes(g, sc))
         self.max_batch = int(max_batch)
         self.window = float(window)
+        self.strip_chunk = sc
+        self.pinned_cache_bytes = int(pinned_cache_bytes)
 
     def run(self, requests):
         """Replay `requests` (arrival offsets in seconds) against the wall
         clock and serve them; returns the results in request-id order."""
+        if self.strip_chunk <= 0:
+            return self._run(requests)
+        import sfwi_gb300 as sg
+        sg.set_pinned_cache(self.pinned_cache_bytes)
+        try:
+            return self._run(requests)
+        finally:
+            sg.set_pinned_cache(0)
+
+    def _run(self, requests):
         reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
         for r in reqs:
             need = self.batch_sizer([r]) if self.batch else self.sizer(r)

@@ -187,10 +187,14 @@ def test_batched_serving_gives_each_request_its_result_alone():
     host = serve.run_requests(reqs, strip_chunk=37)  # edge strips in host memory
     res = serve.Server(8 << 30, max_active=2, batch=True).run(reqs)
     sjf = serve.Server(8 << 30, max_active=2, batch=True, policy="shortest", max_batch=2, window=0.05).run(reqs)
-    for a, m, h, r, q in zip(alone, mixed, host, res, sjf):
-        assert a[0] == m[0] == h[0] == r.misfit == q.misfit
-        for x, y, u, z, w in zip(a[1:], m[1:], h[1:], (r.grad_pp, r.grad_ps, r.illum), (q.grad_pp, q.grad_ps, q.illum)):
+    # host-held strips with the pinned cache on: engines reuse each other's blocks
+    hsrv = serve.Server(8 << 30, max_active=2, batch=True, max_batch=2, strip_chunk=23).run(reqs)
+    for a, m, h, r, q, k in zip(alone, mixed, host, res, sjf, hsrv):
+        assert a[0] == m[0] == h[0] == r.misfit == q.misfit == k.misfit
+        for x, y, u, z, w, v in zip(a[1:], m[1:], h[1:], (r.grad_pp, r.grad_ps, r.illum),
+                                    (q.grad_pp, q.grad_ps, q.illum), (k.grad_pp, k.grad_ps, k.illum)):
             assert np.array_equal(x, y) and np.array_equal(x, u) and np.array_equal(x, z) and np.array_equal(x, w)
+            assert np.array_equal(x, v)
 
 
 @pytest.mark.gpu

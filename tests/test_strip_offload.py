@@ -10,7 +10,10 @@ density kernel) bit for bit, for chunk lengths that divide nt unevenly
 (7, 64), one that sends a single chunk to the host (149), one whose ring
 would hold every step (150: the strips stay on the device), with the L2 and
 OT misfits, in stages 1 and 2, and over repeated runs on one handle.  The
-device strip bytes shrink to the ring's share: 2 ntt / nt.
+device strip bytes shrink to the ring's share: 2 ntt / nt.  Pinned blocks
+that engines release can be cached and handed to later engines
+(sfwi_set_pinned_cache): a reused block holds another run's strips, which
+the new run overwrites before it reads them.
 """
 import numpy as np
 import pytest
@@ -133,3 +136,19 @@ def test_switching_back_to_device_strips(survey):
     with pytest.raises(sg.SfwiError, match="ntt"):
         fd.set_cpu_mem(1, 0)
     fd.close()
+
+
+def test_reused_pinned_blocks_give_the_same_results(survey):
+    import sfwi_gb300 as sg
+    base1 = _run(survey, 1, 0, 0)[0]
+    base2 = _run(survey, 2, 0, 0)[0]
+    sg.set_pinned_cache(1 << 30)
+    try:
+        # each engine takes the block the one before released, holding that
+        # engine's strips (another stage, another model)
+        runs = [(1, _run(survey, 1, 1, 7)[0]), (2, _run(survey, 2, 1, 7)[0]), (1, _run(survey, 1, 1, 9)[0]),
+                (2, _run(survey, 2, 1, 5)[0])]
+    finally:
+        sg.set_pinned_cache(0)
+    for stage, r in runs:
+        _same_run(r, base1 if stage == 1 else base2)

@@ -490,8 +490,11 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, rank=0, clocks=N
     dev_ms, fwd_ms, bwd_ms, mis_ms = [], [], [], []
     del allreduce_s[:]
     wall0 = time.perf_counter()
+    step_walls = []
     for _ in range(steps):
+        ts = time.perf_counter()
         m, g = step()
+        step_walls.append(time.perf_counter() - ts)
         t = fd.last_timing()
         dev_ms.append(t["total_ms"])
         fwd_ms.append(t["forward_ms"])
@@ -578,7 +581,7 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, rank=0, clocks=N
         for fmt in ("f16", "bf16"):
             snap_err[fmt] = {k: float("%.3g" % rel(grads[fmt][j], grads["f32"][j]))
                              for j, k in enumerate(("grad_vp", "grad_vs", "illum"))}
-    out.update(value=value, e2e=e2e, wall=wall, total_dev_s=total_dev_s, steps=steps, launches=launches, clk=clk,
+    out.update(value=value, e2e=e2e, wall=wall, step_walls_ms=[round(1000.0 * x, 2) for x in step_walls], total_dev_s=total_dev_s, steps=steps, launches=launches, clk=clk,
                allreduce_ms=round(1000.0 * float(np.mean(allreduce_s)), 3) if allreduce_s else None,
                h2d=h2d, d2h=d2h, kt=kt, roof=roof, fracs=fracs, cells=cells, alg_bytes_step=alg_bytes_step,
                kernel_bytes=kernel_bytes, plain=plain, snap_err=snap_err, tile=fd.tile_shape(),
@@ -711,7 +714,8 @@ def main():
                        "alg_GBps_whole_step_kernel_accounting": (
                            round(r["kernel_bytes"] * r["cells"] * nt / (total_dev_s / steps) / 1e9, 1)
                            if r["kernel_bytes"] else None)},
-            "e2e": {"value": round(r["e2e"], 3), "unit": "shot-gradients/s", "h2d_bytes_per_step": r["h2d"],
+            "e2e": {"value": round(r["e2e"], 3), "unit": "shot-gradients/s", "wall_ms_per_step": r["step_walls_ms"],
+                    "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"], "roofline": r["roof"], "cpu_baseline": cpu, "clocks": r["clk"],
             "plain": r["plain"], "serving": serving, "snapshot_error": r["snap_err"], "reference_gpu": ref_gpu,

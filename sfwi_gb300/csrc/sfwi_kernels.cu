@@ -77,6 +77,24 @@ constexpr float K4 = (float)(-5.0 / 7168.0);
 // early release (all inputs in registers before the arithmetic) still lets
 // the next tile's loads overlap this tile's arithmetic
 constexpr int NSTAGE = SFWI_STAGES;
+constexpr size_t SMEM_ALIGN_SLACK = 1024;
+// dynamic shared memory of a kernel with nst stages of `stage` floats
+constexpr size_t stage_bytes(int stage, int nst) { return (size_t)nst * stage * sizeof(float) + SMEM_ALIGN_SLACK; }
+// CTAS_PER_SM CTAs of that kernel fit the SM's 228 KB of shared memory (227
+// KB at most per CTA, 1 KB of it reserved per resident CTA; `extra` bytes of
+// static shared memory per CTA)
+constexpr bool fits_stages(int stage, int nst, size_t extra) {
+    return stage_bytes(stage, nst) + extra <= 227 * 1024 &&
+           CTAS_PER_SM * (stage_bytes(stage, nst) + extra + 1024) <= 228 * 1024;
+}
+// the most stages from NSTAGE up to `most` that still fit: kernels with
+// small stages keep more tiles in flight
+constexpr int deep_stages(int stage, int most, size_t extra) {
+    int n = NSTAGE;
+    for (int k = NSTAGE + 1; k <= most; k++)
+        if (fits_stages(stage, k, extra)) n = k;
+    return n;
+}
 constexpr int CORE = TX * TZ;  // floats of a core tile
 constexpr uint32_t BOX_BYTES = BOX * 4u, CORE_BYTES = CORE * 4u;
 
@@ -616,16 +634,16 @@ struct StageRelease {
     }
 };
 
-template <int STAGE_FLOATS, class Issue, class Body>
+template <int STAGE_FLOATS, int NST, class Issue, class Body>
 __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue issue, Body body, int kid) {
     const bool reverse = (p.reverse_tiles >> kid) & 1;
-    __shared__ uint64_t full[NSTAGE], empty[NSTAGE];
-    __shared__ TileCtx s_ctx[NSTAGE];
-    __shared__ int s_tile[NSTAGE];
+    __shared__ uint64_t full[NST], empty[NST];
+    __shared__ TileCtx s_ctx[NST];
+    __shared__ int s_tile[NST];
     float *sm = smem_base();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; s++) {
+        for (int s = 0; s < NST; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], NTHREADS);
         }
@@ -647,8 +665,8 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
         if (t < p.ntiles) ctx = tile_ctx(p, reverse ? p.ntiles - 1 - t : t);
         griddep_wait();
         for (int k = 0;; k++) {
-            const int s = k % NSTAGE;
-            if (k >= NSTAGE && !mbar_wait(&empty[s], (uint32_t)((k / NSTAGE - 1) & 1), p.wait_limit)) {
+            const int s = k % NST;
+            if (k >= NST && !mbar_wait(&empty[s], (uint32_t)((k / NST - 1) & 1), p.wait_limit)) {
                 atomicExch(p.err, 2);
                 return;  // consumers give up on full[s] the same way
             }
@@ -669,13 +687,14 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
     }
     griddep_wait();
     for (int k = 0;; k++) {
-        const int s = k % NSTAGE;
-        const bool ok = mbar_wait(&full[s], (uint32_t)((k / NSTAGE) & 1), p.wait_limit);
+        const int s = k % NST;
+        const bool ok = mbar_wait(&full[s], (uint32_t)((k / NST) & 1), p.wait_limit);
         if (consumer_any(!ok)) {
             if (threadIdx.x == 0) {
                 atomicExch(p.err, 1);
-                // the other stage may still be loading: let it land (bounded)
-                if (NSTAGE > 1) mbar_wait(&full[(k + 1) % NSTAGE], (uint32_t)(((k + 1) / NSTAGE) & 1), p.wait_limit);
+                // the other stages may still be loading: let them land (bounded)
+                for (int j = 1; j < NST; j++)
+                    mbar_wait(&full[(k + j) % NST], (uint32_t)(((k + j) / NST) & 1), p.wait_limit);
             }
             return;
         }
@@ -690,9 +709,10 @@ __device__ __forceinline__ void run_tiles(const Params &p, int *counter, Issue i
 // ---------------------------------------------------------------------------
 // forward snapshots
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool snap_step(const Params &p, int it) {
+__host__ __device__ __forceinline__ bool snap_step(const Params &p, int it) {
     return p.snap != nullptr && it % p.snap_every == 0;
 }
+inline bool snap_step_host(const Params &p, int it) { return snap_step(p, it); }
 // per-shot scales of snapshot k into shared memory (every thread of the CTA
 // takes part; ends with __syncthreads)
 __device__ __forceinline__ void load_snap_scales(const Params &p, int k, float *s_sc) {
@@ -740,6 +760,7 @@ struct FwdV {
     // core slots: 0 ib, 1 vx, 2 vz, 3 dampx, 4 dampz, 5 mvx, 6 mvz, [7 svx, 8 svz, 9 smvx, 10 smvz]
     static constexpr int NC = BORN ? 11 : 7;
     static constexpr int STAGE = NB * BOX + NC * CORE;
+    static constexpr int NST = NSTAGE;
 };
 
 template <bool BORN>
@@ -848,7 +869,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             }
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 0, issue, body, 0);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 0, issue, body, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -861,6 +882,7 @@ struct FwdS {
     //       [10 bp, 11 bs, 12 stxx, 13 stzz, 14 stxz, 15 smtxx, 16 smtzz, 17 smtxz]
     static constexpr int NC = BORN ? 18 : 10;
     static constexpr int STAGE = NB * BOX + NC * CORE;
+    static constexpr int NST = NSTAGE;
 };
 
 template <bool BORN>
@@ -1041,7 +1063,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         griddep_wait();  // the scales come from the velocity sweep just before
         load_snap_scales(p, it / p.snap_every, s_sc);
     }
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 1, issue, body, 1);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 1, issue, body, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1133,6 +1155,7 @@ struct BwdS {
     static constexpr int STRIPS = NB * BOX + NC * CORE;
     static constexpr int RS = STRIPS + 2 * TBF + 2 * LRF;
     static constexpr int STAGE = RS + RSF;
+    static constexpr int NST = NSTAGE;
 };
 // every TMA destination of a stage starts on a 128-byte boundary
 static_assert((BOX * 4) % 128 == 0 && (CORE * 4) % 128 == 0, "box/core alignment");
@@ -1326,7 +1349,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             stc(p.gmu + m.gi, gm);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body, 2);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 2, issue, body, 2);
 }
 
 // Lame-weighted adjoint stresses of a staged box, in place (consumers):
@@ -1361,6 +1384,7 @@ struct BwdV {
     // core: 0 ib, 1 vx, 2 vz, 3 avx, 4 avz, 5 dampx, 6 dampz, 7 mvx, 8 mvz, 9 amvx, 10 amvz, 11 illum
     static constexpr int NC = 12;
     static constexpr int STAGE = NB * BOX + NC * CORE;
+    static constexpr int NST = NSTAGE;
 };
 
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
@@ -1468,7 +1492,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             stc(p.grho + m.gi, gr);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body, 3);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 3, issue, body, 3);
 }
 
 // ---------------------------------------------------------------------------
@@ -1479,23 +1503,27 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
 // halo, decompressed in shared memory) with the reconstruction's stencils,
 // weighted by the snapshot interval, and the illumination from the
 // snapshot's own cells.  k_bwd_v_snap: the adjoint velocity update only.
-template <int FMT>
+// IMG: a snapshot step (imaging); the other steps' stages hold no snapshot
+// boxes or accumulators, so those launches keep more tiles in flight
+template <int FMT, bool IMG>
 struct BwdSSnap {
     static constexpr int NB = 2;  // adjoint vx, vz
-    // core: 0 atxx, 1 atzz, 2 atxz, 3 dampx, 4 dampz, 5 amtxz, 6 glam, 7 gmu, 8 illum
-    static constexpr int NC = 9;
-    static constexpr int SNAPF = NB * BOX + NC * CORE;  // snapshot vx, vz boxes as floats
-    static constexpr int RAW = SNAPF + 2 * BOX;         // 16-bit snapshot boxes as loaded
-    static constexpr int RS = RAW + (FMT == SNAP_F32 ? 0 : BOX);
+    // core: 0 atxx, 1 atzz, 2 atxz, 3 dampx, 4 dampz, 5 amtxz, [6 glam, 7 gmu, 8 illum]
+    static constexpr int NC = IMG ? 9 : 6;
+    static constexpr int SNAPF = NB * BOX + NC * CORE;         // snapshot vx, vz boxes as floats
+    static constexpr int RAW = SNAPF + (IMG ? 2 * BOX : 0);    // 16-bit snapshot boxes as loaded
+    static constexpr int RS = RAW + (IMG && FMT != SNAP_F32 ? BOX : 0);
     static constexpr int STAGE = RS + BX * 4;
+    static constexpr int NST = IMG ? NSTAGE : deep_stages(STAGE, NSTAGE + 2, 8192);
 };
 
-template <int FMT>
+// launched with IMG = snap_step(p, it)
+template <int FMT, bool IMG>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_s_snap(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
-    using S = BwdSSnap<FMT>;
-    __shared__ float s_sc[2 * SNAP_MAX_SHOTS];
-    const bool sstep = snap_step(p, it);
+    using S = BwdSSnap<FMT, IMG>;
+    __shared__ float s_sc[IMG ? 2 * SNAP_MAX_SHOTS : 1];
+    const bool sstep = IMG;
     const int k = it / p.snap_every;
     const float w = (float)p.snap_every;
     auto issue = [&](const TileCtx &c, float *s, uint64_t *bar) {
@@ -1573,11 +1601,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             stc(p.illum + m.gi, il);
         }
     };
-    if (sstep && FMT != SNAP_F32) {
+    if (IMG && FMT != SNAP_F32) {
         griddep_wait();
         load_snap_scales(p, k, s_sc);
     }
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 2, issue, body, 2);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 2, issue, body, 2);
 }
 
 struct BwdVSnap {
@@ -1585,6 +1613,7 @@ struct BwdVSnap {
     // core: 0 ib, 1 avx, 2 avz, 3 dampx, 4 dampz, 5 amvx, 6 amvz
     static constexpr int NC = 7;
     static constexpr int STAGE = NB * BOX + NC * CORE;
+    static constexpr int NST = deep_stages(STAGE, NSTAGE + 1, 1024);
 };
 
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
@@ -1637,7 +1666,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.ad, ad, ib, dm, adj_dir, aax, abz, adx, acz);
         }
     };
-    run_tiles<S::STAGE>(p, p.counters + 4 * it + 3, issue, body, 3);
+    run_tiles<S::STAGE, S::NST>(p, p.counters + 4 * it + 3, issue, body, 3);
 }
 
 // ---------------------------------------------------------------------------
@@ -1652,26 +1681,21 @@ constexpr int PROBE_STAGE = 32;
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM) k_wait_probe(const Params p) {
     auto issue = [&](const TileCtx &, float *, uint64_t *) {};
     auto body = [&](const TileCtx &, float *, StageRelease &) {};
-    run_tiles<PROBE_STAGE>(p, p.counters, issue, body, 0);
+    run_tiles<PROBE_STAGE, NSTAGE>(p, p.counters, issue, body, 0);
 }
 
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
-constexpr size_t SMEM_ALIGN_SLACK = 1024;
-template <int STAGE>
+template <class S>
 constexpr size_t stage_smem() {
-    return (size_t)NSTAGE * STAGE * sizeof(float) + SMEM_ALIGN_SLACK;
+    return stage_bytes(S::STAGE, S::NST);
 }
-
-// CTAS_PER_SM CTAs of the largest kernel must fit the SM's 228 KB of shared
-// memory (227 KB at most per CTA, 1 KB of it reserved per resident CTA)
-template <int STAGE>
-constexpr bool fits_sm() {
-    return stage_smem<STAGE>() <= 227 * 1024 && CTAS_PER_SM * (stage_smem<STAGE>() + 1024) <= 228 * 1024;
-}
-static_assert(fits_sm<FwdV<true>::STAGE>() && fits_sm<FwdS<true>::STAGE>() && fits_sm<BwdS::STAGE>() &&
-                  fits_sm<BwdV::STAGE>() && fits_sm<BwdSSnap<SNAP_F32>::STAGE>() && fits_sm<BwdVSnap::STAGE>(),
+static_assert(fits_stages(FwdV<true>::STAGE, FwdV<true>::NST, 1024) && fits_stages(FwdS<true>::STAGE, FwdS<true>::NST, 1024) &&
+                  fits_stages(BwdS::STAGE, BwdS::NST, 1024) && fits_stages(BwdV::STAGE, BwdV::NST, 1024) &&
+                  fits_stages(BwdSSnap<SNAP_F32, true>::STAGE, BwdSSnap<SNAP_F32, true>::NST, 8192) &&
+                  fits_stages(BwdSSnap<SNAP_F16, true>::STAGE, BwdSSnap<SNAP_F16, true>::NST, 8192) &&
+                  fits_stages(BwdVSnap::STAGE, BwdVSnap::NST, 1024),
               "tile shape too large for CTAS_PER_SM resident CTAs");
 
 int g_nsm = 0;
@@ -1680,16 +1704,19 @@ cudaError_t configure_step_kernels() {
     cudaError_t e;
 #define SET_SMEM(K, BYTES) \
     if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(BYTES))) != cudaSuccess) return e;
-    SET_SMEM(k_fwd_v<true>, stage_smem<FwdV<true>::STAGE>());
-    SET_SMEM(k_fwd_v<false>, stage_smem<FwdV<false>::STAGE>());
-    SET_SMEM(k_fwd_s<true>, stage_smem<FwdS<true>::STAGE>());
-    SET_SMEM(k_fwd_s<false>, stage_smem<FwdS<false>::STAGE>());
-    SET_SMEM(k_bwd_s, stage_smem<BwdS::STAGE>());
-    SET_SMEM(k_bwd_v, stage_smem<BwdV::STAGE>());
-    SET_SMEM(k_bwd_s_snap<SNAP_F32>, stage_smem<BwdSSnap<SNAP_F32>::STAGE>());
-    SET_SMEM(k_bwd_s_snap<SNAP_F16>, stage_smem<BwdSSnap<SNAP_F16>::STAGE>());
-    SET_SMEM(k_bwd_s_snap<SNAP_BF16>, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>());
-    SET_SMEM(k_bwd_v_snap, stage_smem<BwdVSnap::STAGE>());
+    SET_SMEM(k_fwd_v<true>, stage_smem<FwdV<true>>());
+    SET_SMEM(k_fwd_v<false>, stage_smem<FwdV<false>>());
+    SET_SMEM(k_fwd_s<true>, stage_smem<FwdS<true>>());
+    SET_SMEM(k_fwd_s<false>, stage_smem<FwdS<false>>());
+    SET_SMEM(k_bwd_s, stage_smem<BwdS>());
+    SET_SMEM(k_bwd_v, stage_smem<BwdV>());
+    SET_SMEM((k_bwd_s_snap<SNAP_F32, true>), (stage_smem<BwdSSnap<SNAP_F32, true>>()));
+    SET_SMEM((k_bwd_s_snap<SNAP_F16, true>), (stage_smem<BwdSSnap<SNAP_F16, true>>()));
+    SET_SMEM((k_bwd_s_snap<SNAP_BF16, true>), (stage_smem<BwdSSnap<SNAP_BF16, true>>()));
+    SET_SMEM((k_bwd_s_snap<SNAP_F32, false>), (stage_smem<BwdSSnap<SNAP_F32, false>>()));
+    SET_SMEM((k_bwd_s_snap<SNAP_F16, false>), (stage_smem<BwdSSnap<SNAP_F16, false>>()));
+    SET_SMEM((k_bwd_s_snap<SNAP_BF16, false>), (stage_smem<BwdSSnap<SNAP_BF16, false>>()));
+    SET_SMEM(k_bwd_v_snap, stage_smem<BwdVSnap>());
 #undef SET_SMEM
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -1720,7 +1747,16 @@ static void launch_step(void (*k)(KArgs...), size_t smem, const Params &p, cudaS
 // one CTA; with p.ntiles >= 4 its producer draws real tiles (it reads their
 // records) until it waits for a free stage
 void launch_wait_probe(const Params &p, cudaStream_t st) {
-    k_wait_probe<<<1, BLOCK_THREADS, NSTAGE * PROBE_STAGE * sizeof(float) + SMEM_ALIGN_SLACK, st>>>(p);
+    k_wait_probe<<<1, BLOCK_THREADS, stage_bytes(PROBE_STAGE, NSTAGE), st>>>(p);
+}
+
+// the snapshot-mode adjoint stress sweep: the imaging form at snapshot steps
+template <int FMT>
+static void launch_bwd_s_snap(const Params &p, const TmaMaps &tm, int it, float adj_dir, cudaStream_t st) {
+    if (snap_step_host(p, it))
+        launch_step(k_bwd_s_snap<FMT, true>, stage_smem<BwdSSnap<FMT, true>>(), p, st, tm, it, adj_dir);
+    else
+        launch_step(k_bwd_s_snap<FMT, false>, stage_smem<BwdSSnap<FMT, false>>(), p, st, tm, it, adj_dir);
 }
 
 void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, bool born, float adj_dir,
@@ -1728,32 +1764,31 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
     switch (which) {
         case 0:
             if (born)
-                launch_step(k_fwd_v<true>, stage_smem<FwdV<true>::STAGE>(), p, st, tm, it);
+                launch_step(k_fwd_v<true>, stage_smem<FwdV<true>>(), p, st, tm, it);
             else
-                launch_step(k_fwd_v<false>, stage_smem<FwdV<false>::STAGE>(), p, st, tm, it);
+                launch_step(k_fwd_v<false>, stage_smem<FwdV<false>>(), p, st, tm, it);
             break;
         case 1:
             if (born)
-                launch_step(k_fwd_s<true>, stage_smem<FwdS<true>::STAGE>(), p, st, tm, it);
+                launch_step(k_fwd_s<true>, stage_smem<FwdS<true>>(), p, st, tm, it);
             else
-                launch_step(k_fwd_s<false>, stage_smem<FwdS<false>::STAGE>(), p, st, tm, it);
+                launch_step(k_fwd_s<false>, stage_smem<FwdS<false>>(), p, st, tm, it);
             break;
         case 2:
             if (!p.snap)
-                launch_step(k_bwd_s, stage_smem<BwdS::STAGE>(), p, st, tm, it, adj_dir);
+                launch_step(k_bwd_s, stage_smem<BwdS>(), p, st, tm, it, adj_dir);
             else if (p.snap_fmt == SNAP_F32)
-                launch_step(k_bwd_s_snap<SNAP_F32>, stage_smem<BwdSSnap<SNAP_F32>::STAGE>(), p, st, tm, it, adj_dir);
+                launch_bwd_s_snap<SNAP_F32>(p, tm, it, adj_dir, st);
             else if (p.snap_fmt == SNAP_F16)
-                launch_step(k_bwd_s_snap<SNAP_F16>, stage_smem<BwdSSnap<SNAP_F16>::STAGE>(), p, st, tm, it, adj_dir);
+                launch_bwd_s_snap<SNAP_F16>(p, tm, it, adj_dir, st);
             else
-                launch_step(k_bwd_s_snap<SNAP_BF16>, stage_smem<BwdSSnap<SNAP_BF16>::STAGE>(), p, st, tm, it,
-                            adj_dir);
+                launch_bwd_s_snap<SNAP_BF16>(p, tm, it, adj_dir, st);
             break;
         default:
             if (!p.snap)
-                launch_step(k_bwd_v, stage_smem<BwdV::STAGE>(), p, st, tm, it, adj_dir);
+                launch_step(k_bwd_v, stage_smem<BwdV>(), p, st, tm, it, adj_dir);
             else
-                launch_step(k_bwd_v_snap, stage_smem<BwdVSnap::STAGE>(), p, st, tm, it, adj_dir);
+                launch_step(k_bwd_v_snap, stage_smem<BwdVSnap>(), p, st, tm, it, adj_dir);
             break;
     }
 }

@@ -760,7 +760,8 @@ struct FwdV {
     // core slots: 0 ib, 1 vx, 2 vz, 3 dampx, 4 dampz, 5 mvx, 6 mvz, [7 svx, 8 svz, 9 smvx, 10 smvz]
     static constexpr int NC = BORN ? 11 : 7;
     static constexpr int STAGE = NB * BOX + NC * CORE;
-    static constexpr int NST = NSTAGE;
+    // without the scattered field the stage is small enough for more stages
+    static constexpr int NST = BORN ? NSTAGE : deep_stages(STAGE, NSTAGE + 2, 1024);
 };
 
 template <bool BORN>
@@ -882,7 +883,7 @@ struct FwdS {
     //       [10 bp, 11 bs, 12 stxx, 13 stzz, 14 stxz, 15 smtxx, 16 smtzz, 17 smtxz]
     static constexpr int NC = BORN ? 18 : 10;
     static constexpr int STAGE = NB * BOX + NC * CORE;
-    static constexpr int NST = NSTAGE;
+    static constexpr int NST = BORN ? NSTAGE : deep_stages(STAGE, NSTAGE + 2, 5120);  // + s_sc
 };
 
 template <bool BORN>

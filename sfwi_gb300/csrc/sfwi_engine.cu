@@ -291,6 +291,12 @@ struct sfwi_handle {
     // back during the backward sweeps, copied on a second stream while the
     // step kernels run
     int cpu_mem = 0, ntt = 0;
+    // observed records go to the device on their own stream while the
+    // forward sweeps run (they are first read by the misfit); obs_pending:
+    // copies issued that the run's stream has not waited for yet
+    cudaStream_t os = nullptr;
+    cudaEvent_t ev_obs_fork = nullptr, ev_obs = nullptr;
+    bool obs_pending = false;
     cudaStream_t cs = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_copy[2] = {nullptr, nullptr};
     HostBuf<float> htb, hlr;
@@ -824,8 +830,13 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(cudaMemsetAsync(b.grid.p, 0, (size_t)NSTATE * b.cells * sizeof(float), st));
     CK(cudaMemsetAsync(b.recs.p, 0, recs * sizeof(float), st));
     // observed records, trace-major ([ntr][its nt] on the host; a shot with
-    // fewer steps than the batch keeps zeros after its last sample)
+    // fewer steps than the batch keeps zeros after its last sample), copied
+    // on the records stream after the zeroing above; the run's stream waits
+    // for them before the misfit (wait_observed)
     if (with_obs) {
+        CK(cudaEventRecord(h->ev_obs_fork, st));
+        CK(cudaStreamWaitEvent(h->os, h->ev_obs_fork, 0));
+        h->obs_pending = true;
         for (size_t s = 0; s < shots.size(); s++) {
             const ShotIn &in = shots[s];
             const int ns = b.aux[s].nt;
@@ -836,12 +847,13 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
             for (int c = 0; c < 2; c++) {
                 if (!src[c]) continue;
                 if (ns == nt)
-                    CK(cudaMemcpyAsync(dst[c], src[c], n * sizeof(float), cudaMemcpyHostToDevice, st));
+                    CK(cudaMemcpyAsync(dst[c], src[c], n * sizeof(float), cudaMemcpyHostToDevice, h->os));
                 else
                     CK(cudaMemcpy2DAsync(dst[c], (size_t)nt * sizeof(float), src[c], (size_t)ns * sizeof(float),
-                                         (size_t)ns * sizeof(float), in.ntr, cudaMemcpyHostToDevice, st));
+                                         (size_t)ns * sizeof(float), in.ntr, cudaMemcpyHostToDevice, h->os));
             }
         }
+        CK(cudaEventRecord(h->ev_obs, h->os));
     }
     SetupArgs a{};
     a.X = b.X;
@@ -884,17 +896,30 @@ int upload_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, bool forward_
     CK(cudaEventRecord(h->ev[4], st));
     launch_setup(a, b.nshots, b.max_nxpml, st);
     h->launches++;
-    // OT scales: max|obs| per trace and component, floored at a fraction of
-    // the shot's largest (a trace without signal must not blow the transform
-    // up), or the shot's largest for every trace
-    if (with_obs && h->misfit_kind != SFWI_MISFIT_L2 && b.ntr_tot) {
-        launch_ot_scales(b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), nt, b.ntr_tot, b.dgeo.p, b.nshots,
-                         h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE, b.dsigma.p, st);
-        h->launches += 2;
-    }
     CK(cudaGetLastError());
     return SFWI_OK;
 }
+
+// The run's stream waits for the observed records issued by upload_batch.
+int wait_observed(sfwi_handle *h) {
+    if (h->obs_pending) {
+        CK(cudaStreamWaitEvent(h->st, h->ev_obs, 0));
+        h->obs_pending = false;
+    }
+    return SFWI_OK;
+}
+
+// A run that ends early (an error) must not leave a copy reading the
+// caller's host records behind it.
+struct ObservedGuard {
+    sfwi_handle *h;
+    ~ObservedGuard() {
+        if (h->obs_pending) {
+            cudaStreamSynchronize(h->os);
+            h->obs_pending = false;
+        }
+    }
+};
 
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
@@ -1072,6 +1097,7 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
     if (rc) return rc;
     if (!h->b.tlen.empty() && ((mode != RUN_FORWARD && misfit_kind != SFWI_MISFIT_L2) || h->snap_every > 0))
         return fail(SFWI_E_ARG, "shots of different lengths in one run take the L2 misfit and no snapshots");
+    ObservedGuard obs_guard{h};
     rc = upload_batch(h, shots, forward_only, mode != RUN_FORWARD);
     if (rc) return rc;
     Batch &b = h->b;
@@ -1118,8 +1144,17 @@ int run_batch(sfwi_handle *h, const std::vector<ShotIn> &shots, int mode, double
         h->other_ms = 0.f;
         return SFWI_OK;
     }
-    // adjoint source and misfit
+    // adjoint source and misfit, once the observed records are in
     nvtxMarkA("sfwi misfit");
+    if ((rc = wait_observed(h))) return rc;
+    // OT scales: max|obs| per trace and component, floored at a fraction of
+    // the shot's largest (a trace without signal must not blow the transform
+    // up), or the shot's largest for every trace
+    if (misfit_kind != SFWI_MISFIT_L2 && b.ntr_tot) {
+        launch_ot_scales(b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), nt, b.ntr_tot, b.dgeo.p, b.nshots,
+                         h->misfit_kind == SFWI_MISFIT_OT_ALLTRACE, b.dsigma.p, st);
+        h->launches += 2;
+    }
     if (misfit_kind == SFWI_MISFIT_L2) {
         launch_residual_l2(h->stage, nt, b.ntr_tot, b.r(R_SYN_Z, nt), b.r(R_SYN_X, nt), b.r(R_SYN2_Z, nt),
                            b.r(R_SYN2_X, nt), b.r(R_OBS_Z, nt), b.r(R_OBS_X, nt), b.r(R_RES_Z, nt), b.r(R_RES_X, nt),
@@ -1382,6 +1417,7 @@ int born_adjoint(sfwi_handle *h, const std::vector<ShotIn> &q, double *img_vp, d
     h->b.ready = false;
     h->last_perm.clear();
     if (int rc = build_batch(h, q)) return rc;
+    ObservedGuard obs_guard{h};
     if (int rc = upload_batch(h, q, false, true)) return rc;
     Batch &b = h->b;
     b.ready = true;
@@ -1452,6 +1488,7 @@ int born_adjoint(sfwi_handle *h, const std::vector<ShotIn> &q, double *img_vp, d
     a.snap = reinterpret_cast<const float *>(b.snap.p);
     a.dz = b.r(R_OBS_Z, nt);
     a.dx = b.r(R_OBS_X, nt);
+    if (int rc = wait_observed(h)) return rc;  // the records to back-propagate
     CK(cudaEventRecord(h->ev[2], st));
     for (int it = nt - 1; it >= 0; it--) launch_adjoint_step(a, it, st);
     h->launches += 3LL * nt;
@@ -1651,6 +1688,12 @@ int sfwi_create(sfwi_handle **out, int stage, const float *sou, float dx, float 
                 break;
             }
         if (rc) break;
+        if ((e = cudaStreamCreateWithFlags(&h->os, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&h->ev_obs_fork, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&h->ev_obs, cudaEventDisableTiming)) != cudaSuccess) {
+            rc = fail(SFWI_E_CUDA, "records stream: %s", cudaGetErrorString(e));
+            break;
+        }
         if ((rc = upload_model(h->sou, sou, nt))) break;
         rc = ensure_grads(h);
     } while (0);
@@ -1670,6 +1713,7 @@ int sfwi_destroy(sfwi_handle *h) {
     for_each_buf(h, [](auto &d) { d.release(); });
     if (h->st) cudaStreamSynchronize(h->st);  // the stream-ordered frees
     if (h->cs) cudaStreamSynchronize(h->cs);
+    if (h->os) cudaStreamSynchronize(h->os);
     h->htb.release();
     h->hlr.release();
     for (auto &ev : h->ev)
@@ -1678,6 +1722,9 @@ int sfwi_destroy(sfwi_handle *h) {
     for (auto &ev : h->ev_copy)
         if (ev) cudaEventDestroy(ev);
     if (h->cs) cudaStreamDestroy(h->cs);
+    if (h->ev_obs_fork) cudaEventDestroy(h->ev_obs_fork);
+    if (h->ev_obs) cudaEventDestroy(h->ev_obs);
+    if (h->os) cudaStreamDestroy(h->os);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return SFWI_OK;

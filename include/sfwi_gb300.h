@@ -181,6 +181,16 @@ int sfwi_run_forward(sfwi_handle *h);
  * background velocities of every step, plus 88 bytes per packed cell.
  * Clears the queue. */
 int sfwi_born_adjoint(sfwi_handle *h, double *img_vp, double *img_vs);
+/* Gauss-Newton Hessian-vector product of the queued shots (stage 2):
+ * hv_vp, hv_vs (host [allnx][allnz], FP64) += L^T L m for m = (dvp, dvs)
+ * (host [allnx][allnz]), the counterpart of ELSRTM_CALCULATE_Hessian_vector
+ * (sfwi-stage1/FD2DGPU.cuh:477-478, FD2DGPU.cu:5236-5379: a Born forward of
+ * the vector, its scattered records propagated back and imaged) with the
+ * exact adjoint above, so the product is symmetric and <m, H m> = |L m|^2.
+ * It is sfwi_gpu_buffer_m(h, dvp, dvs), sfwi_run_forward, and
+ * sfwi_born_adjoint of the scattered records: the uploaded perturbation is
+ * replaced by m.  Shots run the handle's nt.  Clears the queue. */
+int sfwi_hessian_vector(sfwi_handle *h, const float *dvp, const float *dvs, double *hv_vp, double *hv_vs);
 
 /* ---- shots on several models in one run (request batching) ----
  * No reference counterpart: the reference runs one model per MPI job.  Each

@@ -217,6 +217,21 @@ class FD2DGPU_ELASTIC:
             self._keep = []
         return ip, isv
 
+    def hessian_vector(self, dvp, dvs):
+        """Gauss-Newton Hessian-vector product L^T L m of the queued shots for
+        m = (dvp, dvs) (stage 2; replaces the uploaded perturbation):
+        (hv_vp, hv_vs) float64 [allnx, allnz]."""
+        shp = (self.allnx, self.allnz)
+        dvp, dvs = _f32(dvp, shp), _f32(dvs, shp)
+        hp, hs = np.zeros(shp, np.float64), np.zeros(shp, np.float64)
+        dp = C.POINTER(C.c_double)
+        try:
+            _lib.check(_lib.load().sfwi_hessian_vector(self._h, _fp(dvp), _fp(dvs), hp.ctypes.data_as(dp),
+                                                       hs.ctypes.data_as(dp)))
+        finally:
+            self._keep = []
+        return hp, hs
+
     def run_models(self, models, shot_model):
         """One gradient run of the queued shots, shot i on models[shot_model[i]]
         (sfwi_run_models).  `models` are dicts with vp, vs, rho (stage 1),

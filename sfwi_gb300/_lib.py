@@ -50,6 +50,7 @@ SIGNATURES = {
     "sfwi_run": (C.c_int, [_h, _dp, _dp]),
     "sfwi_run_forward": (C.c_int, [_h]),
     "sfwi_born_adjoint": (C.c_int, [_h, _dp, _dp]),
+    "sfwi_hessian_vector": (C.c_int, [_h, _fp, _fp, _dp, _dp]),
     "sfwi_run_models": (C.c_int, [_h, C.c_int, C.POINTER(ModelDesc), _ip, _dp, _dp, _dp, _dp, _dp]),
     "sfwi_calculate_alpha_parabola_mb": (C.c_int, [_h, _fp, _fp, C.c_float, C.c_float, _dp, _dp, _dp]),
     "sfwi_calculate_alpha": (C.c_int, [_h, _fp, _fp, _fp, _fp, _dp, _dp]),

@@ -2087,6 +2087,33 @@ int sfwi_born_adjoint(sfwi_handle *h, double *img_vp, double *img_vs) {
     return born_adjoint(h, q, img_vp, img_vs);
 }
 
+int sfwi_hessian_vector(sfwi_handle *h, const float *dvp, const float *dvs, double *hv_vp, double *hv_vs) {
+    if (int rc = check(h)) return rc;
+    if (h->stage != 2) return fail(SFWI_E_STATE, "the Born operator belongs to stage 2");
+    if (!dvp || !dvs || !hv_vp || !hv_vs) return fail(SFWI_E_ARG, "null argument");
+    std::vector<ShotIn> q;
+    q.swap(h->queue);
+    if (q.empty()) return fail(SFWI_E_ARG, "no shots queued");
+    for (const ShotIn &in : q)
+        if (in.nt > 0 && in.nt != h->nt) return fail(SFWI_E_ARG, "Hessian-vector products run the handle's nt");
+    // L m: the scattered records of every queued shot
+    if (int rc = sfwi_gpu_buffer_m(h, dvp, dvs)) return rc;
+    if (int rc = run_batch(h, q, RUN_FORWARD, nullptr, nullptr)) return rc;
+    std::vector<std::vector<float>> rec(2 * q.size());
+    for (size_t i = 0; i < q.size(); i++) {
+        const size_t n = std::max<size_t>((size_t)q[i].ntr * h->nt, 1);
+        rec[2 * i].resize(n);
+        rec[2 * i + 1].resize(n);
+        if (int rc = sfwi_read_records(h, (int)i, rec[2 * i].data(), rec[2 * i + 1].data(), nullptr, nullptr, nullptr,
+                                       nullptr))
+            return rc;
+        q[i].obs_z = rec[2 * i].data();
+        q[i].obs_x = rec[2 * i + 1].data();
+    }
+    // L^T (L m)
+    return born_adjoint(h, q, hv_vp, hv_vs);
+}
+
 int sfwi_run_forward(sfwi_handle *h) {
     if (int rc = check(h)) return rc;
     std::vector<ShotIn> q;

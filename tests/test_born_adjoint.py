@@ -14,6 +14,9 @@ with d = L m (no cancellation) the two sides agree within 1e-5 relative;
 with random data within 1e-4 of |L m| |d| (the Cauchy-Schwarz scale).  The
 adjoint is linear and additive over shots: L^T of a batch is the sum of the
 shots' L^T (to the rounding of the FP64 sums), and L^T (2 d) = 2 L^T d.
+The Gauss-Newton Hessian-vector product sfwi_hessian_vector is L^T L m:
+the same bits as the adjoint of the forward records, symmetric
+(<m2, H m1> = <H m2, m1>) and <m, H m> = |L m|^2, both within 1e-5.
 """
 import numpy as np
 import pytest
@@ -119,3 +122,38 @@ def test_adjoint_is_additive_over_shots_and_linear(setup):
     twice = _adjoint(s, [(2 * z, 2 * x) for z, x in d], s["shots"])
     for j in range(2):
         assert np.allclose(twice[j], 2 * both[j], rtol=1e-6, atol=1e-6 * np.abs(both[j]).max())
+
+
+def _hessian(s, m, shots):
+    fd = _engine(s)
+    for d in shots:
+        _enqueue(fd, d)
+    out = fd.hessian_vector(*m)
+    fd.close()
+    return out
+
+
+def test_hessian_vector_is_the_adjoint_of_the_forward_records(setup):
+    s = setup
+    hv = _hessian(s, s["m"], s["shots"])
+    ref = _adjoint(s, _forward(s, s["m"], s["shots"]), s["shots"])
+    for a, b in zip(hv, ref):
+        assert np.array_equal(a, b)
+    assert np.abs(hv[0]).max() > 0
+
+
+def test_hessian_vector_is_symmetric_and_positive(setup):
+    s = setup
+    rng = np.random.default_rng(31)
+    m2 = ((rng.standard_normal((ALLNX, ALLNZ)) * 30.0).astype(np.float32),
+          (rng.standard_normal((ALLNX, ALLNZ)) * 20.0).astype(np.float32))
+    h1 = _hessian(s, s["m"], s["shots"])
+    h2 = _hessian(s, m2, s["shots"])
+    a, b = _dot_model(m2, h1), _dot_model(s["m"], h2)
+    scale = np.sqrt(_dot_model(s["m"], h1) * _dot_model(m2, h2))
+    print("<m2, H m1> = %.9e, <H m2, m1> = %.9e, rel %.2e" % (a, b, abs(a - b) / scale))
+    assert abs(a - b) <= 1e-5 * scale
+    lm = _forward(s, s["m"], s["shots"])
+    q = _dot_model(s["m"], h1)
+    assert q > 0
+    assert abs(q - _dot_records(lm, lm)) <= 1e-5 * q

@@ -167,6 +167,7 @@ int main(int argc, char **argv) {
         shots.push_back(std::move(s));
     }
     if (shots.empty()) die("no shot in [minshot, maxshot]");
+    if (par.rbc) die("rbc = 1 (the random boundary) is not provided");
     for (auto &s : shots) {  // pointers into the vectors, which no longer move
         s.d.gc = s.gc.data();
         s.d.rec_z = s.rz.data();
@@ -183,6 +184,10 @@ int main(int argc, char **argv) {
     check(sfwi_set_misfit(h, misfit_kind), "misfit");
     if (snap_k > 0) check(sfwi_set_snapshots(h, snap_k, snap_fmt), "snapshots");
     check(sfwi_set_source(h, source), "source");
+    // the parameter file's cpu_mem keeps the edge strips in host memory in
+    // chunks of iointerval steps, the chunk length the reference's driver
+    // passes to IMAGE_SINGLESHOT as ntt (sfwi-stage1/main.cpp:631)
+    if (par.cpu_mem) check(sfwi_set_cpu_mem(h, 1, par.iointerval), "cpu_mem");
 
     std::vector<float> grad_pp(n), grad_ps(n), illum(n), cg_pp(n), cg_ps(n), cg_pp_old(n, 0.f), cg_ps_old(n, 0.f);
     std::vector<float> image_pp(n, 0.f), image_ps(n, 0.f);  // stage 2: model perturbation

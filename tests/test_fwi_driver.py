@@ -126,3 +126,30 @@ def test_gradient_only_writes_one_gradient_and_no_model(tmp_path):
         g = np.fromfile(os.path.join(s["out"], "%s_0_%d_%d.dat" % ((name,) + shape)), np.float32)
         assert g.size == shape[0] * shape[1] and np.all(np.isfinite(g)) and np.abs(g).max() > 0, name
     assert not os.path.exists(os.path.join(s["out"], "vel_p_1_%d_%d.dat" % shape))
+
+
+def test_driver_with_host_strips_gives_the_same_files(tmp_path):
+    """cpu_mem = 1 with iointerval = 50 steps (the reference driver's ntt):
+    the edge strips live in host memory and every file the driver writes is
+    the same bit for bit; rbc = 1 is refused"""
+    from sfwi_gb300 import su
+    s = _survey(tmp_path)
+    txt = open(s["para"]).read()
+    outs = []
+    for k, flags in enumerate(("1 0 0 1000", "1 0 1 50")):
+        out = s["out"] + str(k)
+        open(s["para"], "w").write(txt.replace("1 0 0 1000", flags).replace(s["out"], out))
+        r = subprocess.run([su.DRIVER, s["para"], "--stage", "1", "--iters", "1"], capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        outs.append(out)
+    names = sorted(f for f in os.listdir(outs[0]) if f.endswith(".dat"))
+    assert names
+    for f in names:
+        a = np.fromfile(os.path.join(outs[0], f), np.float32)
+        b = np.fromfile(os.path.join(outs[1], f), np.float32)
+        assert np.array_equal(a, b), f
+    open(s["para"], "w").write(txt.replace("1 0 0 1000", "1 1 0 1000"))
+    r = subprocess.run([su.DRIVER, s["para"], "--stage", "1", "--iters", "1"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode != 0 and "random boundary" in r.stderr

@@ -190,13 +190,13 @@ class Server:
     HBM budget free up.  policy "oldest" admits in arrival order, letting a
     later request that fits overtake one that does not; "shortest" admits the
     request with the least work first (request_work); with max_active=1 the
-    loop is the plain FIFO.
+    loop is the plain FIFO.  Requests are admitted once the oldest waiting
+    request has waited `window` seconds (or no request is still due), so
+    that requests arriving close together are ordered (and, batched, run)
+    together.
 
     Batched (batch=True): the requests admitted together share one run, at
-    most max_batch of them; a run forms once the oldest waiting request has
-    waited `window` seconds (or no request is still due), so requests that
-    arrive close together can share it and the shortest-first order sees
-    them all.  strip_chunk > 0 keeps every run's edge strips in host memory
+    most max_batch of them.  strip_chunk > 0 keeps every run's edge strips in host memory
     in chunks of that many steps (sfwi_set_cpu_mem): the budget then counts
     the device ring only, and more requests fit at once.  During run() the
     pinned blocks that finished engines release are kept (up to
@@ -272,12 +272,16 @@ class Server:
                 while nxt < len(reqs) and reqs[nxt].arrival <= t:
                     waiting.append(reqs[nxt])
                     nxt += 1
-                # admit every arrived request that fits, oldest or least work first
+                # admit every arrived request that fits, oldest or least work first,
+                # once the oldest waiting one has waited `window` seconds (or
+                # no request is still due)
                 order = list(waiting) if self.policy == "oldest" else sorted(waiting, key=lambda q: (self.work(q), q.rid))
+                due = bool(waiting) and (nxt >= len(reqs) or t - min(q.arrival for q in waiting) >= self.window)
+                if not due:
+                    order = []
                 if self.batch:
                     # one shared run of every waiting request that fits the budget
-                    due = bool(waiting) and (nxt >= len(reqs) or t - min(q.arrival for q in waiting) >= self.window)
-                    if state["active"] < self.max_active and order and due:
+                    if state["active"] < self.max_active and order:
                         group, size = [], 0
                         for r in order:
                             if len(group) >= self.max_batch:
@@ -311,7 +315,7 @@ class Server:
                 if errors:
                     break
                 timeout = None if nxt >= len(reqs) else max(0.0, reqs[nxt].arrival - now())
-                if self.batch and waiting and state["active"] < self.max_active and nxt < len(reqs):
+                if self.window > 0 and waiting and state["active"] < self.max_active and nxt < len(reqs):
                     # wake when the oldest waiting request's window closes
                     dl = max(0.0, min(q.arrival for q in waiting) + self.window - now())
                     timeout = dl if timeout is None else min(timeout, dl)

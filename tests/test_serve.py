@@ -150,6 +150,20 @@ def test_batching_window_collects_requests_arriving_close_together():
     assert 0.06 <= res[0].admitted < 0.1
 
 
+def test_window_lets_shortest_first_see_requests_arriving_together():
+    # one engine at a time: without a window the first arrival (the largest)
+    # starts alone; with a window covering the arrivals the least work goes first
+    reqs = _fake_requests([50, 10, 40, 20, 30], [0.0, 0.005, 0.01, 0.015, 0.02])
+    rec = Recorder(0.02)
+    serve.Server(1000, max_active=1, runner=rec, sizer=lambda r: r.size, policy="shortest",
+                 work=lambda r: r.size).run(reqs)
+    assert rec.order[0] == 0
+    rec = Recorder(0.02)
+    serve.Server(1000, max_active=1, runner=rec, sizer=lambda r: r.size, policy="shortest", work=lambda r: r.size,
+                 window=0.05).run(reqs)
+    assert rec.order == [1, 3, 4, 2, 0]
+
+
 def test_batched_shortest_first_takes_the_least_work_into_the_first_runs():
     # sizes double as work: with a window covering every arrival the runs
     # are the two smallest, then the next two, then the largest

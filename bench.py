@@ -265,14 +265,15 @@ def reference_gpu_sample(w, data, nshots, warm=True):
                       "wall clock per shot"}
 
 
-def run_serving(n, budget_gb=64.0, slots=4, full=True):
+def run_serving(n, budget_gb=64.0, full=True):
     """Serving loop on a seeded Poisson stream (50 requests/s; grids 200x100
     to 2001x1001, nt 2000-6000 and 1-8 shots drawn per request; with
     full=False scaled by 0.3 in each grid dimension and 0.1 in nt).  Four
     servers on the same stream, each replayed once after one warm request:
       fifo                   one request at a time in arrival order;
-      served_shortest_first  up to `slots` requests at once, each on its own
-                             engine and stream, least work first;
+      served_shortest_first  two requests at once, each on its own engine and
+                             stream, least work first, admitted once the
+                             oldest waiting request has waited 0.3 s;
       batched                the requests admitted together share one engine
                              run (sfwi_run_models), two runs in flight;
       batched_shortest_first as batched, but a run forms once the oldest
@@ -282,23 +283,26 @@ def run_serving(n, budget_gb=64.0, slots=4, full=True):
                              served_shortest_first in an 8 GB budget, the
                              edge strips in pinned host memory (100-step
                              chunks; pinned blocks reused across engines).
+    FIFO is replayed first and last (the line reports the first; `fifo_last`
+    shows the drift between replays on the same box).
     At the drawn sizes a request takes up to several seconds of GPU time, so
     a stream at 50/s queues: the latencies measure the backlog."""
     from sfwi_gb300 import serve
     gs, ns = (1.0, 1.0) if full else (0.3, 0.1)
     reqs = serve.poisson_requests(n, 50.0, seed=4, grid_scale=gs, nt_scale=ns)
     serve.run_request(reqs[0])  # warm the kernels and the allocator
-    out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb, "slots": slots,
+    out = {"requests": n, "rate_per_s": 50.0, "budget_gb": budget_gb,
            "shot_gradients": sum(r.shot_gradients for r in reqs),
            "scale": "the drawn sizes" if full else "grids x0.3 per dimension, nt x0.1 of the drawn sizes"}
     B = budget_gb * 2 ** 30
     for name, srv in (("fifo", serve.Server(B, max_active=1)),
-                      ("served_shortest_first", serve.Server(B, max_active=slots, policy="shortest")),
+                      ("served_shortest_first", serve.Server(B, max_active=2, policy="shortest", window=0.3)),
                       ("batched", serve.Server(B, max_active=2, batch=True)),
                       ("batched_shortest_first", serve.Server(B, max_active=2, batch=True, policy="shortest",
                                                               max_batch=4, window=0.3)),
                       ("served_shortest_first_host_strips_8gb",
-                       serve.Server(min(B, 8 << 30), max_active=slots, policy="shortest", strip_chunk=100))):
+                       serve.Server(min(B, 8 << 30), max_active=2, policy="shortest", window=0.3, strip_chunk=100)),
+                      ("fifo_last", serve.Server(B, max_active=1))):
         if not full:
             srv.run(reqs)  # short requests: a first replay settles the allocator pools and host threads
         res = srv.run(reqs)

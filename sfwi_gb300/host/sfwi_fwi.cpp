@@ -1,7 +1,7 @@
 // sfwi_fwi.cpp — the stage-1 and stage-2 inversion drivers on one GPU.
 //
 //   sfwi_fwi <para_file> [--stage 1|2] [--iters N] [--misfit l2|ot|ot_power|ot_alltrace]
-//            [--snapshots K f32|f16|bf16] [--source txx_tzz|vz] [--gradient-only]
+//            [--snapshots K f32|f16|bf16] [--source txx_tzz|vz] [--gradient-only] [--resume]
 //
 // The reference runs these as MPI programs (sfwi-stage1/main.cpp,
 // sfwi-stage2/main.cpp): a master hands shots to one worker per GPU, each
@@ -23,6 +23,13 @@
 //   cg = 0; beta_num = sum(grad^2 / illumination); cg += beta cg_old;
 //   alpha = fenzi / fenmu (CALCULATE_ALPHA); image -= alpha cg.
 // Output files (float32 [allnx][allnz]) carry the reference's names.
+//
+// Checkpoints: after each iteration the driver also writes state.bin, the
+// whole state the next iteration starts from (the model or the model
+// perturbation, the previous CG direction, the CG denominator and the first
+// misfit).  With --resume it continues from that file, and every later file
+// equals an uninterrupted run's bit for bit.  The reference's drivers can
+// only restart from a dumped model, without the CG state.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -88,6 +95,37 @@ struct Shot {
     std::vector<float> rz, rx;
 };
 
+// state.bin: a fixed header, then four float32 [allnx][allnz] arrays: the
+// model (vp, vs; stage 1) or the perturbation (image_pp, image_ps; stage 2),
+// then the previous CG direction (pp, ps)
+struct StateHeader {
+    char magic[8];
+    int version, stage, next_iter, allnx, allnz, pad;
+    double beta_fenmu, max_misfit;
+};
+constexpr char kStateMagic[8] = {'S', 'F', 'W', 'I', 'S', 'T', 'A', 'T'};
+
+void write_state(const std::string &dir, const StateHeader &hdr, const std::vector<const float *> &arrays, size_t n) {
+    const std::string tmp = dir + "/state.bin.tmp", path = dir + "/state.bin";
+    FILE *f = std::fopen(tmp.c_str(), "wb");
+    if (!f) die("cannot write the checkpoint");
+    bool ok = std::fwrite(&hdr, sizeof hdr, 1, f) == 1;
+    for (const float *a : arrays) ok = ok && std::fwrite(a, sizeof(float), n, f) == n;
+    ok = std::fclose(f) == 0 && ok;
+    // the old checkpoint stays whole until the new one is complete
+    if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) die("cannot write the checkpoint");
+}
+
+bool read_state(const std::string &dir, StateHeader *hdr, const std::vector<float *> &arrays, size_t n) {
+    FILE *f = std::fopen((dir + "/state.bin").c_str(), "rb");
+    if (!f) return false;
+    bool ok = std::fread(hdr, sizeof *hdr, 1, f) == 1 && std::memcmp(hdr->magic, kStateMagic, 8) == 0 &&
+              hdr->version == 1;
+    for (float *a : arrays) ok = ok && std::fread(a, sizeof(float), n, f) == n;
+    std::fclose(f);
+    return ok;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -95,7 +133,7 @@ int main(int argc, char **argv) {
                       "[--snapshots K f32|f16|bf16] [--source txx_tzz|vz] [--gradient-only]");
     int stage = 1, iters = -1, misfit_kind = SFWI_MISFIT_L2, snap_k = 0, snap_fmt = SFWI_SNAP_F16;
     int source = SFWI_SOURCE_TXX_TZZ;
-    bool gradient_only = false;
+    bool gradient_only = false, resume = false;
     for (int i = 2; i < argc; i++) {
         if (!std::strcmp(argv[i], "--stage") && i + 1 < argc)
             stage = std::atoi(argv[++i]);
@@ -121,6 +159,8 @@ int main(int argc, char **argv) {
                 die("--source must be txx_tzz or vz");
         } else if (!std::strcmp(argv[i], "--gradient-only"))
             gradient_only = true;
+        else if (!std::strcmp(argv[i], "--resume"))
+            resume = true;
         else
             die("unknown argument");
     }
@@ -196,8 +236,23 @@ int main(int argc, char **argv) {
     auto enqueue_all = [&]() {
         for (auto &s : shots) check(sfwi_enqueue_shot(h, &s.d), "enqueue");
     };
+    // the state an iteration leaves for the next: stage 1 updates the model,
+    // stage 2 the perturbation; both carry the CG direction and denominator
+    float *model_a = stage == 1 ? vp.data() : image_pp.data(), *model_b = stage == 1 ? vs.data() : image_ps.data();
+    int first_iter = 0;
+    if (resume) {
+        StateHeader hdr{};
+        if (!read_state(out, &hdr, {model_a, model_b, cg_pp_old.data(), cg_ps_old.data()}, n))
+            die("--resume: no readable state.bin in the output directory");
+        if (hdr.stage != stage || hdr.allnx != allnx || hdr.allnz != allnz)
+            die("--resume: state.bin is of another stage or grid");
+        first_iter = hdr.next_iter;
+        beta_fenmu = hdr.beta_fenmu;
+        max_misfit = hdr.max_misfit;
+        std::printf("resuming at iteration %d\n", first_iter);
+    }
 
-    for (int iter = 0; iter < std::max(maxiter, gradient_only ? 1 : 0); iter++) {
+    for (int iter = first_iter; iter < std::max(maxiter, gradient_only ? 1 : 0); iter++) {
         if (stage == 1) {
             check(sfwi_gpu_buffer_vpvs(h, vp.data(), vs.data(), rho.data()), "model");
         } else {
@@ -273,6 +328,16 @@ int main(int argc, char **argv) {
             write_model(out, "sum_image_pp", iter, allnx, allnz, image_pp.data());
             write_model(out, "sum_image_ps", iter, allnx, allnz, image_ps.data());
         }
+        StateHeader hdr{};
+        std::memcpy(hdr.magic, kStateMagic, 8);
+        hdr.version = 1;
+        hdr.stage = stage;
+        hdr.next_iter = iter + 1;
+        hdr.allnx = allnx;
+        hdr.allnz = allnz;
+        hdr.beta_fenmu = beta_fenmu;
+        hdr.max_misfit = max_misfit;
+        write_state(out, hdr, {model_a, model_b, cg_pp_old.data(), cg_ps_old.data()}, n);
     }
     sfwi_destroy(h);
     return 0;

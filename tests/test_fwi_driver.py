@@ -153,3 +153,37 @@ def test_driver_with_host_strips_gives_the_same_files(tmp_path):
     r = subprocess.run([su.DRIVER, s["para"], "--stage", "1", "--iters", "1"], capture_output=True, text=True,
                        timeout=600)
     assert r.returncode != 0 and "random boundary" in r.stderr
+
+
+@pytest.mark.parametrize("stage", [1, 2])
+def test_resume_from_the_checkpoint_equals_an_uninterrupted_run(tmp_path, stage):
+    """Two iterations straight, against one iteration, then --resume to two:
+    the second iteration's files are the same bit for bit (the checkpoint
+    carries the model or perturbation, the CG direction and denominator)"""
+    from sfwi_gb300 import su
+    s = _survey(tmp_path)
+    txt = open(s["para"]).read()
+
+    def run(out, iters, resume=False):
+        open(s["para"], "w").write(txt.replace(s["out"], out))
+        cmd = [su.DRIVER, s["para"], "--stage", str(stage), "--iters", str(iters)] + (["--resume"] if resume else [])
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        return r.stdout
+
+    a, b = s["out"] + "a", s["out"] + "b"
+    run(a, 2)
+    run(b, 1)
+    assert "resuming at iteration 1" in run(b, 2, resume=True)
+    names = sorted(f for f in os.listdir(a) if f.endswith(".dat") and "_1_" in f)
+    assert len(names) >= 4
+    for f in names:
+        assert np.array_equal(np.fromfile(os.path.join(a, f), np.float32), np.fromfile(os.path.join(b, f), np.float32)), f
+    # a checkpoint of the other stage is refused
+    other = s["out"] + "c"
+    os.makedirs(other)
+    os.replace(os.path.join(b, "state.bin"), os.path.join(other, "state.bin"))
+    open(s["para"], "w").write(txt.replace(s["out"], other))
+    r = subprocess.run([su.DRIVER, s["para"], "--stage", str(3 - stage), "--iters", "3", "--resume"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and "another stage" in r.stderr

@@ -79,3 +79,16 @@ def test_ot_rejects_bad_arguments(lib):
 def test_null_handle_is_an_error(lib):
     assert lib.sfwi_image_singleshot(None, None) == -1
     assert lib.sfwi_destroy(None) == 0
+
+
+def test_pinned_cache_limit_needs_no_device(lib):
+    """sfwi_set_pinned_cache only sets a host-side limit (and frees cached
+    blocks above it): callable without a GPU"""
+    assert lib.sfwi_set_pinned_cache(1 << 30) == 0
+    assert lib.sfwi_set_pinned_cache(0) == 0
+
+
+def test_handle_calls_refuse_a_null_handle(lib):
+    for rc in (lib.sfwi_set_cpu_mem(None, 1, 10), lib.sfwi_strip_bytes(None, None, None),
+               lib.sfwi_hessian_vector(None, None, None, None, None)):
+        assert rc != 0

@@ -16,6 +16,11 @@
 //             res_i = (1/2) (A_i - sum_j f_j A_j) / sum p(cal) * p'(cal_i)
 // res is (1/2) dW/dcal, the scaling of the L2 residual (misfit sum r^2,
 // adjoint source r).  The CDFs, the quantile search and every sum are FP64.
+// The exponential weights are FP32 (expf of the argument rounded to FP32,
+// then widened): their argument is at most 0, so a weight is 1 at the
+// trace's maximum and its relative rounding of about 1e-7 stays far below
+// the 1e-4 parity bar, while a double exp would be most of the kernel's
+// FP64 work.
 // One CTA handles one (trace, component); prefix and suffix sums are block
 // scans built on warp shuffles.
 #include <cfloat>
@@ -186,8 +191,8 @@ __global__ void __launch_bounds__(OT_THREADS) k_ot(OtArgs a) {
     }
     const double cmax = block_max(mc, wsum), omax = block_max(mo, wsum);
     const double eps = 1e-3 * sigma * sigma;
-    auto pf = [&](double u) { return pw ? u * u + eps : exp((u - cmax) * inv_sigma); };
-    auto pg = [&](double u) { return pw ? u * u + eps : exp((u - omax) * inv_sigma); };
+    auto pf = [&](double u) { return pw ? u * u + eps : (double)expf((float)((u - cmax) * inv_sigma)); };
+    auto pg = [&](double u) { return pw ? u * u + eps : (double)expf((float)((u - omax) * inv_sigma)); };
 
     double sf = 0.0, sg = 0.0;
     for (int k = k0; k < k1; k++) {

@@ -532,6 +532,8 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, rank=0, clocks=N
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": round(tpc * cells) if tpc else None,
                 "traffic_note": "DRAM bytes per launch: ncu capture of a 16-shot launch scaled by cells",
+                # the DRAM side of the same launch: measured bytes over the event time
+                "dram_achieved": round(tpc * cells / (kt[dom] / 1000.0) / 1e9, 1) if tpc else None,
                 "alg_bytes_per_launch": kbytes[dom] * cells, "peak_source": peak_kind,
                 "launch_ms": round(kt[dom], 5), "all_kernels_ms": {k: round(v, 5) for k, v in kt.items()},
                 "all_kernels_frac": fracs}

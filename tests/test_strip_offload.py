@@ -152,3 +152,50 @@ def test_reused_pinned_blocks_give_the_same_results(survey):
         sg.set_pinned_cache(0)
     for stage, r in runs:
         _same_run(r, base1 if stage == 1 else base2)
+
+
+@pytest.mark.parametrize("tile", ["8x32c2s3", "32x32"])
+def test_host_strips_on_other_tile_shapes(survey, tile):
+    """the ring is addressed by step, not by tile: other tile shapes give the
+    same bits with the strips in host memory"""
+    def run(cpu_mem):
+        fd = _handle(2)
+        fd.GPUbufferVPVS(survey["vp0"], survey["vs0"])
+        fd.GPUbufferM(survey["dvp"], survey["dvs"])
+        fd.set_tile_shape(tile)
+        fd.set_cpu_mem(cpu_mem, 17)
+        for d in survey["shots"]:
+            fd.enqueue_shot(d["nx"], d["isx"], PML + 2, PML, d["ngx_left"], d["delta_left"], 0, d["gc"],
+                            d["obs_z"], d["obs_x"])
+        _, per = fd.run(len(survey["shots"]))
+        g = fd.read_gradients_f64()
+        fd.close()
+        return per, g
+    a, b = run(0), run(1)
+    assert np.array_equal(a[0], b[0])
+    for x, y in zip(a[1], b[1]):
+        assert np.array_equal(x, y)
+
+
+def test_host_strips_leave_snapshot_runs_alone(survey):
+    """snapshot runs keep no strips: cpu_mem changes nothing and reports no
+    strip bytes"""
+    def run(cpu_mem):
+        fd = _handle(2)
+        fd.GPUbufferVPVS(survey["vp0"], survey["vs0"])
+        fd.GPUbufferM(survey["dvp"], survey["dvs"])
+        fd.set_snapshots(4, "f16")
+        fd.set_cpu_mem(cpu_mem, 17)
+        for d in survey["shots"]:
+            fd.enqueue_shot(d["nx"], d["isx"], PML + 2, PML, d["ngx_left"], d["delta_left"], 0, d["gc"],
+                            d["obs_z"], d["obs_x"])
+        _, per = fd.run(len(survey["shots"]))
+        g = fd.read_gradients_f64()
+        sb = fd.strip_bytes()
+        fd.close()
+        return per, g, sb
+    a, b = run(0), run(1)
+    assert np.array_equal(a[0], b[0])
+    for x, y in zip(a[1], b[1]):
+        assert np.array_equal(x, y)
+    assert a[2] == (0, 0) and b[2] == (0, 0)

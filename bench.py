@@ -433,6 +433,8 @@ def measure(w, args, steps, warmup, plain_shots, pg=None, ws=1, rank=0, clocks=N
         fd.GPUbufferVPVS(data["vp0"], data["vs0"], data["rho0"])
     if w.get("source") == "vz":
         fd.set_source(sg.SOURCE_VZ_FORCE)
+    if getattr(args, "tile_order", None) is not None:
+        fd.set_tile_order(args.tile_order)
     if w["misfit"] == "OT":
         fd.set_misfit(sg.MISFIT_OT)
     if w.get("snap"):
@@ -644,6 +646,8 @@ def main():
     ap.add_argument("--extra-workloads", default="salt401,shot376,snap2001",
                     help="workloads measured after the main one and reported as sub-records (comma list; '' for none)")
     ap.add_argument("--extra-steps", type=int, default=3, help="timed steps of each extra workload")
+    ap.add_argument("--tile-order", type=int, default=None,
+                    help="reverse-order bits of the four step kernels' tile draws (default: the engine's)")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.nt:

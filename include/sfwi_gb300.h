@@ -156,6 +156,8 @@ typedef struct {
 
 /* queue a shot; its arrays must stay valid until sfwi_run returns */
 int sfwi_enqueue_shot(sfwi_handle *h, const sfwi_shot_desc *shot);
+/* drop the queued shots without running them */
+int sfwi_clear_queue(sfwi_handle *h);
 /* advance every queued shot together (forward, residual, backward, imaging)
  * and clear the queue; misfit += the sum over the shots (in queue order);
  * per_shot_misfit (may be NULL) receives each shot's misfit. */
@@ -356,6 +358,12 @@ int sfwi_set_tile_shape(sfwi_handle *h, int shape);
  * results on the device, which hides the launch gap between the sweeps.
  * Results do not depend on it. */
 int sfwi_set_launch_overlap(sfwi_handle *h, int on);
+/* Tile order of the time-step sweeps: bit k set (k = 0 forward velocity, 1
+ * forward stress, 2 backward stress, 3 backward velocity sweep) draws that
+ * sweep's tiles in reverse table order.  The default, bits 1 and 3, makes
+ * each sweep start where the one before it ended (its freshest outputs are
+ * still in L2).  Results do not depend on it. */
+int sfwi_set_tile_order(sfwi_handle *h, unsigned reverse_bits);
 int sfwi_get_tile_shape(sfwi_handle *h, int *shape, int *tx, int *tz);
 
 /* Autotuner: after a gradient run (sfwi_run or sfwi_image_singleshot), time one

@@ -71,6 +71,7 @@ class FD2DGPU_ELASTIC:
         self.isx = self.isz = self.igz = 0
         self.ngx_left = self.delta_left = self.record_left_in_v = 0
         self._keep = []
+        self._lens = []  # record length of each queued shot
 
     # -- lifetime --
     def close(self):
@@ -180,6 +181,16 @@ class FD2DGPU_ELASTIC:
         return out
 
     # -- batched shots --
+    def _plain_lengths(self):
+        """the runs of the handle's own model read [ntr, nt] records of every
+        queued shot: a shot queued with another length (for run_models) is
+        refused, and the queue dropped"""
+        if any(n != self.nt for n in self._lens):
+            _lib.load().sfwi_clear_queue(self._h)
+            self._keep, self._lens = [], []
+            raise SfwiError("a queued shot's records are not [ntr, %d]: shots of other lengths run through "
+                            "run_models" % self.nt)
+
     def enqueue_shot(self, nx, isx, isz, igz, ngx_left, delta_left, record_left_in_v, gc, rec_z=None, rec_x=None,
                      nt=None):
         """Queue a shot; records are [ntr, nt] (nt: the handle's, or the
@@ -190,6 +201,7 @@ class FD2DGPU_ELASTIC:
         rz = _f32(rec_z if rec_z is not None else np.zeros((ntr, n), np.float32), (ntr, n))
         rx = _f32(rec_x if rec_x is not None else np.zeros((ntr, n), np.float32), (ntr, n))
         self._keep += [g, rz, rx]  # must outlive run()
+        self._lens.append(n)
         d = ShotDesc(nx=nx, isx=isx, isz=isz, igz=igz, ngx_left=ngx_left, delta_left=delta_left,
                      record_left_in_v=record_left_in_v, ntr=ntr, gc=_ip(g), rec_z=_fp(rz), rec_x=_fp(rx))
         _lib.check(_lib.load().sfwi_enqueue_shot(self._h, C.byref(d)))
@@ -199,10 +211,11 @@ class FD2DGPU_ELASTIC:
         n = nshots if nshots is not None else len(self._keep) // 3
         per = np.zeros(max(n, 1), np.float64)
         m = C.c_double(0.0)
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_run(self._h, C.byref(m), per.ctypes.data_as(C.POINTER(C.c_double))))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         return m.value, per[:n]
 
     def born_adjoint(self):
@@ -211,10 +224,11 @@ class FD2DGPU_ELASTIC:
         shp = (self.allnx, self.allnz)
         ip, isv = np.zeros(shp, np.float64), np.zeros(shp, np.float64)
         dp = C.POINTER(C.c_double)
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_born_adjoint(self._h, ip.ctypes.data_as(dp), isv.ctypes.data_as(dp)))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         return ip, isv
 
     def hessian_vector(self, dvp, dvs):
@@ -225,11 +239,12 @@ class FD2DGPU_ELASTIC:
         dvp, dvs = _f32(dvp, shp), _f32(dvs, shp)
         hp, hs = np.zeros(shp, np.float64), np.zeros(shp, np.float64)
         dp = C.POINTER(C.c_double)
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_hessian_vector(self._h, _fp(dvp), _fp(dvs), hp.ctypes.data_as(dp),
                                                        hs.ctypes.data_as(dp)))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         return hp, hs
 
     def run_models(self, models, shot_model):
@@ -261,7 +276,7 @@ class FD2DGPU_ELASTIC:
             _lib.check(_lib.load().sfwi_run_models(self._h, len(models), descs, _ip(sm), per.ctypes.data_as(dp),
                                                    *[a.ctypes.data_as(dp) for a in g]))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         out, o = [], 0
         for allnx, allnz in sizes:
             k = allnx * allnz
@@ -293,11 +308,12 @@ class FD2DGPU_ELASTIC:
         m = np.zeros(3, np.float64)
         per = np.zeros((max(n, 1), 3), np.float64)
         dp = C.POINTER(C.c_double)
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_line_search_parabola(self._h, _fp(g1), _fp(g2), float(step1), float(step2),
                                                              m.ctypes.data_as(dp), per.ctypes.data_as(dp)))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         return m, per[:n]
 
     def line_search_exact(self, image_pp, image_ps, cg_pp, cg_ps, nshots=None):
@@ -306,18 +322,20 @@ class FD2DGPU_ELASTIC:
         arrs = [_f32(a) for a in (image_pp, image_ps, cg_pp, cg_ps)]
         zi, mu = C.c_double(0.0), C.c_double(0.0)
         per = np.zeros((max(n, 1), 2), np.float64)
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_line_search_exact(self._h, *[_fp(a) for a in arrs], C.byref(zi), C.byref(mu),
                                                           per.ctypes.data_as(C.POINTER(C.c_double))))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
         return zi.value, mu.value, per[:n]
 
     def run_forward(self):
+        self._plain_lengths()
         try:
             _lib.check(_lib.load().sfwi_run_forward(self._h))
         finally:
-            self._keep = []
+            self._keep, self._lens = [], []
 
     def time_kernels(self, reps=20):
         """Average launch duration (ms) of each time-step kernel on the last
@@ -362,6 +380,12 @@ class FD2DGPU_ELASTIC:
     def set_launch_overlap(self, on=True):
         """Programmatic dependent launch of the time-step kernels (default on)."""
         _lib.check(_lib.load().sfwi_set_launch_overlap(self._h, int(bool(on))))
+
+    def set_tile_order(self, reverse_bits):
+        """Bit k: time-step sweep k (forward velocity, forward stress,
+        backward stress, backward velocity) draws its tiles in reverse table
+        order (default 0b1010).  Results do not depend on it."""
+        _lib.check(_lib.load().sfwi_set_tile_order(self._h, int(reverse_bits)))
 
     def tile_shape(self):
         """Name of the current tile shape (TILE_SHAPES)."""

@@ -68,6 +68,8 @@ SIGNATURES = {
     "sfwi_time_kernels": (C.c_int, [_h, C.c_int, _fp]),
     "sfwi_set_tile_shape": (C.c_int, [_h, C.c_int]),
     "sfwi_set_launch_overlap": (C.c_int, [_h, C.c_int]),
+    "sfwi_set_tile_order": (C.c_int, [_h, C.c_uint]),
+    "sfwi_clear_queue": (C.c_int, [_h]),
     "sfwi_set_source": (C.c_int, [_h, C.c_int]),
     "sfwi_wait_selftest": (C.c_int, [_h, C.c_uint]),
     "sfwi_debug_grid_shape": (C.c_int, [_h, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),

@@ -275,6 +275,7 @@ struct sfwi_handle {
     float fwd_ms = 0, bwd_ms = 0, other_ms = 0, total_ms = 0;
     bool use_graphs = true;
     bool launch_overlap = true;  // programmatic dependent launch of the step kernels
+    unsigned tile_order = kReverseTiles;  // bit k: step kernel k draws its tiles in reverse order
     int src_kind = SRC_TXX_TZZ;  // source: the reference's txx+tzz, or a vertical force
     bool last_forward_only = false;
     const TileVariant *tv = nullptr;  // tile shape of the step kernels
@@ -699,7 +700,7 @@ Params make_params(sfwi_handle *h, bool forward_only) {
     Params p{};
     p.overlap = h->launch_overlap ? 1 : 0;
     p.wait_limit = PIPE_WAIT_LIMIT;
-    p.reverse_tiles = kReverseTiles;
+    p.reverse_tiles = h->tile_order;
     p.src_kind = h->src_kind;
     p.X = b.X;
     p.P = b.P;
@@ -924,7 +925,7 @@ struct ObservedGuard {
 std::vector<long long> shape_signature(sfwi_handle *h, bool forward_only) {
     Batch &b = h->b;
     std::vector<long long> s = {h->nt, h->stage, forward_only, h->want_rho, h->snap_every, h->snap_fmt,
-                                (long long)(uintptr_t)h->tv, h->launch_overlap, h->src_kind,
+                                (long long)(uintptr_t)h->tv, h->launch_overlap, h->tile_order, h->src_kind,
                                 (long long)(uintptr_t)b.snap.p, (long long)(uintptr_t)b.sscale.p, b.nshots, b.ntiles,
                                 b.X, b.P,
                                 b.ntr_tot, b.rsp, (long long)(uintptr_t)b.grid.p, (long long)(uintptr_t)b.tb.p,
@@ -1945,6 +1946,12 @@ int sfwi_enqueue_shot(sfwi_handle *h, const sfwi_shot_desc *d) {
     return SFWI_OK;
 }
 
+int sfwi_clear_queue(sfwi_handle *h) {
+    if (int rc = check(h)) return rc;
+    h->queue.clear();
+    return SFWI_OK;
+}
+
 int sfwi_run(sfwi_handle *h, double *misfit, double *per_shot_misfit) {
     if (int rc = check(h)) return rc;
     std::vector<ShotIn> q;
@@ -2285,6 +2292,13 @@ int sfwi_set_source(sfwi_handle *h, int kind) {
 int sfwi_set_launch_overlap(sfwi_handle *h, int on) {
     if (int rc = check(h)) return rc;
     h->launch_overlap = on != 0;
+    return SFWI_OK;
+}
+
+int sfwi_set_tile_order(sfwi_handle *h, unsigned reverse_bits) {
+    if (int rc = check(h)) return rc;
+    if (reverse_bits > 15u) return fail(SFWI_E_ARG, "tile order bits must be in 0..15");
+    h->tile_order = reverse_bits;
     return SFWI_OK;
 }
 

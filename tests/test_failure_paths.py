@@ -44,3 +44,21 @@ def test_wait_selftest_needs_a_batch_and_a_sane_bound():
     with pytest.raises(sg.SfwiError, match="tries"):
         fd.wait_selftest(0)
     fd.close()
+
+
+def test_plain_runs_refuse_shots_of_other_lengths():
+    """records queued for run_models with another length are not read as
+    [ntr, nt] by a plain run: the run is refused and the queue dropped"""
+    import sfwi_gb300 as sg
+    shot, inputs, _ = load_case("s1_full")
+    fd = make_engine(shot, inputs)
+    nt = shot["nt"]
+    gc = np.asarray(inputs["gc"], np.int32)
+    fd.enqueue_shot(shot["nx"], shot["isx"], shot["isz"], shot["igz"], shot["ngx_left"], shot["delta_left"], 0, gc,
+                    nt=nt - 5)
+    with pytest.raises(sg.SfwiError, match="run_models"):
+        fd.run()
+    with pytest.raises(sg.SfwiError, match="no shots queued"):
+        fd.run()
+    fd.close()
+

@@ -1,6 +1,7 @@
 """Launch configurations of the step kernels: tile shapes
-(sfwi_set_tile_shape), the autotuner (sfwi_autotune) and programmatic
-dependent launch (sfwi_set_launch_overlap).  Every configuration runs the same
+(sfwi_set_tile_shape), the autotuner (sfwi_autotune), programmatic
+dependent launch (sfwi_set_launch_overlap) and the tile draw order of each
+sweep (sfwi_set_tile_order).  Every configuration runs the same
 per-cell arithmetic in the same order, so its records, residuals and gradients
 equal the default's bit for bit, and each is within the 1e-4 relative L2 of
 the FP64 oracle."""
@@ -154,6 +155,21 @@ def test_launch_overlap_keeps_results(case):
         fd.close()
     for k in KEYS:
         assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+@pytest.mark.parametrize("order", [0, 0b0101, 0b1111])
+def test_tile_orders_keep_results(order):
+    import sfwi_gb300 as sg
+    shot, inputs, _ = load_case("s2_window")
+    base = run_ref_api(shot, inputs)
+    fd = make_engine(shot, inputs)
+    fd.set_tile_order(order)
+    out = run_ref_api(shot, inputs, fd=fd)
+    with pytest.raises(sg.SfwiError, match="0..15"):
+        fd.set_tile_order(16)
+    fd.close()
+    for k in KEYS:
+        assert np.array_equal(out[k], base[k]), k
 
 
 def test_default_shape_follows_the_batch_size():

@@ -764,7 +764,9 @@ struct FwdV {
     static constexpr int NST = BORN ? NSTAGE : deep_stages(STAGE, NSTAGE + 2, 1024);
 };
 
-template <bool BORN>
+// SNAP: the run stores forward snapshots (p.snap set); without them the
+// snapshot code is compiled out
+template <bool BORN, bool SNAP>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_v(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdV<BORN>;
@@ -847,7 +849,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
             v_apply<false>(p, m, p.bg, bg, ib, d, 1.f, ax, bz, dx_, cz);
             if (BORN) v_apply<false>(p, m, p.sc, sc, ib, d, 1.f, sax, sbz, sdx, scz);
         }
-        if (snap_step(p, it) && p.snap_fmt != SNAP_F32) {
+        if (SNAP && snap_step(p, it) && p.snap_fmt != SNAP_F32) {
             // scale of this step's snapshot: max |v| over the shot (the bits of
             // non-negative floats order as unsigned integers)
             float mx = 0.f, mz = 0.f;
@@ -886,7 +888,7 @@ struct FwdS {
     static constexpr int NST = BORN ? NSTAGE : deep_stages(STAGE, NSTAGE + 2, 5120);  // + s_sc
 };
 
-template <bool BORN>
+template <bool BORN, bool SNAP>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_fwd_s(const Params p, const __grid_constant__ TmaMaps tm, int it) {
     using S = FwdS<BORN>;
@@ -981,7 +983,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // snapshot of the background velocity after this step (the staged box
         // holds it): the tile's core cells of this shot's rows and of the
         // row pitch (a tile's last columns can reach past it)
-        if (snap_step(p, it) && m.lx >= 0 && m.lx < c.g.nxpml && m.lz >= 0 && m.lz < p.PS) {
+        if (SNAP && snap_step(p, it) && m.lx >= 0 && m.lx < c.g.nxpml && m.lz >= 0 && m.lz < p.PS) {
             const int k = it / p.snap_every;
             const size_t cell = (size_t)(c.g.row0 + m.lx) * p.PS + m.lz;
             const float *sc = s_sc + 2 * min(c.t.shot, SNAP_MAX_SHOTS - 1);
@@ -1060,7 +1062,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
                 s_apply<false>(p, m, p.sc, sc, lam, mu, dm, 1.f, as, bs_, cs, ds, born);
         }
     };
-    if (snap_step(p, it) && p.snap_fmt != SNAP_F32) {
+    if (SNAP && snap_step(p, it) && p.snap_fmt != SNAP_F32) {
         griddep_wait();  // the scales come from the velocity sweep just before
         load_snap_scales(p, it / p.snap_every, s_sc);
     }
@@ -1705,10 +1707,14 @@ cudaError_t configure_step_kernels() {
     cudaError_t e;
 #define SET_SMEM(K, BYTES) \
     if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(BYTES))) != cudaSuccess) return e;
-    SET_SMEM(k_fwd_v<true>, stage_smem<FwdV<true>>());
-    SET_SMEM(k_fwd_v<false>, stage_smem<FwdV<false>>());
-    SET_SMEM(k_fwd_s<true>, stage_smem<FwdS<true>>());
-    SET_SMEM(k_fwd_s<false>, stage_smem<FwdS<false>>());
+    SET_SMEM((k_fwd_v<true, true>), stage_smem<FwdV<true>>());
+    SET_SMEM((k_fwd_v<false, true>), stage_smem<FwdV<false>>());
+    SET_SMEM((k_fwd_s<true, true>), stage_smem<FwdS<true>>());
+    SET_SMEM((k_fwd_s<false, true>), stage_smem<FwdS<false>>());
+    SET_SMEM((k_fwd_v<true, false>), stage_smem<FwdV<true>>());
+    SET_SMEM((k_fwd_v<false, false>), stage_smem<FwdV<false>>());
+    SET_SMEM((k_fwd_s<true, false>), stage_smem<FwdS<true>>());
+    SET_SMEM((k_fwd_s<false, false>), stage_smem<FwdS<false>>());
     SET_SMEM(k_bwd_s, stage_smem<BwdS>());
     SET_SMEM(k_bwd_v, stage_smem<BwdV>());
     SET_SMEM((k_bwd_s_snap<SNAP_F32, true>), (stage_smem<BwdSSnap<SNAP_F32, true>>()));
@@ -1765,15 +1771,19 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
     switch (which) {
         case 0:
             if (born)
-                launch_step(k_fwd_v<true>, stage_smem<FwdV<true>>(), p, st, tm, it);
+                launch_step(p.snap ? k_fwd_v<true, true> : k_fwd_v<true, false>, stage_smem<FwdV<true>>(), p, st, tm,
+                            it);
             else
-                launch_step(k_fwd_v<false>, stage_smem<FwdV<false>>(), p, st, tm, it);
+                launch_step(p.snap ? k_fwd_v<false, true> : k_fwd_v<false, false>, stage_smem<FwdV<false>>(), p, st,
+                            tm, it);
             break;
         case 1:
             if (born)
-                launch_step(k_fwd_s<true>, stage_smem<FwdS<true>>(), p, st, tm, it);
+                launch_step(p.snap ? k_fwd_s<true, true> : k_fwd_s<true, false>, stage_smem<FwdS<true>>(), p, st, tm,
+                            it);
             else
-                launch_step(k_fwd_s<false>, stage_smem<FwdS<false>>(), p, st, tm, it);
+                launch_step(p.snap ? k_fwd_s<false, true> : k_fwd_s<false, false>, stage_smem<FwdS<false>>(), p, st,
+                            tm, it);
             break;
         case 2:
             if (!p.snap)

@@ -1390,6 +1390,9 @@ struct BwdV {
     static constexpr int NST = NSTAGE;
 };
 
+// RHO: the run accumulates the density kernel (p.grho set); without it the
+// density code is compiled out
+template <bool RHO>
 __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
     k_bwd_v(const Params p, const __grid_constant__ TmaMaps tm, int it, float adj_dir) {
     using S = BwdV;
@@ -1424,7 +1427,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, CTAS_PER_SM)
         // the density accumulator (when requested) is read from global memory
         // here, so that its round trip overlaps the stencils below (it does
         // not alias the arrays they store to)
-        const bool rho_img = p.grho != nullptr && image;
+        const bool rho_img = RHO && p.grho != nullptr && image;
         float gr[CPT];
         if (rho_img) ldc(p.grho + m.gi, gr);
         // everything this thread needs from the stage, then release it
@@ -1716,7 +1719,8 @@ cudaError_t configure_step_kernels() {
     SET_SMEM((k_fwd_s<true, false>), stage_smem<FwdS<true>>());
     SET_SMEM((k_fwd_s<false, false>), stage_smem<FwdS<false>>());
     SET_SMEM(k_bwd_s, stage_smem<BwdS>());
-    SET_SMEM(k_bwd_v, stage_smem<BwdV>());
+    SET_SMEM(k_bwd_v<true>, stage_smem<BwdV>());
+    SET_SMEM(k_bwd_v<false>, stage_smem<BwdV>());
     SET_SMEM((k_bwd_s_snap<SNAP_F32, true>), (stage_smem<BwdSSnap<SNAP_F32, true>>()));
     SET_SMEM((k_bwd_s_snap<SNAP_F16, true>), (stage_smem<BwdSSnap<SNAP_F16, true>>()));
     SET_SMEM((k_bwd_s_snap<SNAP_BF16, true>), (stage_smem<BwdSSnap<SNAP_BF16, true>>()));
@@ -1797,7 +1801,7 @@ void launch_step_kernel(int which, const Params &p, const TmaMaps &tm, int it, b
             break;
         default:
             if (!p.snap)
-                launch_step(k_bwd_v, stage_smem<BwdV>(), p, st, tm, it, adj_dir);
+                launch_step(p.grho ? k_bwd_v<true> : k_bwd_v<false>, stage_smem<BwdV>(), p, st, tm, it, adj_dir);
             else
                 launch_step(k_bwd_v_snap, stage_smem<BwdVSnap>(), p, st, tm, it, adj_dir);
             break;

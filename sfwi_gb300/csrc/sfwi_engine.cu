@@ -553,6 +553,27 @@ void build_tiles(sfwi_handle *h) {
             }
     }
     b.ntiles = (int)b.tiles.size();
+    // Every sweep ends at one end of the table (forward-order sweeps at the
+    // last shots, reversed ones at the first), and its last wave of tiles is
+    // its tail.  A shot's block starts and ends with PML rows, whose tiles
+    // cost about twice an interior tile, so in the shots that make up the
+    // last two waves at either end the interior tiles are moved to that end
+    // (stable, each class in table order).
+    {
+        const long long wave = (long long)h->tv->ctas * std::max(h->nsm, 1);
+        int head = 0, tail = 0;  // shots at the start / end covering two waves
+        for (long long n = 0; head < b.nshots && n < 2 * wave; head++) n += shot_tiles[head];
+        for (long long n = 0; tail < b.nshots && n < 2 * wave; tail++) n += shot_tiles[b.nshots - 1 - tail];
+        if (head + tail <= b.nshots) {
+            auto interior = [](const Tile &t) { return !(t.flags & TILE_FRAME); };
+            auto first = b.tiles.begin();
+            for (int s = 0; s < head; s++) first += shot_tiles[s];
+            std::stable_partition(b.tiles.begin(), first, interior);
+            auto last = b.tiles.end();
+            for (int s = 0; s < tail; s++) last -= shot_tiles[b.nshots - 1 - s];
+            std::stable_partition(last, b.tiles.end(), [&](const Tile &t) { return !interior(t); });
+        }
+    }
     // shots that run fewer steps than the batch come last (non-increasing
     // nt): at step it the tiles of the shots still running are a prefix of
     // the table
